@@ -1,0 +1,724 @@
+// capi.cu -- the library's C ABI (include/calchem_xc.h).
+//
+// Device state lives in a process-wide map keyed by the caller's grid id, guarded by one mutex,
+// as in the reference (crates/calchem-cuda/src/cuda_kernels.cu:6004-6041, 7354-7562).  Every
+// input is validated on the host before anything is enqueued, so malformed uploads are rejected
+// with an error code and never reach a kernel.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "grid_build.h"
+#include "host_prep.h"
+
+namespace cxc {
+cudaError_t launch_fp64(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st);
+cudaError_t launch_reduce(const double* part, int n_batches, double* out, int n_out, cudaStream_t st);
+cudaError_t launch_mirror(double* V, int n, cudaStream_t st);
+size_t fp64_smem_bytes();
+int mixed_supported(int mode);
+size_t mixed_slab_doubles(int max_m);
+int mixed_ctas_per_sm();
+cudaError_t launch_mixed(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st);
+cudaError_t launch_mixed_prepare(const double* P, int n, void* Phl, cudaStream_t st);
+}  // namespace cxc
+
+using namespace cxc;
+
+namespace {
+
+constexpr int kPlanes = 5;
+
+struct Entry {
+  int n_pts = 0, n_ao = 0, n_shells = 0, n_batches = 0, max_m = 0;
+  size_t bytes = 0;
+  bool has_w = false;
+  double sum_m2n = 0, sum_m2 = 0;
+  AoShellGpu* d_shells = nullptr;
+  AoPrimGpu* d_prims = nullptr;
+  AoCompGpu* d_comps = nullptr;
+  double* d_pts = nullptr;  // SoA x | y | z | w, n_pts each
+  BatchDesc* d_batches = nullptr;
+  int* d_cand = nullptr;
+  int* d_cand_loc = nullptr;
+  int* d_bao = nullptr;
+  int* d_order = nullptr;
+  double* d_P = nullptr;
+  double* d_Pb = nullptr;
+  double* d_V = nullptr;
+  double* d_Vb = nullptr;
+  double* d_rg = nullptr;
+  double* d_red = nullptr;
+  double* d_res = nullptr;
+  int* d_counter = nullptr;
+  double* d_slab = nullptr;
+  size_t slab_stride = 0;
+  int n_ctas = 0;
+  void* d_mixed_ws = nullptr;  // split copies of the density for the tensor-core path
+  size_t mixed_slab_stride = 0;
+  double* d_mixed_slab = nullptr;
+  int mixed_ctas = 0;
+  double* h_stage = nullptr;  // pinned: 2 n^2 + 4 doubles
+  cudaStream_t stream = nullptr;
+  int last_launches = 0;
+
+  void free_all() {
+    void* ptrs[] = {d_shells, d_prims, d_comps, d_pts,  d_batches, d_cand,  d_cand_loc, d_bao,   d_order,
+                    d_P,      d_Pb,    d_V,     d_Vb,   d_rg,      d_red,   d_res,      d_counter, d_slab,
+                    d_mixed_ws, d_mixed_slab};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    if (h_stage) cudaFreeHost(h_stage);
+    if (stream) cudaStreamDestroy(stream);
+    *this = Entry();
+  }
+};
+
+struct Built {
+  int n = 0;
+  double* d_xyzw = nullptr;
+  double* d_raw_w = nullptr;
+  int* d_host = nullptr;
+};
+
+std::mutex g_mu;
+std::map<uint64_t, Entry*> g_grids;
+std::map<uint64_t, Built*> g_built;
+int g_sm_count = -1;
+
+bool device_ok() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, 0) != cudaSuccess) return false;
+  if (g_sm_count < 0) g_sm_count = prop.multiProcessorCount;
+  return prop.major == 10 && prop.minor == 3;
+}
+
+bool mul_ok(size_t a, size_t b, size_t* out) {
+  if (a != 0 && b > SIZE_MAX / a) return false;
+  *out = a * b;
+  return true;
+}
+
+template <typename T>
+bool dalloc(T** p, size_t count) {
+  if (count == 0) count = 1;
+  return cudaMalloc((void**)p, count * sizeof(T)) == cudaSuccess;
+}
+
+// Host-side tables derived from a reference-layout upload.
+struct HostPlan {
+  std::vector<BatchDesc> batches;
+  std::vector<int> cand, cand_loc, bao, order;
+  int max_m = 0;
+  double sum_m2n = 0, sum_m2 = 0;
+};
+
+// Validates the reference layout and splits it into <=128-point batches.
+int build_host_plan(const AoShellGpu* sh, int n_shells, int n_prims, const AoCompGpu* co, int n_comps,
+                    const GridPtGpu* pts, int n_pts, const int* co_off, int n_off, const int* cs, int n_cs, int n_ao,
+                    HostPlan& hp) {
+  for (int s = 0; s < n_shells; ++s) {
+    const AoShellGpu& a = sh[s];
+    if (a.n_funcs < 1 || a.n_funcs > 10 || a.n_prims < 1 || a.prim_start < 0 || a.comp_start < 0 ||
+        a.ao_offset < 0 || (long long)a.prim_start + a.n_prims > n_prims ||
+        (long long)a.comp_start + a.n_funcs > n_comps || (long long)a.ao_offset + a.n_funcs > n_ao)
+      return -1;
+    for (int c = 0; c < a.n_funcs; ++c) {
+      const AoCompGpu& q = co[a.comp_start + c];
+      if (q.lx < 0 || q.ly < 0 || q.lz < 0 || q.lx > 3 || q.ly > 3 || q.lz > 3) return -1;
+    }
+  }
+  const int nb = n_off - 1;
+  if (co_off[0] < 0) return -1;
+  for (int b = 0; b < nb; ++b)
+    if (co_off[b + 1] < co_off[b] || co_off[b + 1] > n_cs) return -1;
+  for (int i = 0; i < n_cs; ++i)
+    if (cs[i] < 0 || cs[i] >= n_shells) return -1;
+  // points grouped by non-decreasing batch id
+  int prev = -1;
+  for (int g = 0; g < n_pts; ++g) {
+    const int b = pts[g].batch_id;
+    if (b < 0 || b >= nb || b < prev) return -1;
+    prev = b;
+  }
+  int g = 0;
+  while (g < n_pts) {
+    const int b = pts[g].batch_id;
+    int e = g;
+    while (e < n_pts && pts[e].batch_id == b) ++e;
+    int m = 0;
+    const int c0 = co_off[b], c1 = co_off[b + 1];
+    for (int s0 = g; s0 < e; s0 += kBlockPts) {
+      BatchDesc d{};
+      d.pt_start = s0;
+      d.n_pts = std::min(kBlockPts, e - s0);
+      d.cand_start = (int)hp.cand.size();
+      d.n_cand = c1 - c0;
+      d.ao_start = (int)hp.bao.size();
+      m = 0;
+      for (int c = c0; c < c1; ++c) {
+        const AoShellGpu& a = sh[cs[c]];
+        hp.cand.push_back(cs[c]);
+        hp.cand_loc.push_back(m);
+        for (int k = 0; k < a.n_funcs; ++k) hp.bao.push_back(a.ao_offset + k);
+        m += a.n_funcs;
+      }
+      d.m = m;
+      hp.max_m = std::max(hp.max_m, m);
+      hp.sum_m2n += (double)m * m * d.n_pts;
+      hp.sum_m2 += (double)m * m;
+      hp.batches.push_back(d);
+    }
+    g = e;
+  }
+  const int n = (int)hp.batches.size();
+  hp.order.resize(n);
+  for (int i = 0; i < n; ++i) hp.order[i] = i;
+  std::stable_sort(hp.order.begin(), hp.order.end(), [&](int a, int b) {
+    const double ca = (double)hp.batches[a].m * hp.batches[a].m * hp.batches[a].n_pts;
+    const double cb = (double)hp.batches[b].m * hp.batches[b].m * hp.batches[b].n_pts;
+    return ca > cb;
+  });
+  return 0;
+}
+
+int upload_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
+                const AoCompGpu* h_comps, int n_comps, const GridPtGpu* h_pts, int n_pts, const int* h_off, int n_off,
+                const int* h_cs, int n_cs, int n_ao, uint64_t grid_id, size_t mem_limit, const double* h_w) {
+  if (!h_shells || !h_prims || !h_comps || !h_pts || !h_off || !h_cs || n_shells <= 0 || n_prims <= 0 ||
+      n_comps <= 0 || n_pts <= 0 || n_off <= 1 || n_cs <= 0 || n_ao <= 0 || grid_id == 0)
+    return -1;
+  if (!device_ok()) return -3;
+  auto it = g_grids.find(grid_id);
+  if (it != g_grids.end()) return (it->second->n_pts == n_pts && it->second->n_ao == n_ao) ? 0 : -2;
+  HostPlan hp;
+  const int rc = build_host_plan(h_shells, n_shells, n_prims, h_comps, n_comps, h_pts, n_pts, h_off, n_off, h_cs,
+                                 n_cs, n_ao, hp);
+  if (rc) return rc;
+  const int nb = (int)hp.batches.size();
+  size_t nn;
+  if (!mul_ok((size_t)n_ao, (size_t)n_ao, &nn) || nn > (size_t)1 << 31) return -2;
+  const int m_pad = (hp.max_m + 63) / 64 * 64;
+  const int per_sm = 1;  // FP64 kernel: 202 registers x 256 threads -> one resident CTA per SM
+  const int n_ctas = std::max(1, std::min(nb, g_sm_count * per_sm));
+  const size_t slab_stride = (size_t)kPlanes * m_pad * kBlockPts;
+  const int mixed_ctas = std::max(1, std::min(nb, g_sm_count * mixed_ctas_per_sm()));
+  const size_t mixed_stride = mixed_slab_doubles(hp.max_m);
+  size_t total = 0;
+  total += (size_t)n_shells * sizeof(AoShellGpu) + (size_t)n_prims * sizeof(AoPrimGpu) +
+           (size_t)n_comps * sizeof(AoCompGpu);
+  total += (size_t)n_pts * 4 * sizeof(double);
+  total += (size_t)nb * sizeof(BatchDesc) + (hp.cand.size() * 2 + hp.bao.size() + hp.order.size()) * sizeof(int);
+  total += nn * sizeof(double) * 4;           // P, Pb, V, Vb
+  total += nn * sizeof(float) * 4;            // split density copies (mixed path)
+  total += (size_t)n_pts * 4 * sizeof(double);  // rho / wv staging
+  total += (size_t)nb * 3 * sizeof(double) + 64;
+  total += slab_stride * n_ctas * sizeof(double);
+  total += mixed_stride * mixed_ctas * sizeof(double);
+  if (total > mem_limit) return -3;
+
+  Entry* e = new Entry;
+  e->n_pts = n_pts;
+  e->n_ao = n_ao;
+  e->n_shells = n_shells;
+  e->n_batches = nb;
+  e->max_m = hp.max_m;
+  e->bytes = total;
+  e->sum_m2n = hp.sum_m2n;
+  e->sum_m2 = hp.sum_m2;
+  e->n_ctas = n_ctas;
+  e->slab_stride = slab_stride;
+  e->mixed_ctas = mixed_ctas;
+  e->mixed_slab_stride = mixed_stride;
+  bool ok = dalloc(&e->d_shells, n_shells) && dalloc(&e->d_prims, n_prims) && dalloc(&e->d_comps, n_comps) &&
+            dalloc(&e->d_pts, (size_t)n_pts * 4) && dalloc(&e->d_batches, nb) && dalloc(&e->d_cand, hp.cand.size()) &&
+            dalloc(&e->d_cand_loc, hp.cand_loc.size()) && dalloc(&e->d_bao, hp.bao.size()) &&
+            dalloc(&e->d_order, hp.order.size()) && dalloc(&e->d_P, nn) && dalloc(&e->d_Pb, nn) &&
+            dalloc(&e->d_V, nn) && dalloc(&e->d_Vb, nn) && dalloc(&e->d_rg, (size_t)n_pts * 4) &&
+            dalloc(&e->d_red, (size_t)nb * 3) && dalloc(&e->d_res, 8) && dalloc(&e->d_counter, 4) &&
+            dalloc(&e->d_slab, slab_stride * n_ctas) &&
+            cudaMalloc(&e->d_mixed_ws, nn * sizeof(float) * 4) == cudaSuccess &&
+            dalloc(&e->d_mixed_slab, mixed_stride * mixed_ctas) &&
+            cudaMallocHost((void**)&e->h_stage, (2 * nn + 8) * sizeof(double)) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    e->free_all();
+    delete e;
+    return -4;
+  }
+  std::vector<double> soa((size_t)n_pts * 4, 0.0);
+  for (int g = 0; g < n_pts; ++g) {
+    soa[g] = h_pts[g].x;
+    soa[(size_t)n_pts + g] = h_pts[g].y;
+    soa[2 * (size_t)n_pts + g] = h_pts[g].z;
+    soa[3 * (size_t)n_pts + g] = h_w ? h_w[g] : 0.0;
+  }
+  e->has_w = h_w != nullptr;
+  ok = cudaMemcpy(e->d_shells, h_shells, n_shells * sizeof(AoShellGpu), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(e->d_prims, h_prims, n_prims * sizeof(AoPrimGpu), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(e->d_comps, h_comps, n_comps * sizeof(AoCompGpu), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(e->d_pts, soa.data(), soa.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(e->d_batches, hp.batches.data(), nb * sizeof(BatchDesc), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(e->d_cand, hp.cand.data(), hp.cand.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(e->d_cand_loc, hp.cand_loc.data(), hp.cand_loc.size() * sizeof(int), cudaMemcpyHostToDevice) ==
+           cudaSuccess &&
+       cudaMemcpy(e->d_bao, hp.bao.data(), hp.bao.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(e->d_order, hp.order.data(), hp.order.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    e->free_all();
+    delete e;
+    return -5;
+  }
+  g_grids[grid_id] = e;
+  return 0;
+}
+
+DevGrid dev_grid(const Entry& e) {
+  DevGrid G;
+  G.n_pts = e.n_pts;
+  G.n_ao = e.n_ao;
+  G.n_shells = e.n_shells;
+  G.n_batches = e.n_batches;
+  G.shells = e.d_shells;
+  G.prims = e.d_prims;
+  G.comps = e.d_comps;
+  G.px = e.d_pts;
+  G.py = e.d_pts + e.n_pts;
+  G.pz = e.d_pts + 2 * (size_t)e.n_pts;
+  G.pw = e.d_pts + 3 * (size_t)e.n_pts;
+  G.batches = e.d_batches;
+  G.cand_shells = e.d_cand;
+  G.cand_loc = e.d_cand_loc;
+  G.batch_ao = e.d_bao;
+  G.order = e.d_order;
+  return G;
+}
+
+// Enqueues one evaluation.  Pa/Pb/Va/Vb are device pointers; result gets (exc, n_a[, n_b]).
+int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, const double* Pb, double* Va,
+                 double* Vb, const double* wv, double* rho_out, double* result, cudaStream_t st) {
+  const size_t nn = (size_t)e.n_ao * e.n_ao;
+  int launches = 0;
+  if (mode != kModeRho) {
+    if (cudaMemsetAsync(Va, 0, nn * sizeof(double), st) != cudaSuccess) return -5;
+    if (mode == kModeUks && cudaMemsetAsync(Vb, 0, nn * sizeof(double), st) != cudaSuccess) return -5;
+  }
+  if (cudaMemsetAsync(e.d_counter, 0, sizeof(int), st) != cudaSuccess) return -5;
+  EvalArgs A{};
+  A.mode = mode;
+  A.xc = xc;
+  A.Pa = Pa;
+  A.Pb = Pb;
+  A.Va = Va;
+  A.Vb = Vb;
+  A.rho_out = rho_out;
+  A.wv_in = wv;
+  A.batch_red = e.d_red;
+  A.counter = e.d_counter;
+  A.max_m = e.max_m;
+  const DevGrid G = dev_grid(e);
+  cudaError_t err;
+  if (precision == CALCHEM_XC_MIXED) {
+    if (cudaMemsetAsync(e.d_counter + 1, 0, sizeof(int), st) != cudaSuccess) return -5;
+    if (launch_mixed_prepare(Pa, e.n_ao, e.d_mixed_ws, st) != cudaSuccess) return -5;
+    ++launches;
+    if (mode == kModeUks) {
+      if (launch_mixed_prepare(Pb, e.n_ao, (char*)e.d_mixed_ws + nn * sizeof(float) * 2, st) != cudaSuccess)
+        return -5;
+      ++launches;
+    }
+    A.slab = e.d_mixed_slab;
+    A.slab_stride = e.mixed_slab_stride;
+    A.Pa = (const double*)e.d_mixed_ws;  // the tensor-core kernel reads the split copies
+    err = launch_mixed(G, A, e.mixed_ctas, st);
+  } else {
+    A.slab = e.d_slab;
+    A.slab_stride = e.slab_stride;
+    err = launch_fp64(G, A, e.n_ctas, st);
+  }
+  if (err != cudaSuccess) return -5;
+  ++launches;
+  if (mode == kModeRks || mode == kModeUks) {
+    if (launch_reduce(e.d_red, e.n_batches, result, mode == kModeRks ? 2 : 3, st) != cudaSuccess) return -5;
+    if (launch_mirror(Va, e.n_ao, st) != cudaSuccess) return -5;
+    launches += 2;
+    if (mode == kModeUks) {
+      if (launch_mirror(Vb, e.n_ao, st) != cudaSuccess) return -5;
+      ++launches;
+    }
+  }
+  e.last_launches = launches;
+  return 0;
+}
+
+bool valid_xc(int xc) { return xc >= 0 && xc <= 5; }
+bool valid_prec(int p, int mode) {
+  if (p == CALCHEM_XC_FP64) return true;
+  return p == CALCHEM_XC_MIXED && mixed_supported(mode);
+}
+
+Entry* find(uint64_t id) {
+  auto it = g_grids.find(id);
+  return it == g_grids.end() ? nullptr : it->second;
+}
+
+}  // namespace
+
+extern "C" {
+
+int calchem_cuda_is_available(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return device_ok() ? 1 : 0;
+}
+
+const char* calchem_xc_version(void) { return "calchem-xc-gb300 0.1 (sm_103a)"; }
+
+int calchem_cuda_vxc_upload_grid(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
+                                 const AoCompGpu* h_comps, int n_comps, const GridPtGpu* h_pts, int n_pts,
+                                 const int* h_cand_offsets, int n_cand_offsets, const int* h_cand_shells,
+                                 int n_cand_shells, int n_ao, uint64_t grid_id, size_t memory_limit_bytes) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return upload_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, h_pts, n_pts, h_cand_offsets,
+                     n_cand_offsets, h_cand_shells, n_cand_shells, n_ao, grid_id, memory_limit_bytes, nullptr);
+}
+
+int calchem_cuda_vxc_eval_rho(uint64_t grid_id, const double* h_p_mat, double* h_rho_grad_out, int n_pts, int n_ao) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_p_mat || !h_rho_grad_out || n_pts <= 0 || n_ao <= 0 || grid_id == 0) return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e || e->n_pts != n_pts || e->n_ao != n_ao) return -2;
+  const size_t nn = (size_t)n_ao * n_ao;
+  std::memcpy(e->h_stage, h_p_mat, nn * sizeof(double));
+  if (cudaMemcpyAsync(e->d_P, e->h_stage, nn * sizeof(double), cudaMemcpyHostToDevice, e->stream) != cudaSuccess)
+    return -5;
+  int rc = enqueue_eval(*e, kModeRho, 0, CALCHEM_XC_FP64, e->d_P, nullptr, nullptr, nullptr, nullptr, e->d_rg,
+                        nullptr, e->stream);
+  if (rc) return rc;
+  if (cudaMemcpyAsync(h_rho_grad_out, e->d_rg, (size_t)n_pts * 4 * sizeof(double), cudaMemcpyDeviceToHost,
+                      e->stream) != cudaSuccess ||
+      cudaStreamSynchronize(e->stream) != cudaSuccess)
+    return -5;
+  return 0;
+}
+
+int calchem_cuda_vxc_accum(uint64_t grid_id, const double* h_wv_in, double* h_vxc_out, int n_pts, int n_ao) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_wv_in || !h_vxc_out || n_pts <= 0 || n_ao <= 0 || grid_id == 0) return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e || e->n_pts != n_pts || e->n_ao != n_ao) return -2;
+  const size_t nn = (size_t)n_ao * n_ao;
+  if (cudaMemcpyAsync(e->d_rg, h_wv_in, (size_t)n_pts * 4 * sizeof(double), cudaMemcpyHostToDevice, e->stream) !=
+      cudaSuccess)
+    return -5;
+  int rc = enqueue_eval(*e, kModeAccum, 0, CALCHEM_XC_FP64, nullptr, nullptr, e->d_V, nullptr, e->d_rg, nullptr,
+                        nullptr, e->stream);
+  if (rc) return rc;
+  if (cudaMemcpyAsync(e->h_stage, e->d_V, nn * sizeof(double), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
+      cudaStreamSynchronize(e->stream) != cudaSuccess)
+    return -5;
+  std::memcpy(h_vxc_out, e->h_stage, nn * sizeof(double));
+  return 0;
+}
+
+int calchem_cuda_vxc_release(uint64_t grid_id) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (grid_id != 0) {
+    auto it = g_grids.find(grid_id);
+    if (it != g_grids.end()) {
+      if (it->second->stream) cudaStreamSynchronize(it->second->stream);
+      it->second->free_all();
+      delete it->second;
+      g_grids.erase(it);
+    }
+  }
+  return 0;
+}
+
+int calchem_xc_prepare_shells(int n_shells, const int* l, const int* atom_index, const double* centers,
+                              const int* n_prims, const double* exponents, const double* raw_coefs,
+                              AoShellGpu* shells_out, AoPrimGpu* prims_out, AoCompGpu* comps_out, int* n_ao_out) {
+  if (n_shells <= 0 || !l || !atom_index || !centers || !n_prims || !exponents || !raw_coefs || !shells_out ||
+      !prims_out || !comps_out || !n_ao_out)
+    return -1;
+  return prepare_shells(n_shells, l, atom_index, centers, n_prims, exponents, raw_coefs, shells_out, prims_out,
+                        comps_out, n_ao_out);
+}
+
+int calchem_xc_overlap(const AoShellGpu* shells, int n_shells, const AoPrimGpu* prims, const AoCompGpu* comps,
+                       int n_ao, double* s_out) {
+  if (!shells || !prims || !comps || !s_out || n_shells <= 0 || n_ao <= 0) return -1;
+  overlap_matrix(shells, n_shells, prims, comps, n_ao, s_out);
+  return 0;
+}
+
+int calchem_xc_grid_build(int n_atoms, const int* z, const double* xyz_bohr, int level, int radial_min,
+                          uint64_t grid_handle, int* n_pts_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (n_atoms <= 0 || !z || !xyz_bohr || level < 0 || level > 3 || radial_min < 0 || radial_min > 4096 ||
+      grid_handle == 0 || !n_pts_out)
+    return -1;
+  for (int a = 0; a < n_atoms; ++a)
+    if (z[a] < 1 || z[a] > 86 || !std::isfinite(xyz_bohr[3 * a]) || !std::isfinite(xyz_bohr[3 * a + 1]) ||
+        !std::isfinite(xyz_bohr[3 * a + 2]))
+      return -1;
+  if (!device_ok()) return -3;
+  if (g_built.count(grid_handle)) return -2;
+  std::vector<RadialShell> rs;
+  long long n_raw = 0;
+  radial_shells(n_atoms, z, level, radial_min, rs, &n_raw);
+  std::vector<double> inv_r, a_ij;
+  becke_tables(n_atoms, z, xyz_bohr, inv_r, a_ij);
+  const LebedevTables& T = lebedev_tables();
+  const int ns = (int)rs.size();
+  std::vector<RadialShellDev> rsd(ns);
+  for (int i = 0; i < ns; ++i) rsd[i] = {rs[i].atom, rs[i].leb_offset, rs[i].n_ang, 0, rs[i].r, rs[i].w_rad,
+                                         rs[i].raw_start};
+  GridBuildArgs a{};
+  double *d_xyz = nullptr, *d_inv = nullptr, *d_aij = nullptr, *d_leb = nullptr, *d_raw = nullptr, *d_raww = nullptr;
+  RadialShellDev* d_rs = nullptr;
+  unsigned char* d_flags = nullptr;
+  int* d_counts = nullptr;
+  long long* d_off = nullptr;
+  auto cleanup = [&]() {
+    void* p[] = {d_xyz, d_inv, d_aij, d_leb, d_raw, d_raww, d_rs, d_flags, d_counts, d_off};
+    for (void* q : p)
+      if (q) cudaFree(q);
+  };
+  bool ok = dalloc(&d_xyz, 3 * (size_t)n_atoms) && dalloc(&d_inv, inv_r.size()) && dalloc(&d_aij, a_ij.size()) &&
+            dalloc(&d_leb, T.xyzw.size()) && dalloc(&d_rs, ns) && dalloc(&d_raw, 4 * (size_t)n_raw) &&
+            dalloc(&d_raww, (size_t)n_raw) && dalloc(&d_flags, (size_t)n_raw) && dalloc(&d_counts, ns) &&
+            dalloc(&d_off, (size_t)ns + 1);
+  if (!ok) {
+    cudaGetLastError();
+    cleanup();
+    return -4;
+  }
+  ok = cudaMemcpy(d_xyz, xyz_bohr, 3 * n_atoms * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(d_inv, inv_r.data(), inv_r.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(d_aij, a_ij.data(), a_ij.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(d_leb, T.xyzw.data(), T.xyzw.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(d_rs, rsd.data(), ns * sizeof(RadialShellDev), cudaMemcpyHostToDevice) == cudaSuccess;
+  a.n_atoms = n_atoms;
+  a.xyz = d_xyz;
+  a.inv_r = d_inv;
+  a.a_ij = d_aij;
+  a.lebedev = d_leb;
+  a.shells = d_rs;
+  a.raw = d_raw;
+  a.raw_w = d_raww;
+  a.flags = d_flags;
+  a.counts = d_counts;
+  ok = ok && launch_grid_expand(a, ns, 0) == cudaSuccess && launch_grid_scan(d_counts, ns, d_off, 0) == cudaSuccess;
+  long long n_keep = 0;
+  ok = ok && cudaMemcpy(&n_keep, d_off + ns, sizeof(long long), cudaMemcpyDeviceToHost) == cudaSuccess;
+  if (!ok || n_keep > 0x7fffffffLL) {
+    cudaGetLastError();
+    cleanup();
+    return ok ? -2 : -5;
+  }
+  Built* b = new Built;
+  b->n = (int)n_keep;
+  if (!(dalloc(&b->d_xyzw, 4 * (size_t)n_keep) && dalloc(&b->d_raw_w, (size_t)n_keep) &&
+        dalloc(&b->d_host, (size_t)n_keep))) {
+    cudaGetLastError();
+    if (b->d_xyzw) cudaFree(b->d_xyzw);
+    if (b->d_raw_w) cudaFree(b->d_raw_w);
+    if (b->d_host) cudaFree(b->d_host);
+    delete b;
+    cleanup();
+    return -4;
+  }
+  a.out_xyzw = b->d_xyzw;
+  a.out_raw_w = b->d_raw_w;
+  a.out_host = b->d_host;
+  ok = launch_grid_compact(a, d_off, ns, 0) == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+  cleanup();
+  if (!ok) {
+    cudaGetLastError();
+    cudaFree(b->d_xyzw);
+    cudaFree(b->d_raw_w);
+    cudaFree(b->d_host);
+    delete b;
+    return -5;
+  }
+  g_built[grid_handle] = b;
+  *n_pts_out = b->n;
+  return 0;
+}
+
+int calchem_xc_grid_fetch(uint64_t grid_handle, double* xyzw, double* raw_w, int* host_atom) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_built.find(grid_handle);
+  if (it == g_built.end()) return -2;
+  if (!xyzw) return -1;
+  const Built& b = *it->second;
+  if (b.n == 0) return 0;
+  if (cudaMemcpy(xyzw, b.d_xyzw, 4 * (size_t)b.n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) return -5;
+  if (raw_w && cudaMemcpy(raw_w, b.d_raw_w, (size_t)b.n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -5;
+  if (host_atom && cudaMemcpy(host_atom, b.d_host, (size_t)b.n * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -5;
+  return 0;
+}
+
+int calchem_xc_grid_release(uint64_t grid_handle) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_built.find(grid_handle);
+  if (it != g_built.end()) {
+    cudaFree(it->second->d_xyzw);
+    cudaFree(it->second->d_raw_w);
+    cudaFree(it->second->d_host);
+    delete it->second;
+    g_built.erase(it);
+  }
+  return 0;
+}
+
+int calchem_xc_upload_points(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
+                             const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
+                             uint64_t grid_id, size_t memory_limit_bytes) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_shells || !h_prims || !h_comps || !h_xyzw || n_shells <= 0 || n_prims <= 0 || n_comps <= 0 || n_pts <= 0 ||
+      n_ao <= 0 || grid_id == 0)
+    return -1;
+  if (g_grids.count(grid_id)) return -2;
+  for (int s = 0; s < n_shells; ++s)
+    if (!(h_shells[s].r2_cutoff >= 0.0)) return -1;
+  Plan plan;
+  plan_batches(h_shells, n_shells, h_xyzw, n_pts, plan);
+  if (plan.pts.empty()) return -1;
+  return upload_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, plan.pts.data(), (int)plan.pts.size(),
+                     plan.cand_offsets.data(), (int)plan.cand_offsets.size(), plan.cand_shells.data(),
+                     (int)plan.cand_shells.size(), n_ao, grid_id, memory_limit_bytes, plan.weights.data());
+}
+
+int calchem_xc_set_weights(uint64_t grid_id, const double* h_weights, int n_pts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_weights || n_pts <= 0) return -1;
+  Entry* e = find(grid_id);
+  if (!e || e->n_pts != n_pts) return -2;
+  if (cudaMemcpy(e->d_pts + 3 * (size_t)n_pts, h_weights, n_pts * sizeof(double), cudaMemcpyHostToDevice) !=
+      cudaSuccess)
+    return -5;
+  e->has_w = true;
+  return 0;
+}
+
+int calchem_xc_plan_stats(uint64_t grid_id, int* n_batches, double* sum_m2n, double* sum_m2, int* max_m) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (n_batches) *n_batches = e->n_batches;
+  if (sum_m2n) *sum_m2n = e->sum_m2n;
+  if (sum_m2) *sum_m2 = e->sum_m2;
+  if (max_m) *max_m = e->max_m;
+  return 0;
+}
+
+int calchem_xc_evaluate_rks(uint64_t grid_id, int xc_code, int precision, const double* h_d_total, double* exc_out,
+                            double* nelec_out, double* h_v_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_d_total || !exc_out || !nelec_out || !h_v_out || !valid_xc(xc_code)) return -1;
+  if (!valid_prec(precision, kModeRks)) return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (!e->has_w) return -1;
+  const size_t nn = (size_t)e->n_ao * e->n_ao;
+  std::memcpy(e->h_stage, h_d_total, nn * sizeof(double));
+  if (cudaMemcpyAsync(e->d_P, e->h_stage, nn * sizeof(double), cudaMemcpyHostToDevice, e->stream) != cudaSuccess)
+    return -5;
+  int rc = enqueue_eval(*e, kModeRks, xc_code, precision, e->d_P, nullptr, e->d_V, nullptr, nullptr, nullptr,
+                        e->d_res, e->stream);
+  if (rc) return rc;
+  if (cudaMemcpyAsync(e->h_stage, e->d_V, nn * sizeof(double), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
+      cudaMemcpyAsync(e->h_stage + 2 * nn, e->d_res, 2 * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(e->stream) != cudaSuccess)
+    return -5;
+  std::memcpy(h_v_out, e->h_stage, nn * sizeof(double));
+  *exc_out = e->h_stage[2 * nn];
+  *nelec_out = e->h_stage[2 * nn + 1];
+  return 0;
+}
+
+int calchem_xc_evaluate_uks(uint64_t grid_id, int xc_code, int precision, const double* h_pa, const double* h_pb,
+                            double* exc_out, double* nelec_out, double* h_va_out, double* h_vb_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_pa || !h_pb || !exc_out || !nelec_out || !h_va_out || !h_vb_out || !valid_xc(xc_code)) return -1;
+  if (!valid_prec(precision, kModeUks)) return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (!e->has_w) return -1;
+  const size_t nn = (size_t)e->n_ao * e->n_ao;
+  std::memcpy(e->h_stage, h_pa, nn * sizeof(double));
+  std::memcpy(e->h_stage + nn, h_pb, nn * sizeof(double));
+  if (cudaMemcpyAsync(e->d_P, e->h_stage, nn * sizeof(double), cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
+      cudaMemcpyAsync(e->d_Pb, e->h_stage + nn, nn * sizeof(double), cudaMemcpyHostToDevice, e->stream) !=
+          cudaSuccess)
+    return -5;
+  int rc = enqueue_eval(*e, kModeUks, xc_code, precision, e->d_P, e->d_Pb, e->d_V, e->d_Vb, nullptr, nullptr,
+                        e->d_res, e->stream);
+  if (rc) return rc;
+  if (cudaMemcpyAsync(e->h_stage, e->d_V, nn * sizeof(double), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
+      cudaMemcpyAsync(e->h_stage + nn, e->d_Vb, nn * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(e->h_stage + 2 * nn, e->d_res, 3 * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(e->stream) != cudaSuccess)
+    return -5;
+  std::memcpy(h_va_out, e->h_stage, nn * sizeof(double));
+  std::memcpy(h_vb_out, e->h_stage + nn, nn * sizeof(double));
+  *exc_out = e->h_stage[2 * nn];
+  nelec_out[0] = e->h_stage[2 * nn + 1];
+  nelec_out[1] = e->h_stage[2 * nn + 2];
+  return 0;
+}
+
+int calchem_xc_evaluate_rks_device(uint64_t grid_id, int xc_code, int precision, const double* d_total,
+                                   double* d_result, double* d_v, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_total || !d_result || !d_v || !valid_xc(xc_code) || !valid_prec(precision, kModeRks)) return -1;
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (!e->has_w) return -1;
+  return enqueue_eval(*e, kModeRks, xc_code, precision, d_total, nullptr, d_v, nullptr, nullptr, nullptr, d_result,
+                      (cudaStream_t)stream);
+}
+
+int calchem_xc_evaluate_uks_device(uint64_t grid_id, int xc_code, int precision, const double* d_pa,
+                                   const double* d_pb, double* d_result, double* d_va, double* d_vb, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_pa || !d_pb || !d_result || !d_va || !d_vb || !valid_xc(xc_code) || !valid_prec(precision, kModeUks))
+    return -1;
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (!e->has_w) return -1;
+  return enqueue_eval(*e, kModeUks, xc_code, precision, d_pa, d_pb, d_va, d_vb, nullptr, nullptr, d_result,
+                      (cudaStream_t)stream);
+}
+
+int calchem_xc_last_launch_count(uint64_t grid_id) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Entry* e = find(grid_id);
+  return e ? e->last_launches : -2;
+}
+
+}  // extern "C"

@@ -1,0 +1,65 @@
+// common.cuh -- device data model shared by the grid, FP64 and tensor-core Vxc kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/calchem_xc.h"
+
+namespace cxc {
+
+constexpr int kBlockPts = 128;  // points per batch (vxc.rs:96)
+
+// One batch of <= 128 consecutive grid points and the shells that can touch it.
+// Built on the host from the reference's batching rules (vxc.rs:443-493).
+struct BatchDesc {
+  int pt_start;    // first point (index into the point arrays)
+  int n_pts;       // points in the batch (<= 128)
+  int cand_start;  // first entry in cand_shells / cand_loc
+  int n_cand;      // candidate shells
+  int ao_start;    // first entry in batch_ao (local AO -> global AO)
+  int m;           // AOs of the candidate shells
+  int pad0, pad1;
+};
+
+// Evaluation modes of the block kernels.
+enum Mode : int {
+  kModeRho = 0,   // drop-in eval_rho: write rho and grad rho per point
+  kModeAccum = 1, // drop-in accum: read (w v_rho / 2, w u) per point, add into V (lower triangle)
+  kModeRks = 2,   // fused closed shell
+  kModeUks = 3    // fused open shell
+};
+
+struct DevGrid {
+  int n_pts, n_ao, n_shells, n_batches;
+  const AoShellGpu* shells;
+  const AoPrimGpu* prims;
+  const AoCompGpu* comps;
+  const double* px;  // point coordinates and weights (SoA)
+  const double* py;
+  const double* pz;
+  const double* pw;
+  const BatchDesc* batches;
+  const int* cand_shells;  // shell index per candidate
+  const int* cand_loc;     // local AO row of the candidate's first component
+  const int* batch_ao;     // global AO per local row
+  const int* order;        // batch processing order (cost descending)
+};
+
+struct EvalArgs {
+  int mode;
+  int xc;
+  const double* Pa;   // density (RKS: total)
+  const double* Pb;   // beta density (UKS)
+  double* Va;         // output (lower triangle accumulated)
+  double* Vb;
+  double* rho_out;    // kModeRho: 4 per point
+  const double* wv_in;  // kModeAccum: 4 per point
+  double* batch_red;  // per batch: exc, nelec_a, nelec_b
+  int* counter;       // work-queue head
+  double* slab;       // per-CTA scratch
+  size_t slab_stride; // doubles per CTA
+  int max_m;
+};
+
+}  // namespace cxc

@@ -1,0 +1,54 @@
+// host_prep.h -- host-side preparation routines (see host_prep.cpp).
+#pragma once
+
+#include <vector>
+
+#include "../../include/calchem_xc.h"
+
+namespace cxc {
+
+constexpr int kPlanBatch = 128;
+
+double gto_norm(double alpha, int l, int m, int n);
+int prepare_shells(int n_shells, const int* l, const int* atom, const double* centers, const int* n_prims,
+                   const double* exps, const double* coefs, AoShellGpu* so, AoPrimGpu* po, AoCompGpu* co,
+                   int* n_ao_out);
+void overlap_matrix(const AoShellGpu* sh, int n_shells, const AoPrimGpu* pr, const AoCompGpu* co, int n_ao,
+                    double* S);
+
+struct LebedevTables {
+  std::vector<double> xyzw;  // concatenated rules, 4 doubles per point
+  int offset[6];
+  int count[6];
+};
+const LebedevTables& lebedev_tables();
+int lebedev_index(int npts);
+
+double bragg_slater_bohr(int z);
+double becke_shift(int zc, int zd);
+int radial_count(int z, int level);
+int angular_points(double r, double rbs, int level);
+
+struct RadialShell {
+  int atom;
+  int leb_offset;
+  int n_ang;
+  int pad;
+  double r;
+  double w_rad;
+  long long raw_start;
+};
+void radial_shells(int n_atoms, const int* z, int level, int radial_min, std::vector<RadialShell>& out,
+                   long long* n_raw);
+void becke_tables(int n, const int* z, const double* xyz, std::vector<double>& inv_r, std::vector<double>& a_ij);
+
+// Reference-layout batch plan (what RksVxcEngine::new_with_gpu uploads, vxc.rs:497-545).
+struct Plan {
+  std::vector<GridPtGpu> pts;
+  std::vector<double> weights;
+  std::vector<int> cand_offsets;
+  std::vector<int> cand_shells;
+};
+int plan_batches(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan);
+
+}  // namespace cxc

@@ -1,0 +1,216 @@
+"""Kohn-Sham XC matrix engines (mirrors crates/calchem-dft/src/vxc.rs and the
+``GpuVxcGrid`` wrapper of crates/calchem-cuda/src/lib.rs:1178-1306).
+
+``RksVxcEngine`` / ``UksVxcEngine`` keep the reference call surface
+(``new_with_gpu``, ``evaluate``, ``telemetry``) and run the whole Vxc build on the
+GPU through the fused C ABI (``calchem_xc_evaluate_rks`` / ``_uks``).  There is no
+CPU path: a device or library failure raises ``CalchemXcError`` instead of
+falling back, so ``telemetry()`` never reports a fallback.
+
+``GpuVxcGrid`` exposes the reference's own four-call FFI
+(upload_grid / eval_rho / accum / release) for callers that evaluate the
+functional themselves, as CalChem's Rust engine does (vxc.rs:728-799).
+"""
+
+import itertools
+import os
+
+import numpy as np
+
+from . import _native
+from .xc import XcFunctional
+
+FP64 = 0
+MIXED = 1
+_PRECISION = {"fp64": FP64, "mixed": MIXED, FP64: FP64, MIXED: MIXED}
+
+_ids = itertools.count(1 << 20)
+
+MAX_GPU_MEMORY_BYTES = 64 << 30
+
+
+def resolve_gpu_memory_limit() -> int:
+    """CALCHEM_MAX_GPU_MEM_MB when set (as calchem-cuda's resolve_gpu_memory_limit, lib.rs:531-538);
+    otherwise 64 GiB, since the reference's 5 GiB ceiling targets 8 GB cards."""
+    v = os.environ.get("CALCHEM_MAX_GPU_MEM_MB")
+    if v is not None:
+        try:
+            return min(int(v) << 20, MAX_GPU_MEMORY_BYTES)
+        except ValueError:
+            pass
+    return MAX_GPU_MEMORY_BYTES
+
+
+def is_cuda_available() -> bool:
+    """calchem_cuda::is_cuda_available (lib.rs:469-483), including the CALCHEM_DISABLE_GPU switch."""
+    if os.environ.get("CALCHEM_DISABLE_GPU") == "1":
+        return False
+    return _native.load().calchem_cuda_is_available() == 1
+
+
+def _as_matrix(m, n):
+    a = np.ascontiguousarray(m, dtype=np.float64)
+    if a.shape != (n, n):
+        raise ValueError(f"expected a {n}x{n} matrix, got {a.shape}")
+    return a
+
+
+class GpuVxcGrid:
+    """The reference's device-resident grid (lib.rs:1178-1306) over the drop-in C ABI."""
+
+    def __init__(self, grid_id, n_pts, n_ao):
+        self.grid_id, self.n_pts, self.n_ao = grid_id, n_pts, n_ao
+
+    @classmethod
+    def upload(cls, shells, prims, comps, pts, cand_offsets, cand_shells, n_ao, memory_limit=None):
+        lib = _native.load()
+        gid = next(_ids)
+        shells = np.ascontiguousarray(shells, dtype=_native.AO_SHELL)
+        prims = np.ascontiguousarray(prims, dtype=_native.AO_PRIM)
+        comps = np.ascontiguousarray(comps, dtype=_native.AO_COMP)
+        pts = np.ascontiguousarray(pts, dtype=_native.GRID_PT)
+        off = np.ascontiguousarray(cand_offsets, dtype=np.int32)
+        cs = np.ascontiguousarray(cand_shells, dtype=np.int32)
+        lim = resolve_gpu_memory_limit() if memory_limit is None else int(memory_limit)
+        _native.check("calchem_cuda_vxc_upload_grid", lib.calchem_cuda_vxc_upload_grid(
+            _native.ptr(shells), len(shells), _native.ptr(prims), len(prims), _native.ptr(comps), len(comps),
+            _native.ptr(pts), len(pts), _native.ptr(off), len(off), _native.ptr(cs), len(cs), int(n_ao), gid, lim))
+        return cls(gid, len(pts), int(n_ao))
+
+    def eval_rho_grad(self, p_mat) -> np.ndarray:
+        lib = _native.load()
+        P = _as_matrix(p_mat, self.n_ao)
+        out = np.zeros((self.n_pts, 4), dtype=np.float64)
+        _native.check("calchem_cuda_vxc_eval_rho", lib.calchem_cuda_vxc_eval_rho(
+            self.grid_id, _native.ptr(P), _native.ptr(out), self.n_pts, self.n_ao))
+        return out
+
+    def accumulate_vxc(self, wv) -> np.ndarray:
+        lib = _native.load()
+        w = np.ascontiguousarray(wv, dtype=np.float64).reshape(self.n_pts, 4)
+        out = np.zeros((self.n_ao, self.n_ao), dtype=np.float64)
+        _native.check("calchem_cuda_vxc_accum", lib.calchem_cuda_vxc_accum(
+            self.grid_id, _native.ptr(w), _native.ptr(out), self.n_pts, self.n_ao))
+        return out
+
+    def release(self):
+        if self.grid_id:
+            _native.load().calchem_cuda_vxc_release(self.grid_id)
+            self.grid_id = 0
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class _EngineBase:
+    def __init__(self, basis, grid, use_gpu=True, precision="fp64"):
+        if not use_gpu:
+            raise NotImplementedError("calchem_gb300 evaluates Vxc on the GPU only; there is no CPU engine")
+        self.n_ao = basis.n_ao
+        self.precision = _PRECISION[precision]
+        self.gpu_kernel_invocations = 0
+        self.gpu_fallback_invocations = 0
+        self.grid_id = 0
+        self.last_nelec = None
+        lib = _native.load()
+        sh, pr, co = basis.gpu_arrays()
+        xyzw = np.ascontiguousarray(grid.xyzw, dtype=np.float64)
+        if len(xyzw) == 0:
+            raise ValueError("empty grid")
+        gid = next(_ids)
+        _native.check("calchem_xc_upload_points", lib.calchem_xc_upload_points(
+            _native.ptr(sh), len(sh), _native.ptr(pr), len(pr), _native.ptr(co), len(co), _native.ptr(xyzw),
+            len(xyzw), self.n_ao, gid, resolve_gpu_memory_limit()))
+        self.grid_id = gid
+
+    @classmethod
+    def new_with_gpu(cls, basis, grid, use_gpu=True, precision="fp64"):
+        return cls(basis, grid, use_gpu, precision)
+
+    def telemetry(self):
+        """(gpu_kernel_invocations, gpu_fallback_invocations) as in vxc.rs:420-425."""
+        return self.gpu_kernel_invocations, self.gpu_fallback_invocations
+
+    def plan_stats(self):
+        """(n_batches, sum m^2 n, sum m^2, max m) of the batch plan."""
+        lib = _native.load()
+        nb = np.zeros(1, np.int32)
+        s1 = np.zeros(1)
+        s2 = np.zeros(1)
+        mm = np.zeros(1, np.int32)
+        _native.check("calchem_xc_plan_stats", lib.calchem_xc_plan_stats(
+            self.grid_id, _native.ptr(nb), _native.ptr(s1), _native.ptr(s2), _native.ptr(mm)))
+        return int(nb[0]), float(s1[0]), float(s2[0]), int(mm[0])
+
+    def last_launch_count(self) -> int:
+        return int(_native.load().calchem_xc_last_launch_count(self.grid_id))
+
+    def close(self):
+        if self.grid_id:
+            _native.load().calchem_cuda_vxc_release(self.grid_id)
+            self.grid_id = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RksVxcEngine(_EngineBase):
+    """Closed-shell engine: evaluate(basis, grid, func, P_total) -> (Exc, Vxc) (vxc.rs:720-726)."""
+
+    def evaluate(self, basis, grid, func, density_total, precision=None):
+        lib = _native.load()
+        P = _as_matrix(density_total, self.n_ao)
+        V = np.zeros((self.n_ao, self.n_ao), dtype=np.float64)
+        exc = np.zeros(1)
+        ne = np.zeros(1)
+        prec = self.precision if precision is None else _PRECISION[precision]
+        _native.check("calchem_xc_evaluate_rks", lib.calchem_xc_evaluate_rks(
+            self.grid_id, int(XcFunctional(func)), prec, _native.ptr(P), _native.ptr(exc), _native.ptr(ne),
+            _native.ptr(V)))
+        self.gpu_kernel_invocations += self.last_launch_count()
+        self.last_nelec = float(ne[0])
+        return float(exc[0]), V
+
+
+class UksVxcEngine(_EngineBase):
+    """Open-shell engine: evaluate(basis, grid, func, Pa, Pb) -> (Exc, Va, Vb) (vxc.rs:1662-1669)."""
+
+    def evaluate(self, basis, grid, func, pa, pb, precision=None):
+        lib = _native.load()
+        Pa = _as_matrix(pa, self.n_ao)
+        Pb = _as_matrix(pb, self.n_ao)
+        Va = np.zeros((self.n_ao, self.n_ao), dtype=np.float64)
+        Vb = np.zeros((self.n_ao, self.n_ao), dtype=np.float64)
+        exc = np.zeros(1)
+        ne = np.zeros(2)
+        prec = self.precision if precision is None else _PRECISION[precision]
+        _native.check("calchem_xc_evaluate_uks", lib.calchem_xc_evaluate_uks(
+            self.grid_id, int(XcFunctional(func)), prec, _native.ptr(Pa), _native.ptr(Pb), _native.ptr(exc),
+            _native.ptr(ne), _native.ptr(Va), _native.ptr(Vb)))
+        self.gpu_kernel_invocations += self.last_launch_count()
+        self.last_nelec = (float(ne[0]), float(ne[1]))
+        return float(exc[0]), Va, Vb
+
+
+def evaluate_vxc_rks(basis, grid, func, density_total, precision="fp64"):
+    """evaluate_vxc_rks (vxc.rs:280-285): one-shot engine build + evaluate."""
+    eng = RksVxcEngine(basis, grid, True, precision)
+    try:
+        return eng.evaluate(basis, grid, func, density_total)
+    finally:
+        eng.close()
+
+
+def evaluate_vxc_uks(basis, grid, func, pa, pb, precision="fp64"):
+    """evaluate_vxc_uks (vxc.rs:1352-1358)."""
+    eng = UksVxcEngine(basis, grid, True, precision)
+    try:
+        return eng.evaluate(basis, grid, func, pa, pb)
+    finally:
+        eng.close()

@@ -1,0 +1,184 @@
+/*
+ * calchem_xc.h -- C ABI of the GB300 (sm_103a) exchange-correlation quadrature library
+ * (libcalchem_xc.so).
+ *
+ * The library replaces CalChem's `calchem-cuda` Vxc path.  It keeps the reference's FFI
+ * contract exactly, so CalChem's Rust `GpuVxcGrid` links against it unchanged, and it adds
+ * fused entry points that compute (Exc, Nelec, Vxc) in one call with no CPU work in between.
+ *
+ * Conventions shared by every function (crates/calchem-cuda/src/cuda_kernels.cu:7354-7562):
+ *   return 0 on success, otherwise
+ *    -1  bad arguments (null pointer, non-positive size, unknown functional/precision code)
+ *    -2  unknown grid id, size mismatch with the uploaded grid, or a size overflow
+ *    -3  no usable CUDA device, or the request exceeds the caller's memory budget
+ *    -4  device allocation failure
+ *    -5  copy or kernel launch failure
+ *    -6  device-side overflow flag (kept for compatibility; the kernels here never set it)
+ *    -7  a device-side wait gave up (bounded spin expired); the result is not valid
+ *   All matrices are dense row-major n_ao x n_ao doubles.  Every call is synchronous with
+ *   respect to the host buffers it is given and is serialised by one process-wide mutex, as in
+ *   the reference.  There is never a CPU fallback: a failure is reported, not recomputed.
+ */
+#ifndef CALCHEM_XC_H
+#define CALCHEM_XC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Data layouts, identical to crates/calchem-cuda/src/lib.rs:46-84 (#[repr(C)]). ---- */
+typedef struct AoShellGpu {
+  double center[3];
+  double r2_cutoff;
+  int ao_offset;
+  int n_funcs;
+  int prim_start;
+  int n_prims;
+  int comp_start;
+  int atom_index;
+} AoShellGpu; /* 56 bytes */
+
+typedef struct AoPrimGpu {
+  double exponent;
+  double weighted_norm;
+} AoPrimGpu; /* 16 bytes */
+
+typedef struct AoCompGpu {
+  double scale;
+  int lx, ly, lz, _pad;
+} AoCompGpu; /* 24 bytes */
+
+typedef struct GridPtGpu {
+  double x, y, z;
+  int batch_id;
+  int host_atom;
+} GridPtGpu; /* 32 bytes */
+
+/* Functional codes, in the order of CalChem's XcFunctional enum (crates/calchem-dft/src/xc.rs:16-35). */
+enum {
+  CALCHEM_XC_SVWN5 = 0,
+  CALCHEM_XC_BLYP = 1,
+  CALCHEM_XC_PBE = 2,
+  CALCHEM_XC_B3LYP = 3,  /* 0.80 Slater + 0.72 dB88 + 0.19 VWN_RPA + 0.81 LYP */
+  CALCHEM_XC_B3LYP5 = 4, /* as B3LYP with VWN5 */
+  CALCHEM_XC_PBE0 = 5    /* 0.75 PBE_X + 1.00 PBE_C */
+};
+
+/* Precision of the two dense contractions (rho = Phi D Phi^T and V = Phi^T (w v) Phi). */
+enum {
+  CALCHEM_XC_FP64 = 0,  /* plain all-FP64 drop-in form (matches the reference to 1e-9 Eh / 1e-10) */
+  CALCHEM_XC_MIXED = 1  /* tcgen05 tensor-core contractions, split operands, FP32 accumulation */
+};
+
+/* Grid levels (crates/calchem-dft/src/grid.rs:13-31). */
+enum { CALCHEM_GRID_COARSE = 0, CALCHEM_GRID_MEDIUM = 1, CALCHEM_GRID_FINE = 2, CALCHEM_GRID_ULTRAFINE = 3 };
+
+/* ======================================================================================
+ * (1) Drop-in replacements of the reference's exports, same signatures and semantics.
+ * ====================================================================================== */
+
+/* Replaces calchem_cuda_is_available (crates/calchem-cuda/src/lib.rs:469-483 binding).
+ * Returns 1 when a CUDA device of compute capability 10.3 is usable, else 0. */
+int calchem_cuda_is_available(void);
+
+/* Replaces calchem_cuda_vxc_upload_grid (cuda_kernels.cu:7354-7450; binding lib.rs:297-312).
+ * Uploads the screened basis, the grid points (grouped by batch_id, batches in increasing
+ * order) and the per-batch candidate-shell CSR lists.  Re-uploading an existing id with the same
+ * (n_pts, n_ao) returns 0 and keeps the old data; different sizes return -2. */
+int calchem_cuda_vxc_upload_grid(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
+                                 const AoCompGpu* h_comps, int n_comps, const GridPtGpu* h_pts, int n_pts,
+                                 const int* h_cand_offsets, int n_cand_offsets, const int* h_cand_shells,
+                                 int n_cand_shells, int n_ao, uint64_t grid_id, size_t memory_limit_bytes);
+
+/* Replaces calchem_cuda_vxc_eval_rho (cuda_kernels.cu:7452-7494; binding lib.rs:313-319).
+ * h_rho_grad_out[4*g + {0,1,2,3}] = rho, d/dx rho, d/dy rho, d/dz rho at point g for density P. */
+int calchem_cuda_vxc_eval_rho(uint64_t grid_id, const double* h_p_mat, double* h_rho_grad_out, int n_pts, int n_ao);
+
+/* Replaces calchem_cuda_vxc_accum (cuda_kernels.cu:7496-7545; binding lib.rs:320-326).
+ * h_wv_in[4*g..] = (w v_rho / 2, w u_x, w u_y, w u_z).  h_vxc_out receives the LOWER triangle
+ * of V (row >= col); the strict upper triangle is zero. */
+int calchem_cuda_vxc_accum(uint64_t grid_id, const double* h_wv_in, double* h_vxc_out, int n_pts, int n_ao);
+
+/* Replaces calchem_cuda_vxc_release (cuda_kernels.cu:7547-7562; binding lib.rs:327). */
+int calchem_cuda_vxc_release(uint64_t grid_id);
+
+/* ======================================================================================
+ * (2) Host-side preparation (what RksVxcEngine::new_with_gpu does before uploading).
+ * ====================================================================================== */
+
+/* Contraction normalisation and screening data for Cartesian shells
+ * (crates/calchem-basis/src/normalization.rs:20-97, lib.rs:462-573; ao_grid.rs:28-71).
+ * Inputs per shell: angular momentum l (0..3), atom index, centre (Bohr), primitive count, and the
+ * raw exponents / contraction coefficients concatenated over shells.  AO offsets follow shell
+ * order.  Outputs: one AoShellGpu per shell, one AoPrimGpu per primitive, one AoCompGpu per
+ * Cartesian component (sum over shells of (l+1)(l+2)/2 entries). */
+int calchem_xc_prepare_shells(int n_shells, const int* l, const int* atom_index, const double* centers,
+                              const int* n_prims, const double* exponents, const double* raw_coefs,
+                              AoShellGpu* shells_out, AoPrimGpu* prims_out, AoCompGpu* comps_out, int* n_ao_out);
+
+/* Overlap matrix S (n_ao x n_ao) of prepared shells (crates/calchem-int/src/one_electron.rs:7-31, 115-128). */
+int calchem_xc_overlap(const AoShellGpu* shells, int n_shells, const AoPrimGpu* prims, const AoCompGpu* comps,
+                       int n_ao, double* s_out);
+
+/* Builds a Becke-partitioned Euler-Maclaurin x Lebedev molecular grid on the GPU
+ * (crates/calchem-dft/src/grid.rs:732-828): atom-major, radial-shell-major, Lebedev order; points
+ * with w <= 1e-18 dropped.  Becke weights are evaluated in FP64 on the device.  The grid stays on
+ * the device under grid_handle until calchem_xc_grid_release. */
+int calchem_xc_grid_build(int n_atoms, const int* z, const double* xyz_bohr, int level, int radial_min,
+                          uint64_t grid_handle, int* n_pts_out);
+/* Copies a built grid to the host: xyzw[4*g] = (x, y, z, weight); raw_w and host_atom may be NULL. */
+int calchem_xc_grid_fetch(uint64_t grid_handle, double* xyzw, double* raw_w, int* host_atom);
+int calchem_xc_grid_release(uint64_t grid_handle);
+
+/* One-call engine construction: chunks the points into batches of 128 (points with |w| < 1e-24
+ * skipped), computes each batch's bounding sphere and candidate shells (vxc.rs:443-493), and
+ * uploads everything -- including the weights, which the fused evaluators need -- under grid_id.
+ * Returns -2 if grid_id exists. */
+int calchem_xc_upload_points(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
+                             const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
+                             uint64_t grid_id, size_t memory_limit_bytes);
+
+/* Attaches quadrature weights to a grid uploaded with calchem_cuda_vxc_upload_grid
+ * (weights in the uploaded point order). */
+int calchem_xc_set_weights(uint64_t grid_id, const double* h_weights, int n_pts);
+
+/* Number of batches and the sum over batches of m_b^2 * n_b (m_b AOs, n_b points): the
+ * algorithmic contraction work is 4x (RKS) that sum in flops. */
+int calchem_xc_plan_stats(uint64_t grid_id, int* n_batches, double* sum_m2n, double* sum_m2, int* max_m);
+
+/* ======================================================================================
+ * (3) Fused evaluators: D -> (Exc, Nelec, V) entirely on the device.
+ * ====================================================================================== */
+
+/* Closed shell.  d_total = P_total = 2 P_alpha (as RksVxcEngine::evaluate, vxc.rs:720-726).
+ * exc_out = sum_g w_g f_xc; nelec_out = sum_g w_g rho_g (points with rho >= 1e-18);
+ * v_out = full symmetric alpha-spin Vxc. */
+int calchem_xc_evaluate_rks(uint64_t grid_id, int xc_code, int precision, const double* h_d_total,
+                            double* exc_out, double* nelec_out, double* h_v_out);
+
+/* Open shell (UksVxcEngine::evaluate, vxc.rs:1662-1669).  nelec_out[0..1] = (N_alpha, N_beta). */
+int calchem_xc_evaluate_uks(uint64_t grid_id, int xc_code, int precision, const double* h_pa, const double* h_pb,
+                            double* exc_out, double* nelec_out, double* h_va_out, double* h_vb_out);
+
+/* Device-pointer variants (inputs and outputs already in device memory; enqueued on `stream`,
+ * a cudaStream_t, 0 for the legacy stream).  d_result receives (Exc, N_alpha + N_beta) for RKS and
+ * (Exc, N_alpha, N_beta) for UKS.  They return after enqueueing; the caller synchronises. */
+int calchem_xc_evaluate_rks_device(uint64_t grid_id, int xc_code, int precision, const double* d_total,
+                                   double* d_result, double* d_v, void* stream);
+int calchem_xc_evaluate_uks_device(uint64_t grid_id, int xc_code, int precision, const double* d_pa,
+                                   const double* d_pb, double* d_result, double* d_va, double* d_vb, void* stream);
+
+/* Number of kernel launches the last evaluate on grid_id enqueued (for launch accounting). */
+int calchem_xc_last_launch_count(uint64_t grid_id);
+
+/* Library version string. */
+const char* calchem_xc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CALCHEM_XC_H */
