@@ -1,0 +1,377 @@
+"""Benchmark: Vxc build time per SCF iteration on one GB300.
+
+Workload (the configuration the headline metric is quoted on): n-octane C8H18
+(all-trans, C-C 1.54 / C-H 1.09 Angstrom, tetrahedral), B3LYP (VWN_RPA),
+6-31G(d,p) Cartesian (210 AOs), CalChem's Fine grid (99 radial shells, pruned
+Lebedev, Becke partition), seeded S-orthonormal density (33 occupied orbitals,
+PCG64 seed 7).  One step = one full Vxc build (D -> Exc, Nelec, Vxc).
+
+* value: mean device time of one build with D already resident in HBM, CUDA
+  events on the launch stream, L2 flushed (256 MiB write) before every step.
+* e2e: the same build through the host-buffer C ABI call
+  (calchem_xc_evaluate_rks), host<->device copies inside the timed region.
+* roofline: the quadrature kernel, algorithmic work 4 * sum_b m_b^2 n_b flops
+  (RKS contractions), timed by CUDA events around that kernel.
+* cpu_baseline: the oracle's restatement of CalChem's RksVxcEngine CPU path on
+  this host's cores (the reference's Rust cannot be built offline).
+
+``--impl reference`` times that CPU restatement as the reference arm.
+With N > 1 GPUs (torchrun) every rank runs an independent replica (the path is
+one GPU by design), and the reported value is the maximum over ranks.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Vxc build ms/SCF iter on 1 GB300: mixed+pruned vs FP64 plain at dExc<=1e-6 Eh"
+WORKLOAD = ("C8H18 all-trans, B3LYP (VWN_RPA), 6-31G(d,p) Cartesian 210 AOs, CalChem Fine grid "
+            "(99 radial shells, pruned Lebedev, Becke), seeded S-orthonormal D (33 occ, seed 7)")
+SEED = 7
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# DRAM bytes (read + write) per launch of the quadrature kernel from one ncu capture of this
+# workload; see profiles/.  None until a capture exists for the precision.
+NCU_TRAFFIC_BYTES = {"fp64": 4.120501e9, "mixed": None}  # profiles/vxc_fp64_kernel_octane_b3lyp.md
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def build_inputs():
+    from calchem_gb300 import BasisSet, workloads
+
+    mol = workloads.octane()
+    basis = BasisSet.from_name("6-31g(d,p)", mol)
+    S = basis.overlap()
+    D = workloads.seeded_density_rks(S, mol.nelectron() // 2, SEED)
+    return mol, basis, D
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def fp64_peak_tflops(torch, dev):
+    """FP64 matmul throughput on this GPU (cuBLAS DGEMM 4096^3, best of 5): the FP64 roofline."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    torch.mm(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.mm(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e))
+    return 2 * 4096 ** 3 / (best * 1e-3) / 1e12
+
+
+def cpu_reference_run(basis, mol, D, steps, warmup, budget_s=150.0):
+    """Times the oracle's restatement of CalChem's RksVxcEngine CPU path (all host threads)."""
+    from oracle import oracle as O
+
+    og = O.Grid.build(mol.z, mol.coords_bohr, "fine")
+    ob = O.Basis.from_name("6-31g(d,p)", [a.symbol for a in mol.atoms], mol.coords_bohr)
+    eng = O.RksEngine(ob, og)
+    threads = O.max_threads()
+    t0 = time.perf_counter()
+    e_full, n_full, _ = eng.evaluate(D, "b3lyp")
+    t_full = time.perf_counter() - t0
+    frac = 1.0
+    nb = eng.n_batches
+    if t_full * (steps + warmup) > budget_s and eng.cached:
+        frac = max(0.02, budget_s / (t_full * (steps + warmup)))
+    sample_b = max(1, int(nb * frac)) if eng.cached else nb
+    rng = (0, sample_b) if eng.cached else (-1, -1)
+    for _ in range(max(0, warmup - 1)):
+        eng.evaluate(D, "b3lyp", batch_range=rng)
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        eng.evaluate(D, "b3lyp", batch_range=rng)
+        ts.append(time.perf_counter() - t0)
+    scale = nb / sample_b if eng.cached else 1.0
+    ms = statistics.mean(ts) * 1e3 * scale
+    path = "cached-AO BLAS-3 RksVxcEngine::evaluate" if eng.cached else "per-point evaluate_vxc_rks"
+    sample = (f"{path} restated in C++ (oracle), {steps} timed builds over batches [0, {sample_b}) of {nb} "
+              f"({len(og)} points), scaled by {scale:.3f} to a full build")
+    return ms, threads, sample, e_full, n_full
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    mol, basis, D = build_inputs()
+    ms, threads, sample, _, _ = cpu_reference_run(basis, mol, D, args.steps, args.warmup)
+    line = {"metric": METRIC, "value": round(ms, 4), "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "path": "CPU, all host threads"},
+            "cpu_baseline": {"value": round(ms, 4), "unit": "ms", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(ms, 4), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    from calchem_gb300 import GridLevel, MolecularGrid, RksVxcEngine, _native
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+    dev = torch.device("cuda", torch.cuda.current_device())
+    lib = _native.load()
+    mol, basis, D = build_inputs()
+    grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
+    prec_name = args.precision
+    mixed_ok = True
+    if prec_name == "auto":
+        prec_name = "mixed"
+    eng = RksVxcEngine(basis, grid)
+    n = basis.n_ao
+    n_batches, sum_m2n, _, max_m = eng.plan_stats()
+    flops = 4.0 * sum_m2n
+    prec = 1 if prec_name == "mixed" else 0
+    # probe the mixed path; fall back to reporting the FP64 form if it is not enabled
+    probe_V = np.zeros((n, n))
+    e1, n1 = np.zeros(1), np.zeros(1)
+    rc = lib.calchem_xc_evaluate_rks(eng.grid_id, 3, prec, _native.ptr(D), _native.ptr(e1), _native.ptr(n1),
+                                     _native.ptr(probe_V))
+    if rc != 0 and prec == 1:
+        mixed_ok = False
+        prec, prec_name = 0, "fp64"
+    stream = torch.cuda.Stream(device=dev)
+    dD = torch.from_numpy(D).to(dev)
+    dV = torch.zeros((n, n), dtype=torch.float64, device=dev)
+    dres = torch.zeros(4, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    _native.check("calchem_xc_set_profiling", lib.calchem_xc_set_profiling(eng.grid_id, 1))
+    torch.cuda.synchronize()
+
+    def step_device():
+        return lib.calchem_xc_evaluate_rks_device(eng.grid_id, 3, prec, dD.data_ptr(), dres.data_ptr(),
+                                                  dV.data_ptr(), stream.cuda_stream)
+
+    for _ in range(max(3, args.warmup)):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        _native.check("evaluate", step_device())
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    step_ms, kern_ms = [], []
+    launches = 0
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        _native.check("evaluate", step_device())
+        e.record(stream)
+        km = np.zeros(1, np.float32)
+        _native.check("last_kernel_ms", lib.calchem_xc_last_kernel_ms(eng.grid_id, _native.ptr(km)))
+        e.synchronize()
+        step_ms.append(s.elapsed_time(e))
+        kern_ms.append(float(km[0]))
+        launches += eng.last_launch_count()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    exc_dev = float(dres[0].item())
+    nelec_dev = float(dres[1].item())
+    ms = statistics.mean(step_ms)
+    kms = statistics.mean(kern_ms)
+    if dist:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    # ---- e2e through the host-buffer C ABI call (copies inside the timed region)
+    Vh = np.zeros((n, n))
+    e_h, n_h = np.zeros(1), np.zeros(1)
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _native.check("calchem_xc_evaluate_rks", lib.calchem_xc_evaluate_rks(
+            eng.grid_id, 3, prec, _native.ptr(D), _native.ptr(e_h), _native.ptr(n_h), _native.ptr(Vh)))
+        if i >= args.warmup:
+            e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = statistics.mean(e2e)
+    # ---- the FP64 plain form on the same build, for the mixed-vs-plain comparison
+    ref_fp64 = {}
+    if prec == 1:
+        Vf = np.zeros((n, n))
+        ef, nf = np.zeros(1), np.zeros(1)
+        lib.calchem_xc_evaluate_rks(eng.grid_id, 3, 0, _native.ptr(D), _native.ptr(ef), _native.ptr(nf),
+                                    _native.ptr(Vf))
+        fts = []
+        for _ in range(3):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            lib.calchem_xc_evaluate_rks_device(eng.grid_id, 3, 0, dD.data_ptr(), dres.data_ptr(), dV.data_ptr(),
+                                               stream.cuda_stream)
+            e.record(stream)
+            e.synchronize()
+            fts.append(s.elapsed_time(e))
+        ref_fp64 = {"fp64_plain_ms": round(statistics.mean(fts), 4),
+                    "speedup_vs_fp64_plain": round(statistics.mean(fts) / ms, 3),
+                    "dExc_vs_fp64": float(e_h[0] - ef[0]), "dNelec_vs_fp64": float(n_h[0] - nf[0]),
+                    "max_abs_dV_vs_fp64": float(np.max(np.abs(Vh - Vf)))}
+    pk, pk_kind = peaks()
+    if prec == 1:
+        peak, bound, unit = pk.get("bf16_tflops", 1900.0), "tensor", "TFLOP/s"
+        peak_note = f"dense bf16 burst, {pk_kind}"
+    else:
+        peak = fp64_peak_tflops(torch, dev)
+        bound, unit = "tensor", "TFLOP/s"
+        peak_note = "FP64 pipe: cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in the measured peaks)"
+    achieved = flops / (kms * 1e-3) / 1e12
+    traffic = NCU_TRAFFIC_BYTES.get(prec_name)
+    line = {
+        "metric": METRIC, "value": round(ms, 4), "unit": "ms", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if prec == 0 else "bf16x3 split (f32 accumulate) contractions, f64 functional/sums",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "precision": prec_name, "n_ao": n, "grid_points": len(grid),
+                   "batches": n_batches, "max_m": max_m, "l2": "flushed before every timed step (256 MiB write)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "grid_points_per_s": round(len(grid) / (ms * 1e-3), 1),
+        "exc": exc_dev, "nelec": nelec_dev,
+        "roofline": {"bound": bound, "achieved": round(achieved, 4), "peak": round(peak, 2), "unit": unit,
+                     "frac": round(achieved / peak, 5), "traffic": traffic,
+                     "kernel": "vxc quadrature kernel", "kernel_ms": round(kms, 4),
+                     "work": f"4*sum(m^2 n) = {flops:.4e} flop per launch", "peak_source": peak_note},
+        "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": n * n * 8,
+                "d2h_bytes_per_step": n * n * 8 + 16},
+        "gpu_launches": launches,
+        "wall_s_timed": round(t_wall, 3),
+        "clocks": clk,
+    }
+    line.update(ref_fp64)
+    if not mixed_ok:
+        line["note"] = "mixed-precision path not enabled in this build; FP64 form reported"
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cms, threads, sample, _, _ = cpu_reference_run(basis, mol, D, 3, 1, budget_s=25.0)
+        line["cpu_baseline"] = {"value": round(cms, 3), "unit": "ms", "cores": threads, "kind": "port",
+                                "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

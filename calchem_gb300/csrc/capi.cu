@@ -68,6 +68,8 @@ struct Entry {
   double* h_stage = nullptr;  // pinned: 2 n^2 + 4 doubles
   cudaStream_t stream = nullptr;
   int last_launches = 0;
+  bool profiling = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
   void free_all() {
     void* ptrs[] = {d_shells, d_prims, d_comps, d_pts,  d_batches, d_cand,  d_cand_loc, d_bao,   d_order,
@@ -76,6 +78,8 @@ struct Entry {
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_stage) cudaFreeHost(h_stage);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
     *this = Entry();
   }
@@ -332,6 +336,7 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
   A.max_m = e.max_m;
   const DevGrid G = dev_grid(e);
   cudaError_t err;
+  const bool prof = e.profiling && e.ev0 && e.ev1;
   if (precision == CALCHEM_XC_MIXED) {
     if (cudaMemsetAsync(e.d_counter + 1, 0, sizeof(int), st) != cudaSuccess) return -5;
     if (launch_mixed_prepare(Pa, e.n_ao, e.d_mixed_ws, st) != cudaSuccess) return -5;
@@ -344,11 +349,15 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
     A.slab = e.d_mixed_slab;
     A.slab_stride = e.mixed_slab_stride;
     A.Pa = (const double*)e.d_mixed_ws;  // the tensor-core kernel reads the split copies
+    if (prof) cudaEventRecord(e.ev0, st);
     err = launch_mixed(G, A, e.mixed_ctas, st);
+    if (prof) cudaEventRecord(e.ev1, st);
   } else {
     A.slab = e.d_slab;
     A.slab_stride = e.slab_stride;
+    if (prof) cudaEventRecord(e.ev0, st);
     err = launch_fp64(G, A, e.n_ctas, st);
+    if (prof) cudaEventRecord(e.ev1, st);
   }
   if (err != cudaSuccess) return -5;
   ++launches;
@@ -719,6 +728,26 @@ int calchem_xc_last_launch_count(uint64_t grid_id) {
   std::lock_guard<std::mutex> lk(g_mu);
   Entry* e = find(grid_id);
   return e ? e->last_launches : -2;
+}
+
+int calchem_xc_set_profiling(uint64_t grid_id, int enable) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (enable && !e->ev0) {
+    if (cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) return -5;
+  }
+  e->profiling = enable != 0;
+  return 0;
+}
+
+int calchem_xc_last_kernel_ms(uint64_t grid_id, float* ms_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (!ms_out || !e->profiling || !e->ev1) return -1;
+  if (cudaEventSynchronize(e->ev1) != cudaSuccess) return -5;
+  return cudaEventElapsedTime(ms_out, e->ev0, e->ev1) == cudaSuccess ? 0 : -5;
 }
 
 }  // extern "C"

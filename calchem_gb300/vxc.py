@@ -48,6 +48,12 @@ def is_cuda_available() -> bool:
     return _native.load().calchem_cuda_is_available() == 1
 
 
+def _xc_code(func) -> int:
+    if isinstance(func, str):
+        return int(XcFunctional.from_name(func))
+    return int(XcFunctional(func))
+
+
 def _as_matrix(m, n):
     a = np.ascontiguousarray(m, dtype=np.float64)
     if a.shape != (n, n):
@@ -171,7 +177,7 @@ class RksVxcEngine(_EngineBase):
         ne = np.zeros(1)
         prec = self.precision if precision is None else _PRECISION[precision]
         _native.check("calchem_xc_evaluate_rks", lib.calchem_xc_evaluate_rks(
-            self.grid_id, int(XcFunctional(func)), prec, _native.ptr(P), _native.ptr(exc), _native.ptr(ne),
+            self.grid_id, _xc_code(func), prec, _native.ptr(P), _native.ptr(exc), _native.ptr(ne),
             _native.ptr(V)))
         self.gpu_kernel_invocations += self.last_launch_count()
         self.last_nelec = float(ne[0])
@@ -191,7 +197,7 @@ class UksVxcEngine(_EngineBase):
         ne = np.zeros(2)
         prec = self.precision if precision is None else _PRECISION[precision]
         _native.check("calchem_xc_evaluate_uks", lib.calchem_xc_evaluate_uks(
-            self.grid_id, int(XcFunctional(func)), prec, _native.ptr(Pa), _native.ptr(Pb), _native.ptr(exc),
+            self.grid_id, _xc_code(func), prec, _native.ptr(Pa), _native.ptr(Pb), _native.ptr(exc),
             _native.ptr(ne), _native.ptr(Va), _native.ptr(Vb)))
         self.gpu_kernel_invocations += self.last_launch_count()
         self.last_nelec = (float(ne[0]), float(ne[1]))

@@ -174,6 +174,12 @@ int calchem_xc_evaluate_uks_device(uint64_t grid_id, int xc_code, int precision,
 /* Number of kernel launches the last evaluate on grid_id enqueued (for launch accounting). */
 int calchem_xc_last_launch_count(uint64_t grid_id);
 
+/* Kernel timing: when enabled, every evaluate on grid_id records CUDA events on its launch stream
+ * around the main quadrature kernel; calchem_xc_last_kernel_ms synchronises on the end event and
+ * returns that kernel's duration in milliseconds. */
+int calchem_xc_set_profiling(uint64_t grid_id, int enable);
+int calchem_xc_last_kernel_ms(uint64_t grid_id, float* ms_out);
+
 /* Library version string. */
 const char* calchem_xc_version(void);
 
