@@ -21,13 +21,13 @@
 namespace cxc {
 cudaError_t launch_fp64(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st);
 cudaError_t launch_reduce(const double* part, int n_batches, double* out, int n_out, cudaStream_t st);
-cudaError_t launch_mirror(double* V, int n, cudaStream_t st);
+cudaError_t launch_mirror(double* V, int n, int from_upper, cudaStream_t st);
 size_t fp64_smem_bytes();
 int mixed_supported(int mode);
 size_t mixed_slab_doubles(int max_m);
 int mixed_ctas_per_sm();
 cudaError_t launch_mixed(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st);
-cudaError_t launch_mixed_prepare(const double* P, int n, void* Phl, cudaStream_t st);
+cudaError_t launch_mixed_prepare(const double* P, int n, void* out, int* fexp, cudaStream_t st);
 }  // namespace cxc
 
 using namespace cxc;
@@ -44,6 +44,9 @@ struct Entry {
   AoShellGpu* d_shells = nullptr;
   AoPrimGpu* d_prims = nullptr;
   AoCompGpu* d_comps = nullptr;
+  float4* d_prim_f = nullptr;
+  float2* d_comp_f = nullptr;
+  float2* d_shell_cf = nullptr;
   double* d_pts = nullptr;  // SoA x | y | z | w, n_pts each
   BatchDesc* d_batches = nullptr;
   int* d_cand = nullptr;
@@ -72,7 +75,7 @@ struct Entry {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
   void free_all() {
-    void* ptrs[] = {d_shells, d_prims, d_comps, d_pts,  d_batches, d_cand,  d_cand_loc, d_bao,   d_order,
+    void* ptrs[] = {d_shells, d_prims, d_comps, d_prim_f, d_comp_f, d_shell_cf, d_pts,  d_batches, d_cand,  d_cand_loc, d_bao,   d_order,
                     d_P,      d_Pb,    d_V,     d_Vb,   d_rg,      d_red,   d_res,      d_counter, d_slab,
                     d_mixed_ws, d_mixed_slab};
     for (void* p : ptrs)
@@ -226,7 +229,7 @@ int upload_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_pri
   total += (size_t)n_pts * 4 * sizeof(double);
   total += (size_t)nb * sizeof(BatchDesc) + (hp.cand.size() * 2 + hp.bao.size() + hp.order.size()) * sizeof(int);
   total += nn * sizeof(double) * 4;           // P, Pb, V, Vb
-  total += nn * sizeof(float) * 4;            // split density copies (mixed path)
+  total += nn * sizeof(uint2) * 2 + (size_t)n_ao * 2 * sizeof(int);  // split densities (mixed path)
   total += (size_t)n_pts * 4 * sizeof(double);  // rho / wv staging
   total += (size_t)nb * 3 * sizeof(double) + 64;
   total += slab_stride * n_ctas * sizeof(double);
@@ -247,13 +250,14 @@ int upload_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_pri
   e->mixed_ctas = mixed_ctas;
   e->mixed_slab_stride = mixed_stride;
   bool ok = dalloc(&e->d_shells, n_shells) && dalloc(&e->d_prims, n_prims) && dalloc(&e->d_comps, n_comps) &&
+            dalloc(&e->d_prim_f, n_prims) && dalloc(&e->d_comp_f, n_comps) && dalloc(&e->d_shell_cf, 3 * (size_t)n_shells) &&
             dalloc(&e->d_pts, (size_t)n_pts * 4) && dalloc(&e->d_batches, nb) && dalloc(&e->d_cand, hp.cand.size()) &&
             dalloc(&e->d_cand_loc, hp.cand_loc.size()) && dalloc(&e->d_bao, hp.bao.size()) &&
             dalloc(&e->d_order, hp.order.size()) && dalloc(&e->d_P, nn) && dalloc(&e->d_Pb, nn) &&
             dalloc(&e->d_V, nn) && dalloc(&e->d_Vb, nn) && dalloc(&e->d_rg, (size_t)n_pts * 4) &&
             dalloc(&e->d_red, (size_t)nb * 3) && dalloc(&e->d_res, 8) && dalloc(&e->d_counter, 4) &&
             dalloc(&e->d_slab, slab_stride * n_ctas) &&
-            cudaMalloc(&e->d_mixed_ws, nn * sizeof(float) * 4) == cudaSuccess &&
+            cudaMalloc(&e->d_mixed_ws, nn * sizeof(uint2) * 2 + (size_t)n_ao * 2 * sizeof(int)) == cudaSuccess &&
             dalloc(&e->d_mixed_slab, mixed_stride * mixed_ctas) &&
             cudaMallocHost((void**)&e->h_stage, (2 * nn + 8) * sizeof(double)) == cudaSuccess &&
             cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) == cudaSuccess;
@@ -271,7 +275,28 @@ int upload_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_pri
     soa[3 * (size_t)n_pts + g] = h_w ? h_w[g] : 0.0;
   }
   e->has_w = h_w != nullptr;
-  ok = cudaMemcpy(e->d_shells, h_shells, n_shells * sizeof(AoShellGpu), cudaMemcpyHostToDevice) == cudaSuccess &&
+  // float-pair copies of the basis constants: hi = float(x), lo = float(x - hi)
+  std::vector<float4> pf(n_prims);
+  for (int i = 0; i < n_prims; ++i) {
+    const float ah = (float)h_prims[i].exponent, wh = (float)h_prims[i].weighted_norm;
+    pf[i] = make_float4(ah, (float)(h_prims[i].exponent - (double)ah), wh,
+                        (float)(h_prims[i].weighted_norm - (double)wh));
+  }
+  std::vector<float2> cf(n_comps);
+  for (int i = 0; i < n_comps; ++i) {
+    const float sh = (float)h_comps[i].scale;
+    cf[i] = make_float2(sh, (float)(h_comps[i].scale - (double)sh));
+  }
+  std::vector<float2> scf(3 * (size_t)n_shells);
+  for (int i = 0; i < n_shells; ++i)
+    for (int k = 0; k < 3; ++k) {
+      const float hi = (float)h_shells[i].center[k];
+      scf[3 * (size_t)i + k] = make_float2(hi, (float)(h_shells[i].center[k] - (double)hi));
+    }
+  ok = cudaMemcpy(e->d_prim_f, pf.data(), n_prims * sizeof(float4), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(e->d_shell_cf, scf.data(), scf.size() * sizeof(float2), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(e->d_comp_f, cf.data(), n_comps * sizeof(float2), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(e->d_shells, h_shells, n_shells * sizeof(AoShellGpu), cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemcpy(e->d_prims, h_prims, n_prims * sizeof(AoPrimGpu), cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemcpy(e->d_comps, h_comps, n_comps * sizeof(AoCompGpu), cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemcpy(e->d_pts, soa.data(), soa.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
@@ -309,6 +334,9 @@ DevGrid dev_grid(const Entry& e) {
   G.cand_loc = e.d_cand_loc;
   G.batch_ao = e.d_bao;
   G.order = e.d_order;
+  G.prim_f = e.d_prim_f;
+  G.comp_f = e.d_comp_f;
+  G.shell_cf = e.d_shell_cf;
   return G;
 }
 
@@ -321,7 +349,7 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
     if (cudaMemsetAsync(Va, 0, nn * sizeof(double), st) != cudaSuccess) return -5;
     if (mode == kModeUks && cudaMemsetAsync(Vb, 0, nn * sizeof(double), st) != cudaSuccess) return -5;
   }
-  if (cudaMemsetAsync(e.d_counter, 0, sizeof(int), st) != cudaSuccess) return -5;
+  if (cudaMemsetAsync(e.d_counter, 0, 4 * sizeof(int), st) != cudaSuccess) return -5;  // queues + status
   EvalArgs A{};
   A.mode = mode;
   A.xc = xc;
@@ -338,12 +366,13 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
   cudaError_t err;
   const bool prof = e.profiling && e.ev0 && e.ev1;
   if (precision == CALCHEM_XC_MIXED) {
-    if (cudaMemsetAsync(e.d_counter + 1, 0, sizeof(int), st) != cudaSuccess) return -5;
-    if (launch_mixed_prepare(Pa, e.n_ao, e.d_mixed_ws, st) != cudaSuccess) return -5;
+    // packed fixed-point densities: [alpha n^2][beta n^2] uint2, then row exponents [alpha n][beta n]
+    uint2* pk = reinterpret_cast<uint2*>(e.d_mixed_ws);
+    int* fx = reinterpret_cast<int*>(pk + 2 * nn);
+    if (launch_mixed_prepare(Pa, e.n_ao, pk, fx, st) != cudaSuccess) return -5;
     ++launches;
     if (mode == kModeUks) {
-      if (launch_mixed_prepare(Pb, e.n_ao, (char*)e.d_mixed_ws + nn * sizeof(float) * 2, st) != cudaSuccess)
-        return -5;
+      if (launch_mixed_prepare(Pb, e.n_ao, pk + nn, fx + e.n_ao, st) != cudaSuccess) return -5;
       ++launches;
     }
     A.slab = e.d_mixed_slab;
@@ -363,10 +392,11 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
   ++launches;
   if (mode == kModeRks || mode == kModeUks) {
     if (launch_reduce(e.d_red, e.n_batches, result, mode == kModeRks ? 2 : 3, st) != cudaSuccess) return -5;
-    if (launch_mirror(Va, e.n_ao, st) != cudaSuccess) return -5;
+    const int from_upper = precision == CALCHEM_XC_MIXED ? 1 : 0;
+    if (launch_mirror(Va, e.n_ao, from_upper, st) != cudaSuccess) return -5;
     launches += 2;
     if (mode == kModeUks) {
-      if (launch_mirror(Vb, e.n_ao, st) != cudaSuccess) return -5;
+      if (launch_mirror(Vb, e.n_ao, from_upper, st) != cudaSuccess) return -5;
       ++launches;
     }
   }
@@ -656,11 +686,14 @@ int calchem_xc_evaluate_rks(uint64_t grid_id, int xc_code, int precision, const 
   int rc = enqueue_eval(*e, kModeRks, xc_code, precision, e->d_P, nullptr, e->d_V, nullptr, nullptr, nullptr,
                         e->d_res, e->stream);
   if (rc) return rc;
+  int* h_status = reinterpret_cast<int*>(e->h_stage + 2 * nn + 4);
   if (cudaMemcpyAsync(e->h_stage, e->d_V, nn * sizeof(double), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
       cudaMemcpyAsync(e->h_stage + 2 * nn, e->d_res, 2 * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
           cudaSuccess ||
+      cudaMemcpyAsync(h_status, e->d_counter + 2, sizeof(int), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
       cudaStreamSynchronize(e->stream) != cudaSuccess)
     return -5;
+  if (*h_status != 0) return -7;
   std::memcpy(h_v_out, e->h_stage, nn * sizeof(double));
   *exc_out = e->h_stage[2 * nn];
   *nelec_out = e->h_stage[2 * nn + 1];
@@ -691,8 +724,11 @@ int calchem_xc_evaluate_uks(uint64_t grid_id, int xc_code, int precision, const 
           cudaSuccess ||
       cudaMemcpyAsync(e->h_stage + 2 * nn, e->d_res, 3 * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
           cudaSuccess ||
+      cudaMemcpyAsync(reinterpret_cast<int*>(e->h_stage + 2 * nn + 4), e->d_counter + 2, sizeof(int),
+                      cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
       cudaStreamSynchronize(e->stream) != cudaSuccess)
     return -5;
+  if (*reinterpret_cast<int*>(e->h_stage + 2 * nn + 4) != 0) return -7;
   std::memcpy(h_va_out, e->h_stage, nn * sizeof(double));
   std::memcpy(h_vb_out, e->h_stage + nn, nn * sizeof(double));
   *exc_out = e->h_stage[2 * nn];

@@ -44,6 +44,12 @@ struct DevGrid {
   const int* cand_loc;     // local AO row of the candidate's first component
   const int* batch_ao;     // global AO per local row
   const int* order;        // batch processing order (cost descending)
+  // Basis constants as float pairs (hi + lo) for the FP32 AO evaluation of the tensor-core path:
+  // (exponent hi, exponent lo, weighted norm hi, weighted norm lo) per primitive and
+  // (scale hi, scale lo) per Cartesian component.
+  const float4* prim_f;
+  const float2* comp_f;
+  const float2* shell_cf;  // shell centres as float pairs, 3 per shell (x, y, z)
 };
 
 struct EvalArgs {

@@ -399,12 +399,13 @@ __global__ void __launch_bounds__(256) reduce_batches_kernel(const double* __res
   }
 }
 
-// Copy the lower triangle into the upper one (the engine returns a full symmetric matrix).
-__global__ void mirror_lower_kernel(double* __restrict__ V, int n) {
+// Completes a symmetric matrix from one triangle: from_upper = 0 copies the lower triangle into
+// the upper one (FP64 path), from_upper = 1 the upper into the lower (tensor-core path).
+__global__ void mirror_kernel(double* __restrict__ V, int n, int from_upper) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (size_t)n * n) return;
   const int i = (int)(idx / n), j = (int)(idx % n);
-  if (j > i) V[idx] = V[(size_t)j * n + i];
+  if (from_upper ? (j < i) : (j > i)) V[idx] = V[(size_t)j * n + i];
 }
 
 }  // namespace cxc
@@ -429,9 +430,9 @@ cudaError_t launch_reduce(const double* part, int n_batches, double* out, int n_
   return cudaGetLastError();
 }
 
-cudaError_t launch_mirror(double* V, int n, cudaStream_t st) {
+cudaError_t launch_mirror(double* V, int n, int from_upper, cudaStream_t st) {
   const size_t nn = (size_t)n * n;
-  mirror_lower_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(V, n);
+  mirror_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(V, n, from_upper);
   return cudaGetLastError();
 }
 

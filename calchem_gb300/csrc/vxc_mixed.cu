@@ -1,15 +1,682 @@
-// vxc_mixed.cu -- tensor-core (tcgen05) XC quadrature path.  Not yet enabled: the C ABI
-// rejects CALCHEM_XC_MIXED with -1 while mixed_supported() returns 0.
+// vxc_mixed.cu -- tensor-core (tcgen05) XC quadrature: the mixed-precision form.
+//
+// One persistent CTA (256 threads, one per SM) takes 128-point batches from a device queue.  For
+// each batch of m candidate AOs (padded to m_pad, a multiple of 128):
+//   (A) AO values and gradients in double-float arithmetic on the FP32 pipe (48-bit: error-free
+//       transformations, a table-driven exp, basis constants and coordinates as float pairs) into
+//       the CTA's scratch slab as eight [m_pad][128] planes (hi and lo of phi, d/dx, d/dy, d/dz),
+//       with the reference's screening (ao_grid.rs:182-230).  Plain FP32 AO values carry errors of
+//       a few ulp that are identical at the 302 angular points of a radial shell and so do not
+//       average out; at 48 bits they are negligible;
+//   (B) GEMM1  T[g][nu] = sum_mu Phi[g][mu] D[mu][nu]  on tcgen05: M = 128 points, N = 128 AOs
+//       per TMEM chunk, K = AOs in blocks of 64.  Every Phi row (point) and every D row is scaled
+//       by a power of two to |x| < 1 and cut into BF16 fixed-point pieces: three for Phi
+//       (multiples of 2^-7, 2^-15, 2^-23, 2^-31) and four for D, 32 bits each, and the ten products
+//       with weight down to 2^-24 are formed.  The hh products are integer multiples of 2^-14 and
+//       a 1024-term sum stays below 2^24 units,
+//       so the tensor core's FP32 accumulation (which truncates) adds them EXACTLY; the correction
+//       classes (i + j = 1; i + j = 2 and 3 for slice indices i of Phi and j of D) are at least
+//       2^8 smaller, so their truncation is below 2^-32 of T.  The three classes accumulate in
+//       separate TMEM accumulators over up to 16 K blocks (the hh sum stays exact up to K = 1024);
+//       longer contractions are combined into a fourth accumulator, and T is scaled back exactly;
+//   (C) epilogue: each thread owns one point (its TMEM lane); T = hh + corrections is kept as a
+//       double-float and rho = sum Phi T, grad rho = 2 sum grad Phi T are accumulated in
+//       double-float;
+//   (D) the functional in FP64 per point, Exc and Nelec partial sums in FP64 (vxc.rs:890-920);
+//   (E) GEMM2  W = Z^T Phi + Phi^T Z  (Z = (w v_rho / 2) Phi + (w u) . grad Phi) on lower
+//       128 x 128 AO tile pairs, K = 128 points: each operand split into three BF16 pieces
+//       x = hi + mid + lo (floating, 24 bits), twelve products per K step, the hh products in one
+//       accumulator and the corrections in another;
+//   (F) the W tile is drained from TMEM and added to V's upper triangle with FP64 atomics,
+//       coalesced across lanes; a final kernel mirrors the upper triangle into the lower.
+// Shared-memory operand tiles use the 128-byte-swizzled K-major layout; every mbarrier wait is
+// bounded, and a wait that expires sets the status flag, drains, frees TMEM and returns.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "common.cuh"
+#include "dfloat.cuh"
+#include "tc_ptx.cuh"
+#include "xc_device.cuh"
 
 namespace cxc {
 
-int mixed_supported(int) { return 0; }
-size_t mixed_slab_doubles(int) { return 1; }
+namespace {
+
+constexpr int kMT = 256;              // threads per CTA
+constexpr int kMaxMixedM = 2048;      // AOs per batch held in shared memory
+constexpr uint32_t kWaitLimit = 1u << 26;
+constexpr uint32_t kTmemCols = 512;
+constexpr int kStageBytes = 196608;   // operand staging area (12 tiles of 16 KB)
+constexpr int kOffCoef = kStageBytes;                    // float [8][128]
+constexpr int kOffDens = kOffCoef + 8 * 128 * 4;         // double [2][4][128]
+constexpr int kOffAo = kOffDens + 2 * 4 * 128 * 8;       // int [kMaxMixedM]
+constexpr int kOffRed = kOffAo + kMaxMixedM * 4;         // double [3][8]
+constexpr int kOffEg = kOffRed + 3 * 8 * 8;              // int [128]: per-point power-of-two scale
+constexpr int kOffTab = kOffEg + 128 * 4;                // df32 [64]: 2^(-j/64)
+constexpr int kOffMisc = kOffTab + 64 * 8;               // mbarrier, tmem slot, batch, flags
+constexpr int kSmemBytes = kOffMisc + 64 + 1024;         // + alignment slack
+
+__device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
+  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+
+// x = hi + mid + lo, each an RN BF16 of the remaining residual; the residuals are exact in FP32.
+__device__ __forceinline__ void split3_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(x);
+  const float r1 = x - __bfloat162float(hi);
+  mid = __float2bfloat16_rn(r1);
+  lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+}
+
+__device__ __forceinline__ void pack8x3(const float* v, uint4& hi, uint4& mid, uint4& lo) {
+  __nv_bfloat16 h[8], m[8], l[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) split3_bf16(v[k], h[k], m[k], l[k]);
+  hi = make_uint4(pack_bf16x2(h[0], h[1]), pack_bf16x2(h[2], h[3]), pack_bf16x2(h[4], h[5]), pack_bf16x2(h[6], h[7]));
+  mid = make_uint4(pack_bf16x2(m[0], m[1]), pack_bf16x2(m[2], m[3]), pack_bf16x2(m[4], m[5]), pack_bf16x2(m[6], m[7]));
+  lo = make_uint4(pack_bf16x2(l[0], l[1]), pack_bf16x2(l[2], l[3]), pack_bf16x2(l[4], l[5]), pack_bf16x2(l[6], l[7]));
+}
+
+// Fixed-point split of |x| < 1 (a double-float hi + lo) into four pieces that are multiples of
+// 2^-7, 2^-15, 2^-23 and 2^-31 with at most 8 significant bits each (exact in BF16); the residual
+// x - (h + m + l + q) is below 2^-32.
+__device__ __forceinline__ void fixsplit4(float xh, float xl, __nv_bfloat16& hi, __nv_bfloat16& mid,
+                                          __nv_bfloat16& lo, __nv_bfloat16& q) {
+  const float h = rintf(xh * 128.f) * (1.f / 128.f);
+  const float r1 = __fadd_rn(__fsub_rn(xh, h), xl);
+  const float m = rintf(r1 * 32768.f) * (1.f / 32768.f);
+  const float r2 = __fsub_rn(r1, m);
+  const float l = rintf(r2 * 8388608.f) * (1.f / 8388608.f);
+  const float r3 = __fsub_rn(r2, l);
+  const float qq = rintf(r3 * 2147483648.f) * (1.f / 2147483648.f);
+  hi = __float2bfloat16_rn(h);
+  mid = __float2bfloat16_rn(m);
+  lo = __float2bfloat16_rn(l);
+  q = __float2bfloat16_rn(qq);
+}
+
+__device__ __forceinline__ uint4 pack8v(const __nv_bfloat16* v) {
+  return make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]), pack_bf16x2(v[6], v[7]));
+}
+
+// Byte offset of 16-byte chunk c (0..7) of row r in a 128-byte-swizzled K-major tile.
+__device__ __forceinline__ uint32_t sw128(int r, int c) { return (uint32_t)(r * 128 + ((c ^ (r & 7)) << 4)); }
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint4 v) {
+  asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+               : "memory");
+}
+
+// (A) AO values and gradients in double-float.  Planes p = 0..3 (phi, d/dx, d/dy, d/dz) hold the
+// hi parts at planes + p * P and the lo parts at planes + (4 + p) * P; row = local AO, column = point.
+__device__ void ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restrict__ planes, size_t P, int m_pad,
+                           const df32* tab) {
+  const int tid = threadIdx.x;
+  const int g = tid & 127;
+  const bool live = g < bd.n_pts;
+  df32 X = {0.f, 0.f}, Y = {0.f, 0.f}, Zc = {0.f, 0.f};
+  if (live) {
+    X = df_from_double(G.px[bd.pt_start + g]);
+    Y = df_from_double(G.py[bd.pt_start + g]);
+    Zc = df_from_double(G.pz[bd.pt_start + g]);
+  }
+  for (int ci = tid >> 7; ci < bd.n_cand; ci += kMT / 128) {
+    const int si = G.cand_shells[bd.cand_start + ci];
+    const AoShellGpu sh = G.shells[si];
+    const int loc = G.cand_loc[bd.cand_start + ci];
+    df32 dx = {0.f, 0.f}, dy = {0.f, 0.f}, dz = {0.f, 0.f}, r0 = {0.f, 0.f}, r1 = {0.f, 0.f};
+    bool on = false;
+    if (live) {
+      const float2 cx = G.shell_cf[3 * si], cy = G.shell_cf[3 * si + 1], cz = G.shell_cf[3 * si + 2];
+      dx = df_sub(X, df32{cx.x, cx.y});
+      dy = df_sub(Y, df32{cy.x, cy.y});
+      dz = df_sub(Zc, df32{cz.x, cz.y});
+      const df32 r2 = df_add(df_add(df_mul(dx, dx), df_mul(dy, dy)), df_mul(dz, dz));
+      if (!(r2.hi > (float)sh.r2_cutoff)) {
+        for (int p = 0; p < sh.n_prims; ++p) {
+          const float4 pf = G.prim_f[sh.prim_start + p];  // (a_hi, a_lo, w_hi, w_lo)
+          const df32 a = {pf.x, pf.y};
+          const df32 e = df_mul(df32{pf.z, pf.w}, df_exp_neg(df_mul(a, r2), tab));
+          r0 = df_add(r0, e);
+          const df32 ae = df_mul(a, e);
+          r1 = df_sub(r1, df_add(ae, ae));
+        }
+        on = !(fabsf(r0.hi) < 1e-18f && fabsf(r1.hi) < 1e-18f);
+      }
+    }
+    for (int c = 0; c < sh.n_funcs; ++c) {
+      df32 v = {0.f, 0.f}, gx = {0.f, 0.f}, gy = {0.f, 0.f}, gz = {0.f, 0.f};
+      if (on) {
+        const AoCompGpu cp = G.comps[sh.comp_start + c];
+        const float2 sc = G.comp_f[sh.comp_start + c];
+        const df32 s = {sc.x, sc.y};
+        // x^l and its derivative l x^(l-1)
+        df32 px = {1.f, 0.f}, dpx = {0.f, 0.f}, py = {1.f, 0.f}, dpy = {0.f, 0.f}, pz = {1.f, 0.f}, dpz = {0.f, 0.f};
+        if (cp.lx >= 1) { dpx = px; px = dx; }
+        if (cp.lx >= 2) { dpx = df_mul_f(dx, 2.f); px = df_mul(dx, dx); }
+        if (cp.lx >= 3) { dpx = df_mul_f(px, 3.f); px = df_mul(px, dx); }
+        if (cp.ly >= 1) { dpy = py; py = dy; }
+        if (cp.ly >= 2) { dpy = df_mul_f(dy, 2.f); py = df_mul(dy, dy); }
+        if (cp.ly >= 3) { dpy = df_mul_f(py, 3.f); py = df_mul(py, dy); }
+        if (cp.lz >= 1) { dpz = pz; pz = dz; }
+        if (cp.lz >= 2) { dpz = df_mul_f(dz, 2.f); pz = df_mul(dz, dz); }
+        if (cp.lz >= 3) { dpz = df_mul_f(pz, 3.f); pz = df_mul(pz, dz); }
+        const df32 yz = df_mul(py, pz), xz = df_mul(px, pz), xy = df_mul(px, py);
+        const df32 mm = df_mul(px, yz);
+        const df32 mr1 = df_mul(mm, r1);
+        v = df_mul(s, df_mul(mm, r0));
+        gx = df_mul(s, df_add(df_mul(df_mul(dpx, yz), r0), df_mul(mr1, dx)));
+        gy = df_mul(s, df_add(df_mul(df_mul(dpy, xz), r0), df_mul(mr1, dy)));
+        gz = df_mul(s, df_add(df_mul(df_mul(dpz, xy), r0), df_mul(mr1, dz)));
+        if (!(fabsf(v.hi) > 1e-16f || fabsf(gx.hi) > 1e-16f || fabsf(gy.hi) > 1e-16f || fabsf(gz.hi) > 1e-16f))
+          v = gx = gy = gz = df32{0.f, 0.f};
+      }
+      const size_t o = (size_t)(loc + c) * 128 + g;
+      planes[o] = v.hi;
+      planes[P + o] = gx.hi;
+      planes[2 * P + o] = gy.hi;
+      planes[3 * P + o] = gz.hi;
+      planes[4 * P + o] = v.lo;
+      planes[5 * P + o] = gx.lo;
+      planes[6 * P + o] = gy.lo;
+      planes[7 * P + o] = gz.lo;
+    }
+  }
+  // zero the padding rows [m, m_pad)
+  const int pad = (m_pad - bd.m) * 128;
+  for (int e = tid; e < pad; e += kMT) {
+    const size_t o = (size_t)bd.m * 128 + e;
+#pragma unroll
+    for (int p = 0; p < 8; ++p) planes[p * P + o] = 0.f;
+  }
+}
+
+// GEMM1 operands for K block kb and N chunk [nc, nc + 128):
+//   A = Phi[g][mu] 2^-e_g (double-float planes) in fixed-point pieces hi / mid / lo / q at
+//       +0 / +16K / +32K / +112K,
+//   B = D[nu][mu] 2^-f_nu pieces hi / mid / lo / lo2 at +48K / +64K / +80K / +96K,
+// B gathered from the packed fixed-point density (x = hi | mid << 16, y = lo | lo2 << 16).
+__device__ void produce_g1(unsigned char* stage, const float* __restrict__ planes, size_t P,
+                           const uint2* __restrict__ Dp, const int* s_ao, const int* s_eg, int n, int m, int kb,
+                           int nc) {
+  const int tid = threadIdx.x;
+  const uint32_t sbase = smem_addr(stage);
+  for (int e = tid; e < 128 * 8; e += kMT) {
+    const int g = e & 127, c = e >> 7;
+    const int mu0 = kb * 64 + c * 8;
+    const int eg = s_eg[g];
+    __nv_bfloat16 h[8], md[8], l[8], q[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const size_t o = (size_t)(mu0 + k) * 128 + g;
+      fixsplit4(ldexpf(planes[o], -eg), ldexpf(planes[4 * P + o], -eg), h[k], md[k], l[k], q[k]);
+    }
+    const uint32_t off = sw128(g, c);
+    st_shared_v4(sbase + off, pack8v(h));
+    st_shared_v4(sbase + 16384 + off, pack8v(md));
+    st_shared_v4(sbase + 32768 + off, pack8v(l));
+    st_shared_v4(sbase + 114688 + off, pack8v(q));
+  }
+  for (int e = tid; e < 128 * 8; e += kMT) {
+    const int c = e & 7, r = e >> 3;
+    const int nu = nc + r;
+    const int mu0 = kb * 64 + c * 8;
+    uint32_t hw[4] = {0, 0, 0, 0}, mw[4] = {0, 0, 0, 0}, lw[4] = {0, 0, 0, 0}, qw[4] = {0, 0, 0, 0};
+    if (nu < m) {
+      const uint2* row = Dp + (size_t)s_ao[nu] * n;
+#pragma unroll
+      for (int k = 0; k < 8; k += 2) {
+        const uint2 a = (mu0 + k < m) ? __ldg(row + s_ao[mu0 + k]) : make_uint2(0u, 0u);
+        const uint2 b = (mu0 + k + 1 < m) ? __ldg(row + s_ao[mu0 + k + 1]) : make_uint2(0u, 0u);
+        hw[k >> 1] = (a.x & 0xFFFFu) | (b.x << 16);
+        mw[k >> 1] = (a.x >> 16) | (b.x & 0xFFFF0000u);
+        lw[k >> 1] = (a.y & 0xFFFFu) | (b.y << 16);
+        qw[k >> 1] = (a.y >> 16) | (b.y & 0xFFFF0000u);
+      }
+    }
+    const uint32_t off = sw128(r, c);
+    st_shared_v4(sbase + 49152 + off, make_uint4(hw[0], hw[1], hw[2], hw[3]));
+    st_shared_v4(sbase + 65536 + off, make_uint4(mw[0], mw[1], mw[2], mw[3]));
+    st_shared_v4(sbase + 81920 + off, make_uint4(lw[0], lw[1], lw[2], lw[3]));
+    st_shared_v4(sbase + 98304 + off, make_uint4(qw[0], qw[1], qw[2], qw[3]));
+  }
+}
+
+// GEMM2 operands for AO tiles I (rows of A) and J (rows of B), points [64 kb2, 64 kb2 + 64).
+// Images in the slab: 0..2 = Phi^T hi/mid/lo, 3..5 = Z^T hi/mid/lo, each [m_pad][128] BF16.
+// Stage tiles (16 KB each): 0..2 Z_I, 3..5 Phi_I, 6..8 Phi_J, 9..11 Z_J (hi, mid, lo).
+__device__ void produce_g2(unsigned char* stage, const __nv_bfloat16* __restrict__ img, size_t IP, int I, int J,
+                           int kb2) {
+  const int tid = threadIdx.x;
+  const uint32_t sbase = smem_addr(stage);
+  for (int e = tid; e < 12 * 128 * 8; e += kMT) {
+    const int t = e >> 10, r = (e >> 3) & 127, c = e & 7;
+    const int piece = t % 3, group = t / 3;               // group: 0 Z_I, 1 Phi_I, 2 Phi_J, 3 Z_J
+    const int img_id = ((group == 0 || group == 3) ? 3 : 0) + piece;
+    const int row = (group < 2 ? I : J) + r;
+    // plain (coherent) load: the images are written earlier in this kernel by this CTA
+    const uint4 v = *reinterpret_cast<const uint4*>(img + img_id * IP + (size_t)row * 128 + kb2 * 64 + c * 8);
+    st_shared_v4(sbase + t * 16384 + sw128(r, c), v);
+  }
+}
+
+__device__ __forceinline__ double cta_sum(double v, double* red_row) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red_row[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < kMT / 32; ++k) s += red_row[k];
+  return s;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* stage = base;
+  float(*coef)[128] = reinterpret_cast<float(*)[128]>(base + kOffCoef);
+  double(*dens)[4][128] = reinterpret_cast<double(*)[4][128]>(base + kOffDens);
+  int* s_ao = reinterpret_cast<int*>(base + kOffAo);
+  double(*red)[8] = reinterpret_cast<double(*)[8]>(base + kOffRed);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(base + kOffMisc);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffMisc + 8);
+  int* s_batch = reinterpret_cast<int*>(base + kOffMisc + 12);
+  int* s_eg = reinterpret_cast<int*>(base + kOffEg);
+  df32* s_tab = reinterpret_cast<df32*>(base + kOffTab);
+
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int g = tid & 127, h = tid >> 7;
+  const int n = G.n_ao;
+  const bool uks = A.mode == kModeUks;
+  const int nspin = uks ? 2 : 1;
+
+  if (tid == 0) {
+    mbar_init(mbar, 1);
+    fence_mbar_init();
+  }
+  if (tid < 64) s_tab[tid] = df_from_double(exp2(-(double)tid / 64.0));
+  if (warp == 0) {
+    tmem_alloc(tmem_slot, kTmemCols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+  // TMEM: GEMM1 uses four 128-column accumulators (hh, hm+mh, hl+mm+lh, running sum); GEMM2, which
+  // runs after GEMM1 is finished, reuses the first two for its hh products and its corrections.
+  const uint32_t tH = tmem, tC1 = tmem + 128, tC2 = tmem + 256, tS = tmem + 384;
+  const uint32_t tW = tmem;
+  const uint32_t tWc = tmem + 128;
+  uint32_t phase = 0;
+  bool failed = false;
+
+  const int m_pad_all = (A.max_m + 127) / 128 * 128;
+  const size_t P = (size_t)m_pad_all * 128;  // floats per plane
+  float* planes = reinterpret_cast<float*>(A.slab + (size_t)blockIdx.x * A.slab_stride);
+  __nv_bfloat16* img = reinterpret_cast<__nv_bfloat16*>(planes + 8 * P);  // 6 images of P bf16
+  const uint2* Dhl_a = reinterpret_cast<const uint2*>(A.Pa);
+  const uint2* Dhl_b = Dhl_a + (size_t)n * n;
+  const int* fexp_a = reinterpret_cast<const int*>(Dhl_a + 2 * (size_t)n * n);
+  const int* fexp_b = fexp_a + n;
+
+  // one MMA round: wait for the commit of the phase just issued
+  auto wait_mma = [&]() -> bool {
+    bool ok = mbar_wait_bounded(mbar, phase, kWaitLimit);
+    phase ^= 1u;
+    tc_fence_after();
+    return __syncthreads_or(!ok) == 0;
+  };
+
+  while (!failed) {
+    if (tid == 0) *s_batch = atomicAdd(A.counter + 1, 1);
+    __syncthreads();
+    const int q = *s_batch;
+    __syncthreads();
+    if (q >= G.n_batches) break;
+    const int b = G.order[q];
+    const BatchDesc bd = G.batches[b];
+    const int m = bd.m;
+    const int m_pad = (m + 127) / 128 * 128;
+    for (int i = tid; i < m; i += kMT) s_ao[i] = G.batch_ao[bd.ao_start + i];
+    ao_eval_df(G, bd, planes, P, m_pad, s_tab);
+    __syncthreads();
+    {  // e_g: power-of-two exponent with max_mu |Phi[g][mu]| 2^-e_g < 1
+      float mx = 0.f;
+      for (int i = h; i < m; i += 2) mx = fmaxf(mx, fabsf(planes[(size_t)i * 128 + g]));
+      dens[0][0][g + 128 * h] = (double)mx;  // scratch
+      __syncthreads();
+      if (h == 0) {
+        int ex = 0;
+        frexpf(fmaxf((float)dens[0][0][g], (float)dens[0][0][g + 128]), &ex);
+        s_eg[g] = ex;
+      }
+      __syncthreads();
+    }
+
+    double spin_rho[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    for (int s = 0; s < nspin && !failed; ++s) {
+      const uint2* Dhl = s ? Dhl_b : Dhl_a;
+      const int* fexp = s ? fexp_b : fexp_a;
+      const int eg = s_eg[g];
+      df32 dr = {0.f, 0.f}, dgx = {0.f, 0.f}, dgy = {0.f, 0.f}, dgz = {0.f, 0.f};
+      const int nkb = m_pad / 64;
+      const uint32_t idesc = idesc_bf16_f32(128, 128);
+      for (int nc = 0; nc < m_pad && !failed; nc += 128) {
+        for (int kb = 0; kb < nkb; ++kb) {
+          produce_g1(stage, planes, P, Dhl, s_ao, s_eg, n, m, kb, nc);
+          fence_proxy_async_smem();
+          __syncthreads();
+          if (tid == 0) {
+            tc_fence_after();
+            const uint32_t sb = smem_addr(stage);
+            const uint64_t ah = sdesc_sw128(sb), am = sdesc_sw128(sb + 16384), al = sdesc_sw128(sb + 32768);
+            const uint64_t aq = sdesc_sw128(sb + 114688);
+            const uint64_t bh = sdesc_sw128(sb + 49152), bm = sdesc_sw128(sb + 65536), bl = sdesc_sw128(sb + 81920);
+            const uint64_t bq = sdesc_sw128(sb + 98304);
+            const bool group_start = (kb & 15) == 0;
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              const uint64_t o = (uint64_t)(ks * 2);  // 32 bytes per K step of 16 BF16
+              const uint32_t acc0 = (!group_start || ks > 0) ? 1u : 0u;
+              mma_bf16_ss(tH, ah + o, bh + o, idesc, acc0);   // weight 1
+              mma_bf16_ss(tC1, ah + o, bm + o, idesc, acc0);  // weight 2^-8
+              mma_bf16_ss(tC1, am + o, bh + o, idesc, 1u);
+              mma_bf16_ss(tC2, ah + o, bl + o, idesc, acc0);  // weight 2^-16
+              mma_bf16_ss(tC2, am + o, bm + o, idesc, 1u);
+              mma_bf16_ss(tC2, al + o, bh + o, idesc, 1u);
+              mma_bf16_ss(tC2, ah + o, bq + o, idesc, 1u);    // weight 2^-24
+              mma_bf16_ss(tC2, am + o, bl + o, idesc, 1u);
+              mma_bf16_ss(tC2, al + o, bm + o, idesc, 1u);
+              mma_bf16_ss(tC2, aq + o, bh + o, idesc, 1u);
+            }
+            mma_commit(mbar);
+          }
+          if (!wait_mma()) { failed = true; break; }
+          const bool group_end = ((kb & 15) == 15) || kb == nkb - 1;
+          if (!group_end) continue;
+          const bool first_group = kb < 16, last_group = kb == nkb - 1;
+          // this thread: point g, columns [64 h, 64 h + 64) of the chunk.  T = S + hh + corrections:
+          // hh is exact, the corrections are >= 2^8 smaller, so T is formed as a double-float.
+          for (int c0 = h * 64; c0 < h * 64 + 64; c0 += 16) {
+            float a[16], b[16];
+            tmem_ld16(tH + lane_base + (uint32_t)c0, a);
+            tmem_ld16(tC1 + lane_base + (uint32_t)c0, b);
+            float cc[16];
+            tmem_ld16(tC2 + lane_base + (uint32_t)c0, cc);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) b[j] += cc[j];  // corrections (small)
+            if (!first_group) {
+              tmem_ld16(tS + lane_base + (uint32_t)c0, cc);
+            }
+            if (!last_group) {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) a[j] = (first_group ? 0.f : cc[j]) + a[j] + b[j];
+              tmem_st16(tS + lane_base + (uint32_t)c0, a);
+            } else {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                const int nu = nc + c0 + j;
+                df32 t = first_group ? two_sum(a[j], b[j]) : df_add_f(two_sum(cc[j], a[j]), b[j]);
+                t = nu < m ? df_ldexp(t, eg + fexp[s_ao[nu]]) : df32{0.f, 0.f};
+                const size_t o = (size_t)nu * 128 + g;
+                dr = df_add(dr, df_mul(df32{planes[o], planes[4 * P + o]}, t));
+                dgx = df_add(dgx, df_mul(df32{planes[P + o], planes[5 * P + o]}, t));
+                dgy = df_add(dgy, df_mul(df32{planes[2 * P + o], planes[6 * P + o]}, t));
+                dgz = df_add(dgz, df_mul(df32{planes[3 * P + o], planes[7 * P + o]}, t));
+              }
+            }
+          }
+          tc_fence_before();
+          __syncthreads();
+        }
+      }
+      double acc[4] = {df_to_double(dr), df_to_double(dgx), df_to_double(dgy), df_to_double(dgz)};
+      if (failed) break;
+      for (int k = 0; k < 4; ++k) dens[h][k][g] = acc[k];
+      __syncthreads();
+      for (int k = 0; k < 4; ++k) spin_rho[s][k] = dens[0][k][g] + dens[1][k][g];
+      __syncthreads();
+    }
+    if (failed) break;
+
+    // (D) functional, one thread per point (threads with h == 0)
+    double e_loc = 0, na_loc = 0, nb_loc = 0;
+    if (h == 0) {
+      const bool live = g < bd.n_pts;
+      for (int k = 0; k < 8; ++k) coef[k][g] = 0.f;
+      const double ra = spin_rho[0][0];
+      const double gax = 2.0 * spin_rho[0][1], gay = 2.0 * spin_rho[0][2], gaz = 2.0 * spin_rho[0][3];
+      const size_t pt = (size_t)bd.pt_start + g;
+      if (!uks) {
+        if (live && !(ra < 1e-18)) {
+          const double w = G.pw[pt];
+          const double rs = 0.5 * ra;
+          const double gss = 0.25 * (gax * gax + gay * gay + gaz * gaz);
+          const XcVal o = xc_eval(A.xc, rs, rs, gss, gss, gss);
+          e_loc = w * o.f;
+          na_loc = w * ra;
+          const double us = w * (o.vgaa + 0.5 * o.vgab);
+          coef[0][g] = (float)(0.5 * w * o.vra);
+          coef[1][g] = (float)(us * gax);
+          coef[2][g] = (float)(us * gay);
+          coef[3][g] = (float)(us * gaz);
+        }
+      } else {
+        const double rb0 = spin_rho[1][0];
+        const double gbx = 2.0 * spin_rho[1][1], gby = 2.0 * spin_rho[1][2], gbz = 2.0 * spin_rho[1][3];
+        const double rpa = fmax(ra, 0.0), rpb = fmax(rb0, 0.0);
+        if (live && !(rpa + rpb < 1e-18)) {
+          const double w = G.pw[pt];
+          const double gaa = gax * gax + gay * gay + gaz * gaz;
+          const double gab = gax * gbx + gay * gby + gaz * gbz;
+          const double gbb = gbx * gbx + gby * gby + gbz * gbz;
+          const XcVal o = xc_eval(A.xc, rpa, rpb, gaa, gab, gbb);
+          e_loc = w * o.f;
+          na_loc = w * rpa;
+          nb_loc = w * rpb;
+          coef[0][g] = (float)(0.5 * w * o.vra);
+          coef[1][g] = (float)(w * (2.0 * o.vgaa * gax + o.vgab * gbx));
+          coef[2][g] = (float)(w * (2.0 * o.vgaa * gay + o.vgab * gby));
+          coef[3][g] = (float)(w * (2.0 * o.vgaa * gaz + o.vgab * gbz));
+          coef[4][g] = (float)(0.5 * w * o.vrb);
+          coef[5][g] = (float)(w * (2.0 * o.vgbb * gbx + o.vgab * gax));
+          coef[6][g] = (float)(w * (2.0 * o.vgbb * gby + o.vgab * gay));
+          coef[7][g] = (float)(w * (2.0 * o.vgbb * gbz + o.vgab * gaz));
+        }
+      }
+    }
+    __syncthreads();
+    {
+      const double es = cta_sum(e_loc, red[0]);
+      const double nas = cta_sum(na_loc, red[1]);
+      const double nbs = cta_sum(nb_loc, red[2]);
+      if (tid == 0) {
+        A.batch_red[3 * (size_t)b] = es;
+        A.batch_red[3 * (size_t)b + 1] = nas;
+        A.batch_red[3 * (size_t)b + 2] = nbs;
+      }
+    }
+
+    // (E)+(F) per spin: images Phi^T / Z^T, then lower tile pairs of W
+    for (int s = 0; s < nspin && !failed; ++s) {
+      for (int e = tid; e < m_pad * 16; e += kMT) {
+        const int mu = e >> 4, c = e & 15;
+        const size_t o = (size_t)mu * 128 + c * 8;
+        float ph[8], zz[8];
+        const float4 p0 = *reinterpret_cast<const float4*>(planes + o);
+        const float4 p1 = *reinterpret_cast<const float4*>(planes + o + 4);
+        const float4 x0 = *reinterpret_cast<const float4*>(planes + P + o);
+        const float4 x1 = *reinterpret_cast<const float4*>(planes + P + o + 4);
+        const float4 y0 = *reinterpret_cast<const float4*>(planes + 2 * P + o);
+        const float4 y1 = *reinterpret_cast<const float4*>(planes + 2 * P + o + 4);
+        const float4 z0 = *reinterpret_cast<const float4*>(planes + 3 * P + o);
+        const float4 z1 = *reinterpret_cast<const float4*>(planes + 3 * P + o + 4);
+        ph[0] = p0.x; ph[1] = p0.y; ph[2] = p0.z; ph[3] = p0.w; ph[4] = p1.x; ph[5] = p1.y; ph[6] = p1.z; ph[7] = p1.w;
+        const float dxv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+        const float dyv[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+        const float dzv[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int gg = c * 8 + k;
+          zz[k] = coef[4 * s][gg] * ph[k] + coef[4 * s + 1][gg] * dxv[k] + coef[4 * s + 2][gg] * dyv[k] +
+                  coef[4 * s + 3][gg] * dzv[k];
+        }
+        uint4 hi, mid, lo;
+        if (s == 0) {
+          pack8x3(ph, hi, mid, lo);
+          *reinterpret_cast<uint4*>(img + o) = hi;
+          *reinterpret_cast<uint4*>(img + P + o) = mid;
+          *reinterpret_cast<uint4*>(img + 2 * P + o) = lo;
+        }
+        pack8x3(zz, hi, mid, lo);
+        *reinterpret_cast<uint4*>(img + 3 * P + o) = hi;
+        *reinterpret_cast<uint4*>(img + 4 * P + o) = mid;
+        *reinterpret_cast<uint4*>(img + 5 * P + o) = lo;
+      }
+      __syncthreads();
+      double* V = s ? A.Vb : A.Va;
+      const uint32_t idesc = idesc_bf16_f32(128, 128);
+      for (int I = 0; I < m_pad && !failed; I += 128) {
+        for (int J = 0; J <= I && !failed; J += 128) {
+          for (int kb2 = 0; kb2 < 2; ++kb2) {
+            produce_g2(stage, img, P, I, J, kb2);
+            fence_proxy_async_smem();
+            __syncthreads();
+            if (tid == 0) {
+              tc_fence_after();
+              const uint32_t sb = smem_addr(stage);
+              uint64_t d[12];
+#pragma unroll
+              for (int t = 0; t < 12; ++t) d[t] = sdesc_sw128(sb + t * 16384);
+              // d[0..2] Z_I, d[3..5] Phi_I, d[6..8] Phi_J, d[9..11] Z_J (hi, mid, lo)
+#pragma unroll
+              for (int ks = 0; ks < 4; ++ks) {
+                const uint64_t o = (uint64_t)(ks * 2);
+                const uint32_t acc = (kb2 > 0 || ks > 0) ? 1u : 0u;
+                mma_bf16_ss(tW, d[0] + o, d[6] + o, idesc, acc);
+                mma_bf16_ss(tW, d[3] + o, d[9] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[0] + o, d[7] + o, idesc, acc);
+                mma_bf16_ss(tWc, d[1] + o, d[6] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[0] + o, d[8] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[1] + o, d[7] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[2] + o, d[6] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[3] + o, d[10] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[4] + o, d[9] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[3] + o, d[11] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[4] + o, d[10] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[5] + o, d[9] + o, idesc, 1u);
+              }
+              mma_commit(mbar);
+            }
+            if (!wait_mma()) { failed = true; break; }
+          }
+          if (failed) break;
+          // drain: lane = AO row i of tile I, this half's 64 columns of tile J
+          const int i = I + g;
+          for (int c0 = h * 64; c0 < h * 64 + 64; c0 += 32) {
+            float wv[32], wc[32];
+            tmem_ld32(tW + lane_base + (uint32_t)c0, wv);
+            tmem_ld32(tWc + lane_base + (uint32_t)c0, wc);
+#pragma unroll
+            for (int jj = 0; jj < 32; ++jj) wv[jj] += wc[jj];
+            if (i < m) {
+              const int ai = s_ao[i];
+#pragma unroll
+              for (int jj = 0; jj < 32; ++jj) {
+                const int j = J + c0 + jj;
+                if (j < m && (I != J || i >= j)) {
+                  const int aj = s_ao[j];
+                  const int r = ai < aj ? ai : aj, c = ai < aj ? aj : ai;
+                  atomicAdd(&V[(size_t)r * n + c], (double)wv[jj]);
+                }
+              }
+            }
+          }
+          tc_fence_before();
+          __syncthreads();
+        }
+      }
+    }
+  }
+
+  // teardown: on failure, give any in-flight MMA a bounded chance to finish before freeing TMEM
+  if (failed) {
+    if (tid == 0) atomicExch(A.counter + 2, 1);
+    mbar_wait_bounded(mbar, phase ^ 1u, kWaitLimit);  // the round that timed out
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+}
+
+// D (FP64, n x n) -> per-row fixed-point split: row nu is scaled by 2^-f_nu (|x| < 1) and cut into
+// multiples of 2^-7, 2^-15, 2^-23, 2^-31 (computed in FP64, each exact in BF16); packed as
+// x = hi | mid << 16, y = lo | lo2 << 16.  One CTA per row.
+__global__ void __launch_bounds__(256) split_density_kernel(const double* __restrict__ D, int n,
+                                                           uint2* __restrict__ out, int* __restrict__ fexp) {
+  __shared__ double red[256];
+  const int row = blockIdx.x;
+  const double* d = D + (size_t)row * n;
+  double mx = 0.0;
+  for (int j = threadIdx.x; j < n; j += 256) mx = fmax(mx, fabs(d[j]));
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  int f = 0;
+  frexp(red[0], &f);
+  if (threadIdx.x == 0) fexp[row] = f;
+  for (int j = threadIdx.x; j < n; j += 256) {
+    const double x = ldexp(d[j], -f);
+    const double h = rint(x * 128.0) / 128.0;
+    const double r1 = x - h;
+    const double m = rint(r1 * 32768.0) / 32768.0;
+    const double r2 = r1 - m;
+    const double l = rint(r2 * 8388608.0) / 8388608.0;
+    const double r3 = r2 - l;
+    const double q = rint(r3 * 2147483648.0) / 2147483648.0;
+    out[(size_t)row * n + j] = make_uint2(pack_bf16x2(__float2bfloat16_rn((float)h), __float2bfloat16_rn((float)m)),
+                                          pack_bf16x2(__float2bfloat16_rn((float)l), __float2bfloat16_rn((float)q)));
+  }
+}
+
+int mixed_supported(int mode) { return (mode == kModeRks || mode == kModeUks) ? 1 : 0; }
+
+size_t mixed_slab_doubles(int max_m) {
+  const size_t m_pad = (size_t)(max_m + 127) / 128 * 128;
+  return m_pad * 128 * (8 * sizeof(float) + 6 * sizeof(__nv_bfloat16)) / sizeof(double);
+}
+
 int mixed_ctas_per_sm() { return 1; }
-cudaError_t launch_mixed(const DevGrid&, const EvalArgs&, int, cudaStream_t) { return cudaErrorNotSupported; }
-cudaError_t launch_mixed_prepare(const double*, int, void*, cudaStream_t) { return cudaErrorNotSupported; }
+
+int mixed_max_m() { return kMaxMixedM; }
+
+cudaError_t launch_mixed(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st) {
+  static bool attr = false;
+  if (A.max_m > kMaxMixedM) return cudaErrorInvalidValue;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(vxc_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  vxc_mixed_kernel<<<n_ctas, kMT, kSmemBytes, st>>>(G, A);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_prepare(const double* P, int n, void* out, int* fexp, cudaStream_t st) {
+  split_density_kernel<<<n, 256, 0, st>>>(P, n, reinterpret_cast<uint2*>(out), fexp);
+  return cudaGetLastError();
+}
 
 }  // namespace cxc
