@@ -48,6 +48,8 @@ SIGNATURES = {
     "calchem_xc_last_launch_count": (_I, [_U64]),
     "calchem_xc_set_profiling": (_I, [_U64, _I]),
     "calchem_xc_last_kernel_ms": (_I, [_U64, _P]),
+    "calchem_xc_evaluate_rks_static": (_I, [_P, _I, _P, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _I, _I, _I, _P, _P,
+                                           _P, _P]),
     "calchem_xc_version": (ctypes.c_char_p, []),
 }
 

@@ -24,6 +24,7 @@ CUDA_UNITS = {
     "vxc_fp64.cu": [],
     "vxc_mixed.cu": [],
     "grid_build.cu": ["-fmad=false"],
+    "noalloc.cu": [],
 }
 CXX_UNITS = {"host_prep.cpp": []}
 

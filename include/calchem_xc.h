@@ -180,6 +180,41 @@ int calchem_xc_last_launch_count(uint64_t grid_id);
 int calchem_xc_set_profiling(uint64_t grid_id, int enable);
 int calchem_xc_last_kernel_ms(uint64_t grid_id, float* ms_out);
 
+/* ======================================================================================
+ * (4) Evaluation without device allocation.  No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc -- a framework that owns all device memory through its own
+ * pool, or a serving loop that must not take cudaMalloc's implicit device synchronisation in the
+ * middle of an SCF iteration.
+ * ====================================================================================== */
+
+/* Size of the library's fixed device working buffer (a static device array held by every GPU that
+ * loads the library until the process exits). */
+#define CALCHEM_XC_STATIC_SCRATCH_BYTES ((size_t)96 << 20)
+
+/* Closed-shell FP64 evaluation (same results as calchem_xc_evaluate_rks with precision FP64) where
+ * every input and output is a device buffer owned by the caller, in the reference's upload layout:
+ * shells / prims / comps, points grouped by non-decreasing batch_id (<= 128 per batch) with their
+ * quadrature weights, the per-batch candidate-shell CSR lists, max_batch_ao = the largest number of
+ * AOs of any batch, d_total (n_ao x n_ao), d_result (Exc, Nelec) and d_v (n_ao x n_ao, full symmetric).
+ * All working memory comes from the static buffer above; nothing is allocated.
+ *   - The first call on a device looks up the buffer's device address (cudaGetSymbolAddress); make
+ *     that first call before any stream capture on that device.
+ *   - Work on `stream` (a cudaStream_t, 0 for the legacy stream); returns after it completes.
+ *   - Returns -3 when the points, tables and one CTA's working set do not fit in the buffer
+ *     (large n_pts or max_batch_ao), -2 when the layout is inconsistent (a batch of more than 128
+ *     points, a shell index or range out of bounds, a batch with more than max_batch_ao AOs), -1
+ *     for null pointers or non-positive sizes, -5 for a launch or copy failure.
+ *   - Every call shares the buffer and finds the previous call's contents in it (the work-queue head
+ *     and status word are cleared on entry, the rest is overwritten before use).  Calls through this
+ *     entry point are serialised and synchronous, so they never overlap; GPU work that did overlap
+ *     on the buffer would race. */
+int calchem_xc_evaluate_rks_static(const AoShellGpu* d_shells, int n_shells, const AoPrimGpu* d_prims, int n_prims,
+                                   const AoCompGpu* d_comps, int n_comps, const GridPtGpu* d_pts,
+                                   const double* d_weights, int n_pts, const int* d_cand_offsets,
+                                   const int* d_cand_shells, int n_batches, int n_cand_shells, int n_ao,
+                                   int max_batch_ao, int xc_code, const double* d_total, double* d_result,
+                                   double* d_v, void* stream);
+
 /* Library version string. */
 const char* calchem_xc_version(void);
 
