@@ -1,6 +1,6 @@
 // vxc_mixed.cu -- tensor-core (tcgen05) XC quadrature: the mixed-precision form.
 //
-// One persistent CTA (256 threads, one per SM) takes 128-point batches from a device queue.  For
+// One persistent CTA (512 threads, one per SM) takes 128-point batches from a device queue.  For
 // each batch of m candidate AOs (padded to m_pad, a multiple of 128):
 //   (A) AO values and gradients in double-float arithmetic on the FP32 pipe (48-bit: error-free
 //       transformations, a table-driven exp, basis constants and coordinates as float pairs) into
@@ -45,16 +45,18 @@ namespace cxc {
 
 namespace {
 
-constexpr int kMT = 256;              // threads per CTA
+constexpr int kMT = 512;              // threads per CTA
+constexpr int kGroups = kMT / 128;    // thread groups of 128 (one thread per point in each)
+constexpr int kGroupCols = 128 / kGroups;  // TMEM columns of a 128-column chunk per group
 constexpr int kMaxMixedM = 2048;      // AOs per batch held in shared memory
 constexpr uint32_t kWaitLimit = 1u << 26;
 constexpr uint32_t kTmemCols = 512;
 constexpr int kStageBytes = 196608;   // operand staging area (12 tiles of 16 KB)
 constexpr int kOffCoef = kStageBytes;                    // float [8][128]
-constexpr int kOffDens = kOffCoef + 8 * 128 * 4;         // double [2][4][128]
-constexpr int kOffAo = kOffDens + 2 * 4 * 128 * 8;       // int [kMaxMixedM]
-constexpr int kOffRed = kOffAo + kMaxMixedM * 4;         // double [3][8]
-constexpr int kOffEg = kOffRed + 3 * 8 * 8;              // int [128]: per-point power-of-two scale
+constexpr int kOffDens = kOffCoef + 8 * 128 * 4;         // double [kGroups][4][128]
+constexpr int kOffAo = kOffDens + kGroups * 4 * 128 * 8; // int [kMaxMixedM]
+constexpr int kOffRed = kOffAo + kMaxMixedM * 4;         // double [3][kMT / 32]
+constexpr int kOffEg = kOffRed + 3 * (kMT / 32) * 8;     // int [128]: per-point power-of-two scale
 constexpr int kOffTab = kOffEg + 128 * 4;                // df32 [64]: 2^(-j/64)
 constexpr int kOffMisc = kOffTab + 64 * 8;               // mbarrier, tmem slot, batch, flags
 constexpr int kSmemBytes = kOffMisc + 64 + 1024;         // + alignment slack
@@ -252,7 +254,8 @@ __device__ void produce_g2(unsigned char* stage, const __nv_bfloat16* __restrict
                            int kb2) {
   const int tid = threadIdx.x;
   const uint32_t sbase = smem_addr(stage);
-  for (int e = tid; e < 12 * 128 * 8; e += kMT) {
+  const int n_tiles = I == J ? 6 : 12;  // a diagonal pair reads Z_I and Phi_I only
+  for (int e = tid; e < n_tiles * 128 * 8; e += kMT) {
     const int t = e >> 10, r = (e >> 3) & 127, c = e & 7;
     const int piece = t % 3, group = t / 3;               // group: 0 Z_I, 1 Phi_I, 2 Phi_J, 3 Z_J
     const int img_id = ((group == 0 || group == 3) ? 3 : 0) + piece;
@@ -281,9 +284,9 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* stage = base;
   float(*coef)[128] = reinterpret_cast<float(*)[128]>(base + kOffCoef);
-  double(*dens)[4][128] = reinterpret_cast<double(*)[4][128]>(base + kOffDens);
+  double(*dens)[4][128] = reinterpret_cast<double(*)[4][128]>(base + kOffDens);  // [kGroups]
   int* s_ao = reinterpret_cast<int*>(base + kOffAo);
-  double(*red)[8] = reinterpret_cast<double(*)[8]>(base + kOffRed);
+  double(*red)[kMT / 32] = reinterpret_cast<double(*)[kMT / 32]>(base + kOffRed);
   uint64_t* mbar = reinterpret_cast<uint64_t*>(base + kOffMisc);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffMisc + 8);
   int* s_batch = reinterpret_cast<int*>(base + kOffMisc + 12);
@@ -350,12 +353,14 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
     __syncthreads();
     {  // e_g: power-of-two exponent with max_mu |Phi[g][mu]| 2^-e_g < 1
       float mx = 0.f;
-      for (int i = h; i < m; i += 2) mx = fmaxf(mx, fabsf(planes[(size_t)i * 128 + g]));
+      for (int i = h; i < m; i += kGroups) mx = fmaxf(mx, fabsf(planes[(size_t)i * 128 + g]));
       dens[0][0][g + 128 * h] = (double)mx;  // scratch
       __syncthreads();
       if (h == 0) {
+        float t = 0.f;
+        for (int k = 0; k < kGroups; ++k) t = fmaxf(t, (float)dens[0][0][g + 128 * k]);
         int ex = 0;
-        frexpf(fmaxf((float)dens[0][0][g], (float)dens[0][0][g + 128]), &ex);
+        frexpf(t, &ex);
         s_eg[g] = ex;
       }
       __syncthreads();
@@ -403,9 +408,10 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
           const bool group_end = ((kb & 15) == 15) || kb == nkb - 1;
           if (!group_end) continue;
           const bool first_group = kb < 16, last_group = kb == nkb - 1;
-          // this thread: point g, columns [64 h, 64 h + 64) of the chunk.  T = S + hh + corrections:
-          // hh is exact, the corrections are >= 2^8 smaller, so T is formed as a double-float.
-          for (int c0 = h * 64; c0 < h * 64 + 64; c0 += 16) {
+          // this thread: point g, columns [kGroupCols h, kGroupCols (h + 1)) of the chunk.
+          // T = S + hh + corrections: hh is exact, the corrections are >= 2^8 smaller, so T is
+          // formed as a double-float.
+          for (int c0 = h * kGroupCols; c0 < (h + 1) * kGroupCols; c0 += 16) {
             float a[16], b[16];
             tmem_ld16(tH + lane_base + (uint32_t)c0, a);
             tmem_ld16(tC1 + lane_base + (uint32_t)c0, b);
@@ -442,7 +448,11 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
       if (failed) break;
       for (int k = 0; k < 4; ++k) dens[h][k][g] = acc[k];
       __syncthreads();
-      for (int k = 0; k < 4; ++k) spin_rho[s][k] = dens[0][k][g] + dens[1][k][g];
+      for (int k = 0; k < 4; ++k) {
+        double t = dens[0][k][g];
+        for (int j = 1; j < kGroups; ++j) t += dens[j][k][g];
+        spin_rho[s][k] = t;
+      }
       __syncthreads();
     }
     if (failed) break;
@@ -460,11 +470,11 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
           const double w = G.pw[pt];
           const double rs = 0.5 * ra;
           const double gss = 0.25 * (gax * gax + gay * gay + gaz * gaz);
-          const XcVal o = xc_eval(A.xc, rs, rs, gss, gss, gss);
+          const XcCs o = xc_eval_cs(A.xc, rs, gss);
           e_loc = w * o.f;
           na_loc = w * ra;
-          const double us = w * (o.vgaa + 0.5 * o.vgab);
-          coef[0][g] = (float)(0.5 * w * o.vra);
+          const double us = w * o.vg;
+          coef[0][g] = (float)(0.5 * w * o.vr);
           coef[1][g] = (float)(us * gax);
           coef[2][g] = (float)(us * gay);
           coef[3][g] = (float)(us * gaz);
@@ -556,6 +566,10 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
               uint64_t d[12];
 #pragma unroll
               for (int t = 0; t < 12; ++t) d[t] = sdesc_sw128(sb + t * 16384);
+              if (I == J) {
+#pragma unroll
+                for (int t = 0; t < 3; ++t) { d[6 + t] = d[3 + t]; d[9 + t] = d[t]; }
+              }
               // d[0..2] Z_I, d[3..5] Phi_I, d[6..8] Phi_J, d[9..11] Z_J (hi, mid, lo)
 #pragma unroll
               for (int ks = 0; ks < 4; ++ks) {
@@ -579,9 +593,9 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
             if (!wait_mma()) { failed = true; break; }
           }
           if (failed) break;
-          // drain: lane = AO row i of tile I, this half's 64 columns of tile J
+          // drain: lane = AO row i of tile I, this group's columns of tile J
           const int i = I + g;
-          for (int c0 = h * 64; c0 < h * 64 + 64; c0 += 32) {
+          for (int c0 = h * kGroupCols; c0 < (h + 1) * kGroupCols; c0 += 32) {
             float wv[32], wc[32];
             tmem_ld32(tW + lane_base + (uint32_t)c0, wv);
             tmem_ld32(tWc + lane_base + (uint32_t)c0, wc);

@@ -16,9 +16,9 @@ struct XcVal {
   double f, vra, vrb, vgaa, vgab, vgbb;
 };
 
-__device__ __forceinline__ XcVal xc_zero() { return XcVal{0, 0, 0, 0, 0, 0}; }
+__host__ __device__ __forceinline__ XcVal xc_zero() { return XcVal{0, 0, 0, 0, 0, 0}; }
 
-__device__ __forceinline__ void xc_axpy(XcVal& acc, double s, const XcVal& o) {
+__host__ __device__ __forceinline__ void xc_axpy(XcVal& acc, double s, const XcVal& o) {
   acc.f += s * o.f;
   acc.vra += s * o.vra;
   acc.vrb += s * o.vrb;
@@ -31,7 +31,7 @@ constexpr double kPiD = 3.14159265358979323846;
 constexpr double kRhoFloor = 1e-18;  // xc.rs:13
 
 // -------------------------------------------------------------------------- Slater (xc.rs:229-251)
-__device__ __forceinline__ void slater_spin(double r, double& f, double& v) {
+__host__ __device__ __forceinline__ void slater_spin(double r, double& f, double& v) {
   if (r < kRhoFloor) { f = 0.0; v = 0.0; return; }
   const double cx = 0.75 * cbrt(6.0 / kPiD);  // 3/4 (6/pi)^(1/3)
   const double r13 = cbrt(r);
@@ -42,7 +42,7 @@ __device__ __forceinline__ void slater_spin(double r, double& f, double& v) {
 // -------------------------------------------------------------------------- VWN (xc.rs:270-404)
 struct VwnChannel { double a, x0, b, c; };
 
-__device__ __forceinline__ void vwn_eps(double x, VwnChannel ch, double& eps, double& rs_deps) {
+__host__ __device__ __forceinline__ void vwn_eps(double x, VwnChannel ch, double& eps, double& rs_deps) {
   const double X = x * x + ch.b * x + ch.c;
   const double X0 = ch.x0 * ch.x0 + ch.b * ch.x0 + ch.c;
   const double q = sqrt(4.0 * ch.c - ch.b * ch.b);
@@ -53,7 +53,7 @@ __device__ __forceinline__ void vwn_eps(double x, VwnChannel ch, double& eps, do
   rs_deps = ch.a * (ch.c * dx0 - ch.b * x * ch.x0) / (dx0 * X);
 }
 
-__device__ __forceinline__ void spin_f(double zeta, double& fz, double& dfz, double& inv_fdd0) {
+__host__ __device__ __forceinline__ void spin_f(double zeta, double& fz, double& dfz, double& inv_fdd0) {
   const double c2 = cbrt(2.0) - 1.0;
   const double den = 2.0 * c2;
   inv_fdd0 = 1.0 / (4.0 / (9.0 * c2));
@@ -64,7 +64,7 @@ __device__ __forceinline__ void spin_f(double zeta, double& fz, double& dfz, dou
 }
 
 // rpa = false: VWN5 parameters; rpa = true: VWN_RPA parameters (xc.rs:291-334).
-__device__ __forceinline__ XcVal vwn_corr(double ra, double rb, bool rpa) {
+__host__ __device__ __forceinline__ XcVal vwn_corr(double ra, double rb, bool rpa) {
   XcVal o = xc_zero();
   const double rho = ra + rb;
   if (rho < kRhoFloor) return o;
@@ -96,7 +96,7 @@ __device__ __forceinline__ XcVal vwn_corr(double ra, double rb, bool rpa) {
 }
 
 // -------------------------------------------------------------------------- B88 (xc.rs:388-424)
-__device__ __forceinline__ void b88_spin(double r, double g, double& f, double& vr, double& vg) {
+__host__ __device__ __forceinline__ void b88_spin(double r, double g, double& f, double& vr, double& vg) {
   if (r < kRhoFloor) { f = vr = vg = 0.0; return; }
   const double beta = 0.0042;
   const double r13 = cbrt(r), r43 = r * r13;
@@ -112,7 +112,7 @@ __device__ __forceinline__ void b88_spin(double r, double g, double& f, double& 
 }
 
 // -------------------------------------------------------------------------- LYP (xc.rs:433-547)
-__device__ __forceinline__ void lyp_bracket_d(double ra, double rb, double delta, double ddelta, double gaa,
+__host__ __device__ __forceinline__ void lyp_bracket_d(double ra, double rb, double delta, double ddelta, double gaa,
                                               double gab, double gbb, double& s, double& ds, double& aaa,
                                               double& aab, double& abb) {
   const double rho = ra + rb, rho2 = rho * rho;
@@ -141,7 +141,7 @@ __device__ __forceinline__ void lyp_bracket_d(double ra, double rb, double delta
   ds = dstf + (dcg + dea) * gaa + (2.0 * dcg) * gab + (dcg + deb) * gbb;
 }
 
-__device__ __forceinline__ XcVal lyp_corr(double ra, double rb, double gaa, double gab, double gbb) {
+__host__ __device__ __forceinline__ XcVal lyp_corr(double ra, double rb, double gaa, double gab, double gbb) {
   XcVal o = xc_zero();
   const double rho = ra + rb;
   if (rho < kRhoFloor) return o;
@@ -183,7 +183,7 @@ constexpr double kMu = 0.2195149727645171;
 constexpr double kBetaPbe = 0.06672455060314922;
 constexpr double kGammaPbe = 0.0310906908696549;
 
-__device__ __forceinline__ void pbex_spin(double r, double g, double& f, double& vr, double& vg) {
+__host__ __device__ __forceinline__ void pbex_spin(double r, double g, double& f, double& vr, double& vg) {
   if (r < kRhoFloor) { f = vr = vg = 0.0; return; }
   const double ru = 2.0 * r, gu = 4.0 * fmax(g, 0.0);  // spin scaling to the unpolarised form
   const double cxu = -0.75 * cbrt(3.0 / kPiD);
@@ -202,7 +202,7 @@ __device__ __forceinline__ void pbex_spin(double r, double g, double& f, double&
 
 struct Pw92Channel { double a, a1, b1, b2, b3, b4; };
 
-__device__ __forceinline__ void pw92(double rs, Pw92Channel c, double& g, double& dg) {
+__host__ __device__ __forceinline__ void pw92(double rs, Pw92Channel c, double& g, double& dg) {
   const double x = sqrt(rs), x3 = rs * x, x4 = rs * rs;
   const double q0 = -2.0 * c.a * (1.0 + c.a1 * rs);
   const double q1 = 2.0 * c.a * (c.b1 * x + c.b2 * rs + c.b3 * x3 + c.b4 * x4);
@@ -212,7 +212,7 @@ __device__ __forceinline__ void pw92(double rs, Pw92Channel c, double& g, double
   dg = -2.0 * c.a * c.a1 * ln - q0 * dq1 / (q1 * (q1 + 1.0));
 }
 
-__device__ __forceinline__ XcVal pbe_corr(double ra, double rb, double gaa, double gab, double gbb) {
+__host__ __device__ __forceinline__ XcVal pbe_corr(double ra, double rb, double gaa, double gab, double gbb) {
   XcVal o = xc_zero();
   const double rho = ra + rb;
   if (rho < kRhoFloor) return o;
@@ -279,7 +279,7 @@ __device__ __forceinline__ XcVal pbe_corr(double ra, double rb, double gaa, doub
 }
 
 // -------------------------------------------------------------------------- mixtures (xc.rs:159-223)
-__device__ __forceinline__ XcVal xc_eval(int code, double rho_a, double rho_b, double g_aa, double g_ab,
+__host__ __device__ __forceinline__ XcVal xc_eval(int code, double rho_a, double rho_b, double g_aa, double g_ab,
                                          double g_bb) {
   XcVal o = xc_zero();
   const double ra = fmax(rho_a, 0.0), rb = fmax(rho_b, 0.0);
@@ -322,6 +322,171 @@ __device__ __forceinline__ XcVal xc_eval(int code, double rho_a, double rho_b, d
   if (code == 1) xc_axpy(o, 1.0, lyp_corr(ra, rb, gaa, gab, gbb));
   if (code == 3 || code == 4) xc_axpy(o, 0.81, lyp_corr(ra, rb, gaa, gab, gbb));
   if (code == 2 || code == 5) xc_axpy(o, 1.0, pbe_corr(ra, rb, gaa, gab, gbb));
+  return o;
+}
+
+// -------------------------------------------------------------------------- closed shell
+// The same functionals at rho_a = rho_b = r, gamma_aa = gamma_ab = gamma_bb = g (an RKS point), for
+// the tensor-core form.  At zeta = 0 the spin interpolation terms of VWN and PW92 vanish exactly and
+// the two LYP brackets coincide, so only the paramagnetic channels and one bracket are evaluated.
+// One cube root serves every term (rho^(1/3) = 2^(1/3) r^(1/3), r^(8/3) = r^2 (r^(1/3))^2,
+// rho^(-11/3) = rho^(-2/3) / rho^3), asinh(s) = log1p(s + s^2 / (1 + sqrt(1 + s^2))) reuses the
+// square root B88 needs anyway, exp(w) = expm1(w) + 1, and the constant factors are literals (their
+// values computed in double precision from the definitions beside them).  The results agree with
+// xc_eval(code, r, r, g, g, g) to rounding (~1e-15 relative).
+struct XcCs {
+  double f;   // energy density
+  double vr;  // dF/drho_a (= dF/drho_b)
+  double vg;  // dF/dgamma_aa + dF/dgamma_ab / 2, the coefficient of the RKS gradient term
+};
+
+constexpr double kCsCbrt2 = 1.2599210498948732;       // 2^(1/3)
+constexpr double kCsCx = 0.9305257363491;             // 3/4 (6/pi)^(1/3)
+constexpr double kCsRsK = 0.6203504908994001;         // (3/(4 pi))^(1/3)
+constexpr double kCsK0 = 36.46239897876477;           // 2^(11/3) 0.3 (3 pi^2)^(2/3)
+constexpr double kCsCbrt3Pi2 = 3.0936677262801355;    // (3 pi^2)^(1/3)
+constexpr double kCsCxu = -0.7385587663820223;        // -3/4 (3/pi)^(1/3)
+constexpr double kCsCt = 15.755920349483144;          // (16/pi) (3 pi^2)^(1/3)
+
+// Paramagnetic VWN channel with its derived constants: q = sqrt(4c - b^2), c1 = 2b/q,
+// c2 = b x0 / X(x0), c3 = 2(b + 2 x0)/q.
+struct VwnPara { double a, x0, b, c, q, c1, c2, c3; };
+constexpr VwnPara kVwn5Para{0.0310907, -0.10498, 3.72744, 12.9352,
+                            6.15199081975908, 1.2117833427280607, -0.031167608678943783, 1.1435257636284148};
+constexpr VwnPara kVwnRpaPara{0.0310907, -0.409286, 13.0720, 42.7198,
+                              0.0448998886415768, 582.2731590427809, -0.14253052416798392, 545.8110641572265};
+
+__host__ __device__ __forceinline__ XcCs xc_eval_cs(int code, double r_in, double g_in) {
+  XcCs o{0.0, 0.0, 0.0};
+  const double r = fmax(r_in, 0.0);
+  const double rho = r + r;
+  if (rho < kRhoFloor) return o;
+  const double g = fmax(g_in, 0.0);
+  const double c13 = cbrt(r);
+  const double rho13 = kCsCbrt2 * c13;
+  const bool spin_on = !(r < kRhoFloor);  // the per-spin floor of the exchange terms
+  if (spin_on && (code == 0 || code == 1 || code == 3 || code == 4)) {  // Slater
+    const double sc = (code == 3 || code == 4) ? 0.80 : 1.0;
+    o.f += sc * (-2.0 * kCsCx * r * c13);
+    o.vr += sc * (-(4.0 / 3.0) * kCsCx * c13);
+  }
+  if (spin_on && (code == 1 || code == 3 || code == 4)) {  // B88
+    const double sc = code == 1 ? 1.0 : 0.72;
+    const double beta = 0.0042;
+    const double r43 = r * c13;
+    const double s2 = g / (r43 * r43);
+    const double s = sqrt(s2);
+    const double q1 = sqrt(1.0 + s2);
+    const double ash = log1p(s + s2 / (1.0 + q1));
+    const double den = 1.0 + 6.0 * beta * s * ash;
+    const double gfun = -beta * s2 / den;
+    const double h = -beta * (2.0 + 6.0 * beta * s * ash - 6.0 * beta * s2 / q1) / (den * den);
+    o.f += sc * (2.0 * r43 * gfun);
+    o.vr += sc * ((4.0 / 3.0) * c13 * (gfun - s2 * h));
+    o.vg += sc * (0.5 * h / r43);
+  }
+  if (spin_on && (code == 2 || code == 5)) {  // PBE exchange (spin scaling: rho_u = rho, gamma_u = 4g)
+    const double sc = code == 2 ? 1.0 : 0.75;
+    const double r43 = rho * rho13;
+    const double exl = kCsCxu * r43;
+    const double kf = kCsCbrt3Pi2 * rho13;
+    const double den_s2 = 4.0 * kf * kf * rho * rho;
+    const double s2 = 4.0 * g / den_s2;
+    const double q = 1.0 + (kMu / kKappa) * s2;
+    const double fx = 1.0 + kKappa - kKappa / q;
+    const double dfx = kMu / (q * q);
+    o.f += sc * (exl * fx);
+    o.vr += sc * ((4.0 / 3.0) * kCsCxu * rho13 * fx + exl * dfx * (-(8.0 / 3.0) * s2 / rho));
+    o.vg += sc * (2.0 * (exl * dfx / den_s2));
+  }
+  if (code == 0 || code == 3 || code == 4) {  // VWN5 / VWN_RPA, paramagnetic channel
+    const double sc = code == 0 ? 1.0 : 0.19;
+    const VwnPara ch = code == 3 ? kVwnRpaPara : kVwn5Para;
+    const double x = sqrt(kCsRsK / rho13);
+    const double X = x * x + ch.b * x + ch.c;
+    const double at = atan(ch.q / (2.0 * x + ch.b));
+    const double dx0 = x - ch.x0;
+    const double ep = ch.a * (log(x * x / X) + ch.c1 * at - ch.c2 * (log(dx0 * dx0 / X) + ch.c3 * at));
+    const double dp = ch.a * (ch.c * dx0 - ch.b * x * ch.x0) / (dx0 * X);
+    o.f += sc * (rho * ep);
+    o.vr += sc * (ep - (1.0 / 3.0) * dp);
+  }
+  if (code == 1 || code == 3 || code == 4) {  // LYP
+    const double sc = code == 1 ? 1.0 : 0.81;
+    const double A = 0.04918, B = 0.132, C = 0.2533, D = 0.349;
+    const double rm13 = 1.0 / rho13;
+    const double den = 1.0 + D * rm13;
+    const double g0 = -4.0 * A / (rho * den);
+    const double dg0 = -g0 * (1.0 + (2.0 / 3.0) * D * rm13) / (rho * den);
+    const double t0 = g0 * r * r;
+    const double dt0 = dg0 * r * r + g0 * r;
+    if (C * rm13 > 500.0) {
+      o.f += sc * t0;
+      o.vr += sc * dt0;
+    } else {
+      const double rho2 = rho * rho;
+      const double omega = exp(-C * rm13) / den * (rm13 * rm13 / (rho2 * rho));
+      const double delta = C * rm13 + D * rm13 / den;
+      const double domega = omega * (delta - 11.0) / (3.0 * rho);
+      const double ddelta = -(1.0 / 3.0) * (rm13 / rho) * (C + D / (den * den));
+      const double r2 = r * r, r83 = r2 * c13 * c13;
+      const double stf = kCsK0 * r2 * (r83 + r83);
+      const double dstf = kCsK0 * ((11.0 / 3.0) * r83 * r + r * r83);
+      const double cg = r2 * (47.0 - 7.0 * delta) / 18.0 - (2.0 / 3.0) * rho2;
+      const double dcg = r * (47.0 - 7.0 * delta) / 18.0 + r2 * (-7.0 * ddelta) / 18.0 - (4.0 / 3.0) * rho;
+      const double c25 = 2.5 - delta / 18.0, c11 = (delta - 11.0) / 9.0;
+      const double qa = r2 * r / rho;
+      const double dqa = (2.0 * r2 * rho - r2 * r) / rho2;
+      const double dqb = (r2 * rho - r2 * r) / rho2;
+      const double ea = -r2 * c25 - c11 * qa + ((2.0 / 3.0) * rho2 - r2);
+      const double dea = -r * c25 + r2 * (ddelta / 18.0) - (ddelta / 9.0) * qa - c11 * dqa + (4.0 / 3.0) * rho;
+      const double deb =
+          -r * c25 + r2 * (ddelta / 18.0) - (ddelta / 9.0) * qa - c11 * dqb + (4.0 / 3.0) * rho - 2.0 * r;
+      const double aaa = cg + ea, aab = 2.0 * cg;
+      const double sb = stf + (aaa + aab + aaa) * g;
+      const double ds = dstf + (dcg + dea) * g + (2.0 * dcg) * g + (dcg + deb) * g;
+      const double ab = A * B;
+      o.f += sc * (t0 - ab * omega * sb);
+      o.vr += sc * (dt0 - ab * (domega * sb + omega * ds));
+      o.vg += sc * (-ab * omega * (aaa + 0.5 * aab));
+    }
+  }
+  if (code == 2 || code == 5) {  // PBE correlation on the paramagnetic PW92 channel
+    const double gt = 4.0 * g;
+    const double rs = kCsRsK / rho13;
+    const double drs = -rs / (3.0 * rho);
+    double ec, de0;
+    pw92(rs, Pw92Channel{0.0310907, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294}, ec, de0);
+    const double dec_drho = de0 * drs;
+    if (gt < 1e-36) {
+      o.f += rho * ec;
+      o.vr += ec + rho * dec_drho;
+    } else {
+      const double b0 = kBetaPbe / kGammaPbe;
+      const double den_t2 = kCsCt * (rho * rho * rho13);
+      const double t2 = gt / den_t2;
+      const double gp3 = kGammaPbe;
+      const double w = -ec / gp3;
+      double af = 0.0, daw = 0.0;
+      if (!(w > 100.0)) {
+        const double em1 = expm1(w);
+        af = b0 / em1;
+        daw = -af * (em1 + 1.0) / em1;
+      }
+      const double u = af * t2;
+      const double dpol = 1.0 + u + u * u;
+      const double za = 1.0 + b0 * t2 * ((1.0 + u) / dpol);
+      const double lnz = log(za);
+      const double h = gp3 * lnz;
+      const double dh_dt2 = gp3 * (b0 * (1.0 + 2.0 * u) / (dpol * dpol)) / za;
+      const double dh_dw = gp3 * ((-b0 * t2 * t2 * u * (2.0 + u) / (dpol * dpol)) * daw) / za;
+      const double dh_drho = dh_dt2 * (-(7.0 / 3.0) * t2 / rho) + dh_dw * (-dec_drho / gp3);
+      const double te = ec + h;
+      o.f += rho * te;
+      o.vr += te + rho * (dec_drho + dh_drho);
+      o.vg += 2.0 * (rho * dh_dt2 / den_t2);
+    }
+  }
   return o;
 }
 
