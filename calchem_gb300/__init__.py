@@ -9,12 +9,12 @@ Rust call surface (``RksVxcEngine``, ``UksVxcEngine``, ``MolecularGrid``,
 from .basis import BasisSet
 from .grid import GridLevel, MolecularGrid
 from .molecule import ANGSTROM_TO_BOHR, Atom, Molecule
-from .vxc import (FP64, MIXED, GpuVxcGrid, RksVxcEngine, UksVxcEngine, evaluate_vxc_rks, evaluate_vxc_uks,
-                  is_cuda_available)
+from .vxc import (FP64, MIXED, GpuVxcGrid, RksVxcEngine, UksVxcEngine, VxcGroup, evaluate_vxc_rks,
+                  evaluate_vxc_uks, is_cuda_available)
 from .xc import XcFunctional
 
 __all__ = [
     "ANGSTROM_TO_BOHR", "Atom", "Molecule", "BasisSet", "GridLevel", "MolecularGrid", "XcFunctional",
-    "RksVxcEngine", "UksVxcEngine", "GpuVxcGrid", "evaluate_vxc_rks", "evaluate_vxc_uks", "is_cuda_available",
+    "RksVxcEngine", "UksVxcEngine", "VxcGroup", "GpuVxcGrid", "evaluate_vxc_rks", "evaluate_vxc_uks", "is_cuda_available",
     "FP64", "MIXED",
 ]

@@ -50,6 +50,11 @@ SIGNATURES = {
     "calchem_xc_last_kernel_ms": (_I, [_U64, _P]),
     "calchem_xc_evaluate_rks_static": (_I, [_P, _I, _P, _I, _P, _I, _P, _P, _I, _P, _P, _I, _I, _I, _I, _I, _P, _P,
                                            _P, _P]),
+    "calchem_xc_group_create": (_I, [_P, _I, _U64, ctypes.c_size_t]),
+    "calchem_xc_group_layout": (_I, [_U64, _P, _P, _P]),
+    "calchem_xc_graph_capture": (_I, [_U64, _I, _I, _I, _P, _P, _P, _P, _P]),
+    "calchem_xc_graph_launch": (_I, [_U64, _P]),
+    "calchem_xc_last_status": (_I, [_U64]),
     "calchem_xc_version": (ctypes.c_char_p, []),
 }
 

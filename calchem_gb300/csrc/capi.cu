@@ -17,18 +17,8 @@
 #include "common.cuh"
 #include "grid_build.h"
 #include "host_prep.h"
+#include "launch.h"
 
-namespace cxc {
-cudaError_t launch_fp64(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st);
-cudaError_t launch_reduce(const double* part, int n_batches, double* out, int n_out, cudaStream_t st);
-cudaError_t launch_mirror(double* V, int n, int from_upper, cudaStream_t st);
-size_t fp64_smem_bytes();
-int mixed_supported(int mode);
-size_t mixed_slab_doubles(int max_m);
-int mixed_ctas_per_sm();
-cudaError_t launch_mixed(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st);
-cudaError_t launch_mixed_prepare(const double* P, int n, void* out, int* fexp, cudaStream_t st);
-}  // namespace cxc
 
 using namespace cxc;
 
@@ -38,6 +28,19 @@ constexpr int kPlanes = 5;
 
 struct Entry {
   int n_pts = 0, n_ao = 0, n_shells = 0, n_batches = 0, max_m = 0;
+  int n_prims = 0, n_comps = 0;
+  size_t n_cand = 0, n_bao = 0;
+  // molecules: one for an uploaded grid; several for a group (calchem_xc_group_create), whose
+  // densities and Vxc are packed blocks (n_ao then counts the rows of all blocks)
+  int n_mols = 1, max_n = 0;
+  long long nn_total = 0;
+  std::vector<int> h_mol_n, h_mol_ao_off, h_mol_boff;
+  std::vector<long long> h_mol_off;
+  int* d_mol_n = nullptr;
+  long long* d_mol_off = nullptr;
+  int* d_mol_ao_off = nullptr;
+  int* d_mol_boff = nullptr;
+  bool ws = false;  // evaluation workspace allocated (ensure_ws)
   size_t bytes = 0;
   bool has_w = false;
   double sum_m2n = 0, sum_m2 = 0;
@@ -73,13 +76,15 @@ struct Entry {
   int last_launches = 0;
   bool profiling = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaGraphExec_t graph = nullptr;  // captured evaluation (calchem_xc_graph_capture_*)
 
   void free_all() {
     void* ptrs[] = {d_shells, d_prims, d_comps, d_prim_f, d_comp_f, d_shell_cf, d_pts,  d_batches, d_cand,  d_cand_loc, d_bao,   d_order,
                     d_P,      d_Pb,    d_V,     d_Vb,   d_rg,      d_red,   d_res,      d_counter, d_slab,
-                    d_mixed_ws, d_mixed_slab};
+                    d_mixed_ws, d_mixed_slab, d_mol_n, d_mol_off, d_mol_ao_off, d_mol_boff};
     for (void* p : ptrs)
       if (p) cudaFree(p);
+    if (graph) cudaGraphExecDestroy(graph);
     if (h_stage) cudaFreeHost(h_stage);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -201,9 +206,54 @@ int build_host_plan(const AoShellGpu* sh, int n_shells, int n_prims, const AoCom
   return 0;
 }
 
+// Bytes of the evaluation workspace of an entry (densities, Vxc, split densities, slabs, partials).
+size_t workspace_bytes(const Entry& e) {
+  const size_t nn = (size_t)e.nn_total;
+  size_t t = nn * sizeof(double) * 4;                                           // P, Pb, V, Vb
+  t += nn * sizeof(uint2) * 2 + (size_t)e.n_ao * 2 * sizeof(int);              // split densities
+  if (e.n_mols == 1) t += (size_t)e.n_pts * 4 * sizeof(double);                // rho / wv staging
+  t += (size_t)e.n_batches * 3 * sizeof(double) + (3 * (size_t)e.n_mols + 8) * sizeof(double) + 64;
+  t += e.slab_stride * e.n_ctas * sizeof(double);
+  t += e.mixed_slab_stride * e.mixed_ctas * sizeof(double);
+  return t;
+}
+
+// Allocates the evaluation workspace on first use.  Uploads through calchem_xc_upload_points and
+// groups defer it, so that grids uploaded only to be grouped hold no workspace.
+int ensure_ws(Entry& e) {
+  if (e.ws) return 0;
+  const size_t nn = (size_t)e.nn_total;
+  bool ok = dalloc(&e.d_P, nn) && dalloc(&e.d_Pb, nn) && dalloc(&e.d_V, nn) && dalloc(&e.d_Vb, nn) &&
+            (e.n_mols != 1 || dalloc(&e.d_rg, (size_t)e.n_pts * 4)) && dalloc(&e.d_red, (size_t)e.n_batches * 3) &&
+            dalloc(&e.d_res, 3 * (size_t)e.n_mols + 8) && dalloc(&e.d_counter, 4) &&
+            dalloc(&e.d_slab, e.slab_stride * e.n_ctas) &&
+            cudaMalloc(&e.d_mixed_ws, nn * sizeof(uint2) * 2 + (size_t)e.n_ao * 2 * sizeof(int)) == cudaSuccess &&
+            dalloc(&e.d_mixed_slab, e.mixed_slab_stride * e.mixed_ctas) &&
+            cudaMallocHost((void**)&e.h_stage, (2 * nn + 3 * (size_t)e.n_mols + 8) * sizeof(double)) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    void* ptrs[] = {e.d_P, e.d_Pb, e.d_V, e.d_Vb, e.d_rg, e.d_red, e.d_res, e.d_counter, e.d_slab, e.d_mixed_ws,
+                    e.d_mixed_slab};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    if (e.h_stage) cudaFreeHost(e.h_stage);
+    if (e.stream) cudaStreamDestroy(e.stream);
+    e.d_P = e.d_Pb = e.d_V = e.d_Vb = e.d_rg = e.d_red = e.d_res = e.d_slab = e.d_mixed_slab = nullptr;
+    e.d_counter = nullptr;
+    e.d_mixed_ws = nullptr;
+    e.h_stage = nullptr;
+    e.stream = nullptr;
+    return -4;
+  }
+  e.ws = true;
+  return 0;
+}
+
 int upload_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
                 const AoCompGpu* h_comps, int n_comps, const GridPtGpu* h_pts, int n_pts, const int* h_off, int n_off,
-                const int* h_cs, int n_cs, int n_ao, uint64_t grid_id, size_t mem_limit, const double* h_w) {
+                const int* h_cs, int n_cs, int n_ao, uint64_t grid_id, size_t mem_limit, const double* h_w,
+                bool eager_ws) {
   if (!h_shells || !h_prims || !h_comps || !h_pts || !h_off || !h_cs || n_shells <= 0 || n_prims <= 0 ||
       n_comps <= 0 || n_pts <= 0 || n_off <= 1 || n_cs <= 0 || n_ao <= 0 || grid_id == 0)
     return -1;
@@ -249,18 +299,22 @@ int upload_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_pri
   e->slab_stride = slab_stride;
   e->mixed_ctas = mixed_ctas;
   e->mixed_slab_stride = mixed_stride;
+  e->n_prims = n_prims;
+  e->n_comps = n_comps;
+  e->n_cand = hp.cand.size();
+  e->n_bao = hp.bao.size();
+  e->n_mols = 1;
+  e->max_n = n_ao;
+  e->nn_total = (long long)nn;
+  e->h_mol_n = {n_ao};
+  e->h_mol_off = {0};
+  e->h_mol_ao_off = {0, n_ao};
+  e->h_mol_boff = {0, nb};
   bool ok = dalloc(&e->d_shells, n_shells) && dalloc(&e->d_prims, n_prims) && dalloc(&e->d_comps, n_comps) &&
             dalloc(&e->d_prim_f, n_prims) && dalloc(&e->d_comp_f, n_comps) && dalloc(&e->d_shell_cf, 3 * (size_t)n_shells) &&
             dalloc(&e->d_pts, (size_t)n_pts * 4) && dalloc(&e->d_batches, nb) && dalloc(&e->d_cand, hp.cand.size()) &&
             dalloc(&e->d_cand_loc, hp.cand_loc.size()) && dalloc(&e->d_bao, hp.bao.size()) &&
-            dalloc(&e->d_order, hp.order.size()) && dalloc(&e->d_P, nn) && dalloc(&e->d_Pb, nn) &&
-            dalloc(&e->d_V, nn) && dalloc(&e->d_Vb, nn) && dalloc(&e->d_rg, (size_t)n_pts * 4) &&
-            dalloc(&e->d_red, (size_t)nb * 3) && dalloc(&e->d_res, 8) && dalloc(&e->d_counter, 4) &&
-            dalloc(&e->d_slab, slab_stride * n_ctas) &&
-            cudaMalloc(&e->d_mixed_ws, nn * sizeof(uint2) * 2 + (size_t)n_ao * 2 * sizeof(int)) == cudaSuccess &&
-            dalloc(&e->d_mixed_slab, mixed_stride * mixed_ctas) &&
-            cudaMallocHost((void**)&e->h_stage, (2 * nn + 8) * sizeof(double)) == cudaSuccess &&
-            cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) == cudaSuccess;
+            dalloc(&e->d_order, hp.order.size()) && (!eager_ws || ensure_ws(*e) == 0);
   if (!ok) {
     cudaGetLastError();
     e->free_all();
@@ -317,7 +371,7 @@ int upload_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_pri
 }
 
 DevGrid dev_grid(const Entry& e) {
-  DevGrid G;
+  DevGrid G{};
   G.n_pts = e.n_pts;
   G.n_ao = e.n_ao;
   G.n_shells = e.n_shells;
@@ -337,13 +391,18 @@ DevGrid dev_grid(const Entry& e) {
   G.prim_f = e.d_prim_f;
   G.comp_f = e.d_comp_f;
   G.shell_cf = e.d_shell_cf;
+  G.mol_n = e.d_mol_n;  // nullptr unless the entry is a group
+  G.mol_off = e.d_mol_off;
+  G.mol_ao_off = e.d_mol_ao_off;
+  G.nn_total = e.nn_total;
+  G.n_total = e.n_ao;
   return G;
 }
 
 // Enqueues one evaluation.  Pa/Pb/Va/Vb are device pointers; result gets (exc, n_a[, n_b]).
 int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, const double* Pb, double* Va,
                  double* Vb, const double* wv, double* rho_out, double* result, cudaStream_t st) {
-  const size_t nn = (size_t)e.n_ao * e.n_ao;
+  const size_t nn = (size_t)e.nn_total;
   int launches = 0;
   if (mode != kModeRho) {
     if (cudaMemsetAsync(Va, 0, nn * sizeof(double), st) != cudaSuccess) return -5;
@@ -369,10 +428,14 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
     // packed fixed-point densities: [alpha n^2][beta n^2] uint2, then row exponents [alpha n][beta n]
     uint2* pk = reinterpret_cast<uint2*>(e.d_mixed_ws);
     int* fx = reinterpret_cast<int*>(pk + 2 * nn);
-    if (launch_mixed_prepare(Pa, e.n_ao, pk, fx, st) != cudaSuccess) return -5;
+    if (launch_mixed_prepare(Pa, e.n_ao, e.d_mol_n, e.d_mol_off, e.d_mol_ao_off, e.n_mols, pk, fx, st) !=
+        cudaSuccess)
+      return -5;
     ++launches;
     if (mode == kModeUks) {
-      if (launch_mixed_prepare(Pb, e.n_ao, pk + nn, fx + e.n_ao, st) != cudaSuccess) return -5;
+      if (launch_mixed_prepare(Pb, e.n_ao, e.d_mol_n, e.d_mol_off, e.d_mol_ao_off, e.n_mols, pk + nn, fx + e.n_ao,
+                               st) != cudaSuccess)
+        return -5;
       ++launches;
     }
     A.slab = e.d_mixed_slab;
@@ -391,12 +454,14 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
   if (err != cudaSuccess) return -5;
   ++launches;
   if (mode == kModeRks || mode == kModeUks) {
-    if (launch_reduce(e.d_red, e.n_batches, result, mode == kModeRks ? 2 : 3, st) != cudaSuccess) return -5;
+    if (launch_reduce(e.d_red, e.n_batches, e.d_mol_boff, e.n_mols, result, mode == kModeRks ? 2 : 3, st) !=
+        cudaSuccess)
+      return -5;
     const int from_upper = precision == CALCHEM_XC_MIXED ? 1 : 0;
-    if (launch_mirror(Va, e.n_ao, from_upper, st) != cudaSuccess) return -5;
+    if (launch_mirror(Va, e.max_n, e.d_mol_n, e.d_mol_off, e.n_mols, from_upper, st) != cudaSuccess) return -5;
     launches += 2;
     if (mode == kModeUks) {
-      if (launch_mirror(Vb, e.n_ao, from_upper, st) != cudaSuccess) return -5;
+      if (launch_mirror(Vb, e.max_n, e.d_mol_n, e.d_mol_off, e.n_mols, from_upper, st) != cudaSuccess) return -5;
       ++launches;
     }
   }
@@ -432,7 +497,7 @@ int calchem_cuda_vxc_upload_grid(const AoShellGpu* h_shells, int n_shells, const
                                  int n_cand_shells, int n_ao, uint64_t grid_id, size_t memory_limit_bytes) {
   std::lock_guard<std::mutex> lk(g_mu);
   return upload_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, h_pts, n_pts, h_cand_offsets,
-                     n_cand_offsets, h_cand_shells, n_cand_shells, n_ao, grid_id, memory_limit_bytes, nullptr);
+                     n_cand_offsets, h_cand_shells, n_cand_shells, n_ao, grid_id, memory_limit_bytes, nullptr, true);
 }
 
 int calchem_cuda_vxc_eval_rho(uint64_t grid_id, const double* h_p_mat, double* h_rho_grad_out, int n_pts, int n_ao) {
@@ -440,7 +505,8 @@ int calchem_cuda_vxc_eval_rho(uint64_t grid_id, const double* h_p_mat, double* h
   if (!h_p_mat || !h_rho_grad_out || n_pts <= 0 || n_ao <= 0 || grid_id == 0) return -1;
   if (!device_ok()) return -3;
   Entry* e = find(grid_id);
-  if (!e || e->n_pts != n_pts || e->n_ao != n_ao) return -2;
+  if (!e || e->n_mols != 1 || e->n_pts != n_pts || e->n_ao != n_ao) return -2;
+  if (int rc0 = ensure_ws(*e)) return rc0;
   const size_t nn = (size_t)n_ao * n_ao;
   std::memcpy(e->h_stage, h_p_mat, nn * sizeof(double));
   if (cudaMemcpyAsync(e->d_P, e->h_stage, nn * sizeof(double), cudaMemcpyHostToDevice, e->stream) != cudaSuccess)
@@ -460,7 +526,8 @@ int calchem_cuda_vxc_accum(uint64_t grid_id, const double* h_wv_in, double* h_vx
   if (!h_wv_in || !h_vxc_out || n_pts <= 0 || n_ao <= 0 || grid_id == 0) return -1;
   if (!device_ok()) return -3;
   Entry* e = find(grid_id);
-  if (!e || e->n_pts != n_pts || e->n_ao != n_ao) return -2;
+  if (!e || e->n_mols != 1 || e->n_pts != n_pts || e->n_ao != n_ao) return -2;
+  if (int rc0 = ensure_ws(*e)) return rc0;
   const size_t nn = (size_t)n_ao * n_ao;
   if (cudaMemcpyAsync(e->d_rg, h_wv_in, (size_t)n_pts * 4 * sizeof(double), cudaMemcpyHostToDevice, e->stream) !=
       cudaSuccess)
@@ -644,14 +711,14 @@ int calchem_xc_upload_points(const AoShellGpu* h_shells, int n_shells, const AoP
   if (plan.pts.empty()) return -1;
   return upload_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, plan.pts.data(), (int)plan.pts.size(),
                      plan.cand_offsets.data(), (int)plan.cand_offsets.size(), plan.cand_shells.data(),
-                     (int)plan.cand_shells.size(), n_ao, grid_id, memory_limit_bytes, plan.weights.data());
+                     (int)plan.cand_shells.size(), n_ao, grid_id, memory_limit_bytes, plan.weights.data(), false);
 }
 
 int calchem_xc_set_weights(uint64_t grid_id, const double* h_weights, int n_pts) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!h_weights || n_pts <= 0) return -1;
   Entry* e = find(grid_id);
-  if (!e || e->n_pts != n_pts) return -2;
+  if (!e || e->n_mols != 1 || e->n_pts != n_pts) return -2;
   if (cudaMemcpy(e->d_pts + 3 * (size_t)n_pts, h_weights, n_pts * sizeof(double), cudaMemcpyHostToDevice) !=
       cudaSuccess)
     return -5;
@@ -679,24 +746,29 @@ int calchem_xc_evaluate_rks(uint64_t grid_id, int xc_code, int precision, const 
   Entry* e = find(grid_id);
   if (!e) return -2;
   if (!e->has_w) return -1;
-  const size_t nn = (size_t)e->n_ao * e->n_ao;
+  if (int rc0 = ensure_ws(*e)) return rc0;
+  const size_t nn = (size_t)e->nn_total;
+  const int M = e->n_mols;
   std::memcpy(e->h_stage, h_d_total, nn * sizeof(double));
   if (cudaMemcpyAsync(e->d_P, e->h_stage, nn * sizeof(double), cudaMemcpyHostToDevice, e->stream) != cudaSuccess)
     return -5;
   int rc = enqueue_eval(*e, kModeRks, xc_code, precision, e->d_P, nullptr, e->d_V, nullptr, nullptr, nullptr,
                         e->d_res, e->stream);
   if (rc) return rc;
-  int* h_status = reinterpret_cast<int*>(e->h_stage + 2 * nn + 4);
+  double* h_res = e->h_stage + 2 * nn;
+  int* h_status = reinterpret_cast<int*>(h_res + 3 * (size_t)M + 1);
   if (cudaMemcpyAsync(e->h_stage, e->d_V, nn * sizeof(double), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
-      cudaMemcpyAsync(e->h_stage + 2 * nn, e->d_res, 2 * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
+      cudaMemcpyAsync(h_res, e->d_res, 2 * (size_t)M * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
           cudaSuccess ||
       cudaMemcpyAsync(h_status, e->d_counter + 2, sizeof(int), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
       cudaStreamSynchronize(e->stream) != cudaSuccess)
     return -5;
   if (*h_status != 0) return -7;
   std::memcpy(h_v_out, e->h_stage, nn * sizeof(double));
-  *exc_out = e->h_stage[2 * nn];
-  *nelec_out = e->h_stage[2 * nn + 1];
+  for (int i = 0; i < M; ++i) {
+    exc_out[i] = h_res[2 * i];
+    nelec_out[i] = h_res[2 * i + 1];
+  }
   return 0;
 }
 
@@ -709,7 +781,9 @@ int calchem_xc_evaluate_uks(uint64_t grid_id, int xc_code, int precision, const 
   Entry* e = find(grid_id);
   if (!e) return -2;
   if (!e->has_w) return -1;
-  const size_t nn = (size_t)e->n_ao * e->n_ao;
+  if (int rc0 = ensure_ws(*e)) return rc0;
+  const size_t nn = (size_t)e->nn_total;
+  const int M = e->n_mols;
   std::memcpy(e->h_stage, h_pa, nn * sizeof(double));
   std::memcpy(e->h_stage + nn, h_pb, nn * sizeof(double));
   if (cudaMemcpyAsync(e->d_P, e->h_stage, nn * sizeof(double), cudaMemcpyHostToDevice, e->stream) != cudaSuccess ||
@@ -719,21 +793,24 @@ int calchem_xc_evaluate_uks(uint64_t grid_id, int xc_code, int precision, const 
   int rc = enqueue_eval(*e, kModeUks, xc_code, precision, e->d_P, e->d_Pb, e->d_V, e->d_Vb, nullptr, nullptr,
                         e->d_res, e->stream);
   if (rc) return rc;
+  double* h_res = e->h_stage + 2 * nn;
+  int* h_status = reinterpret_cast<int*>(h_res + 3 * (size_t)M + 1);
   if (cudaMemcpyAsync(e->h_stage, e->d_V, nn * sizeof(double), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
       cudaMemcpyAsync(e->h_stage + nn, e->d_Vb, nn * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
           cudaSuccess ||
-      cudaMemcpyAsync(e->h_stage + 2 * nn, e->d_res, 3 * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
+      cudaMemcpyAsync(h_res, e->d_res, 3 * (size_t)M * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
           cudaSuccess ||
-      cudaMemcpyAsync(reinterpret_cast<int*>(e->h_stage + 2 * nn + 4), e->d_counter + 2, sizeof(int),
-                      cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
+      cudaMemcpyAsync(h_status, e->d_counter + 2, sizeof(int), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
       cudaStreamSynchronize(e->stream) != cudaSuccess)
     return -5;
-  if (*reinterpret_cast<int*>(e->h_stage + 2 * nn + 4) != 0) return -7;
+  if (*h_status != 0) return -7;
   std::memcpy(h_va_out, e->h_stage, nn * sizeof(double));
   std::memcpy(h_vb_out, e->h_stage + nn, nn * sizeof(double));
-  *exc_out = e->h_stage[2 * nn];
-  nelec_out[0] = e->h_stage[2 * nn + 1];
-  nelec_out[1] = e->h_stage[2 * nn + 2];
+  for (int i = 0; i < M; ++i) {
+    exc_out[i] = h_res[3 * i];
+    nelec_out[2 * i] = h_res[3 * i + 1];
+    nelec_out[2 * i + 1] = h_res[3 * i + 2];
+  }
   return 0;
 }
 
@@ -744,6 +821,7 @@ int calchem_xc_evaluate_rks_device(uint64_t grid_id, int xc_code, int precision,
   Entry* e = find(grid_id);
   if (!e) return -2;
   if (!e->has_w) return -1;
+  if (int rc0 = ensure_ws(*e)) return rc0;
   return enqueue_eval(*e, kModeRks, xc_code, precision, d_total, nullptr, d_v, nullptr, nullptr, nullptr, d_result,
                       (cudaStream_t)stream);
 }
@@ -756,8 +834,238 @@ int calchem_xc_evaluate_uks_device(uint64_t grid_id, int xc_code, int precision,
   Entry* e = find(grid_id);
   if (!e) return -2;
   if (!e->has_w) return -1;
+  if (int rc0 = ensure_ws(*e)) return rc0;
   return enqueue_eval(*e, kModeUks, xc_code, precision, d_pa, d_pb, d_va, d_vb, nullptr, nullptr, d_result,
                       (cudaStream_t)stream);
+}
+
+int calchem_xc_group_create(const uint64_t* member_ids, int n_members, uint64_t group_id, size_t memory_limit_bytes) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!member_ids || n_members <= 0 || group_id == 0) return -1;
+  if (!device_ok()) return -3;
+  if (g_grids.count(group_id)) return -2;
+  std::vector<Entry*> mem(n_members);
+  for (int i = 0; i < n_members; ++i) {
+    mem[i] = find(member_ids[i]);
+    if (!mem[i] || mem[i]->n_mols != 1) return -2;
+    if (!mem[i]->has_w) return -1;
+    for (int j = 0; j < i; ++j)
+      if (member_ids[j] == member_ids[i]) return -1;
+  }
+  // offsets of every member's arrays inside the group's
+  long long n_pts = 0, n_shells = 0, n_prims = 0, n_comps = 0, n_cand = 0, n_bao = 0, n_b = 0, n_rows = 0, nn = 0;
+  int max_m = 0, max_n = 0;
+  double s_m2n = 0, s_m2 = 0;
+  std::vector<long long> o_pts(n_members), o_sh(n_members), o_pr(n_members), o_co(n_members), o_ca(n_members),
+      o_bao(n_members), o_b(n_members);
+  Entry* g = new Entry;
+  for (int i = 0; i < n_members; ++i) {
+    const Entry& m = *mem[i];
+    o_pts[i] = n_pts; o_sh[i] = n_shells; o_pr[i] = n_prims; o_co[i] = n_comps; o_ca[i] = n_cand;
+    o_bao[i] = n_bao; o_b[i] = n_b;
+    g->h_mol_n.push_back(m.n_ao);
+    g->h_mol_off.push_back(nn);
+    g->h_mol_ao_off.push_back((int)n_rows);
+    g->h_mol_boff.push_back((int)n_b);
+    n_pts += m.n_pts; n_shells += m.n_shells; n_prims += m.n_prims; n_comps += m.n_comps;
+    n_cand += (long long)m.n_cand; n_bao += (long long)m.n_bao; n_b += m.n_batches; n_rows += m.n_ao;
+    nn += (long long)m.n_ao * m.n_ao;
+    max_m = std::max(max_m, m.max_m);
+    max_n = std::max(max_n, m.n_ao);
+    s_m2n += m.sum_m2n;
+    s_m2 += m.sum_m2;
+  }
+  g->h_mol_ao_off.push_back((int)n_rows);
+  g->h_mol_boff.push_back((int)n_b);
+  if (n_pts > INT32_MAX || n_cand > INT32_MAX || n_bao > INT32_MAX || n_rows > INT32_MAX || n_b > INT32_MAX ||
+      n_shells > INT32_MAX) {
+    delete g;
+    return -2;
+  }
+  g->n_pts = (int)n_pts;
+  g->n_ao = (int)n_rows;
+  g->n_shells = (int)n_shells;
+  g->n_prims = (int)n_prims;
+  g->n_comps = (int)n_comps;
+  g->n_batches = (int)n_b;
+  g->n_cand = (size_t)n_cand;
+  g->n_bao = (size_t)n_bao;
+  g->max_m = max_m;
+  g->max_n = max_n;
+  g->n_mols = n_members;
+  g->nn_total = nn;
+  g->sum_m2n = s_m2n;
+  g->sum_m2 = s_m2;
+  g->has_w = true;
+  const int m_pad = (max_m + 63) / 64 * 64;
+  g->n_ctas = std::max(1, std::min(g->n_batches, g_sm_count));
+  g->slab_stride = (size_t)kPlanes * m_pad * kBlockPts;
+  g->mixed_ctas = std::max(1, std::min(g->n_batches, g_sm_count * mixed_ctas_per_sm()));
+  g->mixed_slab_stride = mixed_slab_doubles(max_m);
+  size_t total = (size_t)n_shells * sizeof(AoShellGpu) + (size_t)n_prims * (sizeof(AoPrimGpu) + sizeof(float4)) +
+                 (size_t)n_comps * (sizeof(AoCompGpu) + sizeof(float2)) + (size_t)n_shells * 3 * sizeof(float2) +
+                 (size_t)n_pts * 4 * sizeof(double) + (size_t)n_b * (sizeof(BatchDesc) + sizeof(int)) +
+                 (size_t)n_cand * 2 * sizeof(int) + (size_t)n_bao * sizeof(int) + (size_t)n_members * 32;
+  total += workspace_bytes(*g);
+  g->bytes = total;
+  if (total > memory_limit_bytes) {
+    delete g;
+    return -3;
+  }
+  auto fail = [&](int code) {
+    cudaGetLastError();
+    g->free_all();
+    delete g;
+    return code;
+  };
+  if (!(dalloc(&g->d_shells, n_shells) && dalloc(&g->d_prims, n_prims) && dalloc(&g->d_comps, n_comps) &&
+        dalloc(&g->d_prim_f, n_prims) && dalloc(&g->d_comp_f, n_comps) && dalloc(&g->d_shell_cf, 3 * (size_t)n_shells) &&
+        dalloc(&g->d_pts, (size_t)n_pts * 4) && dalloc(&g->d_batches, n_b) && dalloc(&g->d_cand, n_cand) &&
+        dalloc(&g->d_cand_loc, n_cand) && dalloc(&g->d_bao, n_bao) && dalloc(&g->d_order, n_b) &&
+        dalloc(&g->d_mol_n, n_members) && dalloc(&g->d_mol_off, n_members) &&
+        dalloc(&g->d_mol_ao_off, n_members + 1) && dalloc(&g->d_mol_boff, n_members + 1)))
+    return fail(-4);
+  // device-to-device copies of the arrays that need no renumbering; host renumbering of the rest
+  std::vector<AoShellGpu> shells((size_t)n_shells);
+  std::vector<BatchDesc> batches((size_t)n_b);
+  std::vector<int> cand((size_t)n_cand);
+  bool ok = true;
+  for (int i = 0; i < n_members && ok; ++i) {
+    const Entry& m = *mem[i];
+    const auto d2d = cudaMemcpyDeviceToDevice;
+    for (int k = 0; k < 4 && ok; ++k)
+      ok = cudaMemcpy(g->d_pts + (size_t)k * n_pts + o_pts[i], m.d_pts + (size_t)k * m.n_pts,
+                      (size_t)m.n_pts * sizeof(double), d2d) == cudaSuccess;
+    ok = ok &&
+         cudaMemcpy(g->d_prims + o_pr[i], m.d_prims, (size_t)m.n_prims * sizeof(AoPrimGpu), d2d) == cudaSuccess &&
+         cudaMemcpy(g->d_prim_f + o_pr[i], m.d_prim_f, (size_t)m.n_prims * sizeof(float4), d2d) == cudaSuccess &&
+         cudaMemcpy(g->d_comps + o_co[i], m.d_comps, (size_t)m.n_comps * sizeof(AoCompGpu), d2d) == cudaSuccess &&
+         cudaMemcpy(g->d_comp_f + o_co[i], m.d_comp_f, (size_t)m.n_comps * sizeof(float2), d2d) == cudaSuccess &&
+         cudaMemcpy(g->d_shell_cf + 3 * o_sh[i], m.d_shell_cf, 3 * (size_t)m.n_shells * sizeof(float2), d2d) ==
+             cudaSuccess &&
+         cudaMemcpy(g->d_cand_loc + o_ca[i], m.d_cand_loc, m.n_cand * sizeof(int), d2d) == cudaSuccess &&
+         cudaMemcpy(g->d_bao + o_bao[i], m.d_bao, m.n_bao * sizeof(int), d2d) == cudaSuccess &&
+         cudaMemcpy(shells.data() + o_sh[i], m.d_shells, (size_t)m.n_shells * sizeof(AoShellGpu),
+                    cudaMemcpyDeviceToHost) == cudaSuccess &&
+         cudaMemcpy(batches.data() + o_b[i], m.d_batches, (size_t)m.n_batches * sizeof(BatchDesc),
+                    cudaMemcpyDeviceToHost) == cudaSuccess &&
+         cudaMemcpy(cand.data() + o_ca[i], m.d_cand, m.n_cand * sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+    if (!ok) break;
+    for (int k = 0; k < m.n_shells; ++k) {
+      AoShellGpu& sh = shells[(size_t)o_sh[i] + k];
+      sh.prim_start += (int)o_pr[i];
+      sh.comp_start += (int)o_co[i];
+    }
+    for (size_t k = 0; k < m.n_cand; ++k) cand[(size_t)o_ca[i] + k] += (int)o_sh[i];
+    for (int k = 0; k < m.n_batches; ++k) {
+      BatchDesc& d = batches[(size_t)o_b[i] + k];
+      d.pt_start += (int)o_pts[i];
+      d.cand_start += (int)o_ca[i];
+      d.ao_start += (int)o_bao[i];
+      d.mol = i;
+    }
+  }
+  if (!ok) return fail(-5);
+  // one work queue over all molecules, most expensive batches first
+  std::vector<int> order((size_t)n_b);
+  for (long long i = 0; i < n_b; ++i) order[(size_t)i] = (int)i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    const double cx = (double)batches[x].m * batches[x].m * batches[x].n_pts;
+    const double cy = (double)batches[y].m * batches[y].m * batches[y].n_pts;
+    return cx > cy;
+  });
+  ok = cudaMemcpy(g->d_shells, shells.data(), shells.size() * sizeof(AoShellGpu), cudaMemcpyHostToDevice) ==
+           cudaSuccess &&
+       cudaMemcpy(g->d_batches, batches.data(), batches.size() * sizeof(BatchDesc), cudaMemcpyHostToDevice) ==
+           cudaSuccess &&
+       cudaMemcpy(g->d_cand, cand.data(), cand.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(g->d_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(g->d_mol_n, g->h_mol_n.data(), n_members * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(g->d_mol_off, g->h_mol_off.data(), n_members * sizeof(long long), cudaMemcpyHostToDevice) ==
+           cudaSuccess &&
+       cudaMemcpy(g->d_mol_ao_off, g->h_mol_ao_off.data(), (n_members + 1) * sizeof(int), cudaMemcpyHostToDevice) ==
+           cudaSuccess &&
+       cudaMemcpy(g->d_mol_boff, g->h_mol_boff.data(), (n_members + 1) * sizeof(int), cudaMemcpyHostToDevice) ==
+           cudaSuccess;
+  if (!ok) return fail(-5);
+  g_grids[group_id] = g;
+  return 0;
+}
+
+int calchem_xc_group_layout(uint64_t grid_id, int* n_mols_out, int* mol_n_out, long long* mol_off_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (!n_mols_out) return -1;
+  *n_mols_out = e->n_mols;
+  for (int i = 0; i < e->n_mols; ++i) {
+    if (mol_n_out) mol_n_out[i] = e->h_mol_n[i];
+    if (mol_off_out) mol_off_out[i] = e->h_mol_off[i];
+  }
+  return 0;
+}
+
+int calchem_xc_graph_capture(uint64_t grid_id, int mode, int xc_code, int precision, const double* d_pa,
+                             const double* d_pb, double* d_result, double* d_va, double* d_vb) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (mode != 0 && mode != 1) return -1;
+  const int kmode = mode == 0 ? kModeRks : kModeUks;
+  if (!d_pa || !d_result || !d_va || (kmode == kModeUks && (!d_pb || !d_vb)) || !valid_xc(xc_code) ||
+      !valid_prec(precision, kmode))
+    return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (!e->has_w) return -1;
+  if (int rc0 = ensure_ws(*e)) return rc0;
+  // kernel attributes are set outside the capture
+  if (fp64_set_attributes() != cudaSuccess || mixed_set_attributes() != cudaSuccess) return -5;
+  if (e->graph) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  const bool prof = e->profiling;
+  e->profiling = false;
+  if (cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    e->profiling = prof;
+    return -5;
+  }
+  const int rc = enqueue_eval(*e, kmode, xc_code, precision, d_pa, kmode == kModeUks ? d_pb : nullptr, d_va,
+                              kmode == kModeUks ? d_vb : nullptr, nullptr, nullptr, d_result, e->stream);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t end = cudaStreamEndCapture(e->stream, &graph);
+  e->profiling = prof;
+  if (rc || end != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return rc ? rc : -5;
+  }
+  const cudaError_t inst = cudaGraphInstantiate(&e->graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (inst != cudaSuccess) {
+    e->graph = nullptr;
+    cudaGetLastError();
+    return -5;
+  }
+  return 0;
+}
+
+int calchem_xc_graph_launch(uint64_t grid_id, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (!e->graph) return -1;
+  return cudaGraphLaunch(e->graph, (cudaStream_t)stream) == cudaSuccess ? 0 : -5;
+}
+
+int calchem_xc_last_status(uint64_t grid_id) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (!e->ws) return 0;
+  int st = 0;
+  if (cudaMemcpy(&st, e->d_counter + 2, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -5;
+  return st != 0 ? -7 : 0;
 }
 
 int calchem_xc_last_launch_count(uint64_t grid_id) {

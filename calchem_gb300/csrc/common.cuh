@@ -19,7 +19,8 @@ struct BatchDesc {
   int n_cand;      // candidate shells
   int ao_start;    // first entry in batch_ao (local AO -> global AO)
   int m;           // AOs of the candidate shells
-  int pad0, pad1;
+  int mol;         // molecule of the batch in a multi-molecule grid (0 otherwise)
+  int pad1;
 };
 
 // Evaluation modes of the block kernels.
@@ -50,7 +51,19 @@ struct DevGrid {
   const float4* prim_f;
   const float2* comp_f;
   const float2* shell_cf;  // shell centres as float pairs, 3 per shell (x, y, z)
+  // Multi-molecule grids: molecule i has mol_n[i] AOs, its density and Vxc are the mol_n[i]^2
+  // block starting at element mol_off[i] of the packed matrices, and its rows start at
+  // mol_ao_off[i] of packed per-AO vectors.  nullptr for a single molecule (n_ao AOs, offset 0).
+  const int* mol_n;
+  const long long* mol_off;
+  const int* mol_ao_off;
+  long long nn_total;  // elements of the packed matrices (n_ao^2 for a single molecule)
+  int n_total;         // rows of the packed matrices (n_ao for a single molecule)
 };
+
+__device__ __forceinline__ int mol_nao(const DevGrid& G, int mol) { return G.mol_n ? G.mol_n[mol] : G.n_ao; }
+__device__ __forceinline__ long long mol_mat(const DevGrid& G, int mol) { return G.mol_off ? G.mol_off[mol] : 0ll; }
+__device__ __forceinline__ int mol_row(const DevGrid& G, int mol) { return G.mol_ao_off ? G.mol_ao_off[mol] : 0; }
 
 struct EvalArgs {
   int mode;

@@ -1,0 +1,33 @@
+// launch.h -- host-side launchers of the device kernels, shared by the C ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace cxc {
+// FP64 form (vxc_fp64.cu)
+cudaError_t launch_fp64(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st);
+size_t fp64_smem_bytes();
+// Per-molecule deterministic (Exc, N_a, N_b) sums: batches [batch_off[i], batch_off[i + 1]) go to
+// out[i * n_out ...]; batch_off = nullptr for one molecule.
+cudaError_t launch_reduce(const double* part, int n_batches, const int* batch_off, int n_mols, double* out, int n_out,
+                          cudaStream_t st);
+cudaError_t launch_reduce(const double* part, int n_batches, double* out, int n_out, cudaStream_t st);
+// Symmetric completion of each molecule's Vxc block (mol_n / mol_off = nullptr for one molecule).
+cudaError_t launch_mirror(double* V, int max_n, const int* mol_n, const long long* mol_off, int n_mols, int from_upper,
+                          cudaStream_t st);
+cudaError_t launch_mirror(double* V, int n, int from_upper, cudaStream_t st);
+// Tensor-core form (vxc_mixed.cu)
+int mixed_supported(int mode);
+size_t mixed_slab_doubles(int max_m);
+int mixed_ctas_per_sm();
+int mixed_max_m();
+cudaError_t launch_mixed(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st);
+cudaError_t launch_mixed_prepare(const double* P, int n_total, const int* mol_n, const long long* mol_off,
+                                 const int* mol_ao_off, int n_mols, void* out, int* fexp, cudaStream_t st);
+// Dynamic shared-memory limits of the persistent kernels, set once per process (the launchers call
+// these; a graph capture calls them first so that no attribute is set while capturing).
+cudaError_t fp64_set_attributes();
+cudaError_t mixed_set_attributes();
+}  // namespace cxc

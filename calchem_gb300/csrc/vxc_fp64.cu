@@ -18,6 +18,8 @@
 // supplied by the caller.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "xc_device.cuh"
 
@@ -122,7 +124,8 @@ __device__ void batch_density(const DevGrid& G, const BatchDesc& bd, const doubl
   const int g = tid & (kBlockPts - 1);
   const int h = tid >> 7;
   const int m = bd.m;
-  const int n = G.n_ao;
+  const int n = mol_nao(G, bd.mol);
+  P += mol_mat(G, bd.mol);
   const int* __restrict__ ao = G.batch_ao + bd.ao_start;
   const size_t plane = (size_t)m_pad * kBlockPts;
   double rho = 0, sx = 0, sy = 0, sz = 0;
@@ -194,7 +197,8 @@ __device__ void accumulate_v(const DevGrid& G, const BatchDesc& bd, const double
                              int zplane, double* __restrict__ V, Fp64Smem& S) {
   const int tid = threadIdx.x;
   const int m = bd.m;
-  const int n = G.n_ao;
+  const int n = mol_nao(G, bd.mol);
+  V += mol_mat(G, bd.mol);
   const int* __restrict__ ao = G.batch_ao + bd.ao_start;
   const size_t plane = (size_t)m_pad * kBlockPts;
   const double* __restrict__ phi = slab;
@@ -371,11 +375,16 @@ __global__ void __launch_bounds__(kThreads, 1) vxc_fp64_kernel(DevGrid G, EvalAr
 
 // Deterministic final reduction of the per-batch (Exc, N_a, N_b) partials.
 __global__ void __launch_bounds__(256) reduce_batches_kernel(const double* __restrict__ part, int n_batches,
+                                                             const int* __restrict__ batch_off,
                                                              double* __restrict__ out, int n_out) {
   __shared__ double s[3][256];
   const int t = threadIdx.x;
+  // one CTA per molecule: its batches are [batch_off[mol], batch_off[mol + 1])
+  const int b0 = batch_off ? batch_off[blockIdx.x] : 0;
+  const int b1 = batch_off ? batch_off[blockIdx.x + 1] : n_batches;
+  out += (size_t)blockIdx.x * n_out;
   double a = 0, b = 0, c = 0;
-  for (int i = t; i < n_batches; i += 256) {
+  for (int i = b0 + t; i < b1; i += 256) {
     a += part[3 * (size_t)i];
     b += part[3 * (size_t)i + 1];
     c += part[3 * (size_t)i + 2];
@@ -401,11 +410,16 @@ __global__ void __launch_bounds__(256) reduce_batches_kernel(const double* __res
 
 // Completes a symmetric matrix from one triangle: from_upper = 0 copies the lower triangle into
 // the upper one (FP64 path), from_upper = 1 the upper into the lower (tensor-core path).
-__global__ void mirror_kernel(double* __restrict__ V, int n, int from_upper) {
-  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (size_t)n * n) return;
-  const int i = (int)(idx / n), j = (int)(idx % n);
-  if (from_upper ? (j < i) : (j > i)) V[idx] = V[(size_t)j * n + i];
+__global__ void mirror_kernel(double* __restrict__ V, int n_single, const int* __restrict__ mol_n,
+                              const long long* __restrict__ mol_off, int from_upper) {
+  // blockIdx.y = molecule; grid-stride over its n^2 elements
+  const int n = mol_n ? mol_n[blockIdx.y] : n_single;
+  double* Vm = V + (mol_off ? mol_off[blockIdx.y] : 0ll);
+  const size_t nn = (size_t)n * n;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < nn; idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / n), j = (int)(idx % n);
+    if (from_upper ? (j < i) : (j > i)) Vm[idx] = Vm[(size_t)j * n + i];
+  }
 }
 
 }  // namespace cxc
@@ -413,27 +427,42 @@ __global__ void mirror_kernel(double* __restrict__ V, int n, int from_upper) {
 // Launch helpers used by the C ABI layer.
 namespace cxc {
 
-cudaError_t launch_fp64(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st) {
+cudaError_t fp64_set_attributes() {
   static bool attr_set = false;
-  const size_t smem = sizeof(Fp64Smem);
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(vxc_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
-  vxc_fp64_kernel<<<n_ctas, kThreads, smem, st>>>(G, A);
+  if (attr_set) return cudaSuccess;
+  const cudaError_t e =
+      cudaFuncSetAttribute(vxc_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Fp64Smem));
+  if (e == cudaSuccess) attr_set = true;
+  return e;
+}
+
+cudaError_t launch_fp64(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st) {
+  const cudaError_t e = fp64_set_attributes();
+  if (e != cudaSuccess) return e;
+  vxc_fp64_kernel<<<n_ctas, kThreads, sizeof(Fp64Smem), st>>>(G, A);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reduce(const double* part, int n_batches, const int* batch_off, int n_mols, double* out, int n_out,
+                          cudaStream_t st) {
+  reduce_batches_kernel<<<n_mols, 256, 0, st>>>(part, n_batches, batch_off, out, n_out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_reduce(const double* part, int n_batches, double* out, int n_out, cudaStream_t st) {
-  reduce_batches_kernel<<<1, 256, 0, st>>>(part, n_batches, out, n_out);
+  return launch_reduce(part, n_batches, nullptr, 1, out, n_out, st);
+}
+
+cudaError_t launch_mirror(double* V, int max_n, const int* mol_n, const long long* mol_off, int n_mols, int from_upper,
+                          cudaStream_t st) {
+  const size_t nn = (size_t)max_n * max_n;
+  const unsigned bx = (unsigned)std::min<size_t>((nn + 255) / 256, 4096);
+  mirror_kernel<<<dim3(bx, (unsigned)n_mols), 256, 0, st>>>(V, max_n, mol_n, mol_off, from_upper);
   return cudaGetLastError();
 }
 
 cudaError_t launch_mirror(double* V, int n, int from_upper, cudaStream_t st) {
-  const size_t nn = (size_t)n * n;
-  mirror_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(V, n, from_upper);
-  return cudaGetLastError();
+  return launch_mirror(V, n, nullptr, nullptr, 1, from_upper, st);
 }
 
 }  // namespace cxc

@@ -295,7 +295,6 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
 
   const int tid = threadIdx.x, warp = tid >> 5;
   const int g = tid & 127, h = tid >> 7;
-  const int n = G.n_ao;
   const bool uks = A.mode == kModeUks;
   const int nspin = uks ? 2 : 1;
 
@@ -325,10 +324,11 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
   const size_t P = (size_t)m_pad_all * 128;  // floats per plane
   float* planes = reinterpret_cast<float*>(A.slab + (size_t)blockIdx.x * A.slab_stride);
   __nv_bfloat16* img = reinterpret_cast<__nv_bfloat16*>(planes + 8 * P);  // 6 images of P bf16
-  const uint2* Dhl_a = reinterpret_cast<const uint2*>(A.Pa);
-  const uint2* Dhl_b = Dhl_a + (size_t)n * n;
-  const int* fexp_a = reinterpret_cast<const int*>(Dhl_a + 2 * (size_t)n * n);
-  const int* fexp_b = fexp_a + n;
+  // split densities: [alpha nn_total][beta nn_total] uint2, then row exponents [alpha n_total][beta n_total]
+  const uint2* Dhl_a0 = reinterpret_cast<const uint2*>(A.Pa);
+  const uint2* Dhl_b0 = Dhl_a0 + G.nn_total;
+  const int* fexp_a0 = reinterpret_cast<const int*>(Dhl_a0 + 2 * G.nn_total);
+  const int* fexp_b0 = fexp_a0 + G.n_total;
 
   // one MMA round: wait for the commit of the phase just issued
   auto wait_mma = [&]() -> bool {
@@ -347,6 +347,9 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
     const int b = G.order[q];
     const BatchDesc bd = G.batches[b];
     const int m = bd.m;
+    const int n = mol_nao(G, bd.mol);
+    const long long moff = mol_mat(G, bd.mol);
+    const int roff = mol_row(G, bd.mol);
     const int m_pad = (m + 127) / 128 * 128;
     for (int i = tid; i < m; i += kMT) s_ao[i] = G.batch_ao[bd.ao_start + i];
     ao_eval_df(G, bd, planes, P, m_pad, s_tab);
@@ -368,8 +371,8 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
 
     double spin_rho[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     for (int s = 0; s < nspin && !failed; ++s) {
-      const uint2* Dhl = s ? Dhl_b : Dhl_a;
-      const int* fexp = s ? fexp_b : fexp_a;
+      const uint2* Dhl = (s ? Dhl_b0 : Dhl_a0) + moff;
+      const int* fexp = (s ? fexp_b0 : fexp_a0) + roff;
       const int eg = s_eg[g];
       df32 dr = {0.f, 0.f}, dgx = {0.f, 0.f}, dgy = {0.f, 0.f}, dgz = {0.f, 0.f};
       const int nkb = m_pad / 64;
@@ -552,7 +555,7 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
         *reinterpret_cast<uint4*>(img + 5 * P + o) = lo;
       }
       __syncthreads();
-      double* V = s ? A.Vb : A.Va;
+      double* V = (s ? A.Vb : A.Va) + moff;
       const uint32_t idesc = idesc_bf16_f32(128, 128);
       for (int I = 0; I < m_pad && !failed; I += 128) {
         for (int J = 0; J <= I && !failed; J += 128) {
@@ -635,10 +638,26 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
 // D (FP64, n x n) -> per-row fixed-point split: row nu is scaled by 2^-f_nu (|x| < 1) and cut into
 // multiples of 2^-7, 2^-15, 2^-23, 2^-31 (computed in FP64, each exact in BF16); packed as
 // x = hi | mid << 16, y = lo | lo2 << 16.  One CTA per row.
-__global__ void __launch_bounds__(256) split_density_kernel(const double* __restrict__ D, int n,
+__global__ void __launch_bounds__(256) split_density_kernel(const double* __restrict__ D, int n_single,
+                                                           const int* __restrict__ mol_n,
+                                                           const long long* __restrict__ mol_off,
+                                                           const int* __restrict__ mol_ao_off, int n_mols,
                                                            uint2* __restrict__ out, int* __restrict__ fexp) {
   __shared__ double red[256];
-  const int row = blockIdx.x;
+  // packed row r belongs to the molecule whose row range [mol_ao_off[i], mol_ao_off[i + 1]) holds it
+  int mol = 0;
+  if (mol_ao_off) {
+    int lo = 0, hi = n_mols - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (mol_ao_off[mid] <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    mol = lo;
+  }
+  const int n = mol_n ? mol_n[mol] : n_single;
+  const int row = (int)blockIdx.x - (mol_ao_off ? mol_ao_off[mol] : 0);
+  D += mol_off ? mol_off[mol] : 0ll;
+  out += mol_off ? mol_off[mol] : 0ll;
   const double* d = D + (size_t)row * n;
   double mx = 0.0;
   for (int j = threadIdx.x; j < n; j += 256) mx = fmax(mx, fabs(d[j]));
@@ -650,7 +669,7 @@ __global__ void __launch_bounds__(256) split_density_kernel(const double* __rest
   }
   int f = 0;
   frexp(red[0], &f);
-  if (threadIdx.x == 0) fexp[row] = f;
+  if (threadIdx.x == 0) fexp[blockIdx.x] = f;
   for (int j = threadIdx.x; j < n; j += 256) {
     const double x = ldexp(d[j], -f);
     const double h = rint(x * 128.0) / 128.0;
@@ -676,20 +695,26 @@ int mixed_ctas_per_sm() { return 1; }
 
 int mixed_max_m() { return kMaxMixedM; }
 
-cudaError_t launch_mixed(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st) {
+cudaError_t mixed_set_attributes() {
   static bool attr = false;
+  if (attr) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(vxc_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  if (e == cudaSuccess) attr = true;
+  return e;
+}
+
+cudaError_t launch_mixed(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st) {
   if (A.max_m > kMaxMixedM) return cudaErrorInvalidValue;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(vxc_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  const cudaError_t e = mixed_set_attributes();
+  if (e != cudaSuccess) return e;
   vxc_mixed_kernel<<<n_ctas, kMT, kSmemBytes, st>>>(G, A);
   return cudaGetLastError();
 }
 
-cudaError_t launch_mixed_prepare(const double* P, int n, void* out, int* fexp, cudaStream_t st) {
-  split_density_kernel<<<n, 256, 0, st>>>(P, n, reinterpret_cast<uint2*>(out), fexp);
+cudaError_t launch_mixed_prepare(const double* P, int n_total, const int* mol_n, const long long* mol_off,
+                                 const int* mol_ao_off, int n_mols, void* out, int* fexp, cudaStream_t st) {
+  split_density_kernel<<<n_total, 256, 0, st>>>(P, n_total, mol_n, mol_off, mol_ao_off, n_mols,
+                                                reinterpret_cast<uint2*>(out), fexp);
   return cudaGetLastError();
 }
 

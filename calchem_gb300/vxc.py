@@ -111,6 +111,20 @@ class GpuVxcGrid:
             pass
 
 
+def _upload_points(basis, grid) -> int:
+    """Batches and uploads one molecule's grid (calchem_xc_upload_points); returns its grid id."""
+    lib = _native.load()
+    sh, pr, co = basis.gpu_arrays()
+    xyzw = np.ascontiguousarray(grid.xyzw, dtype=np.float64)
+    if len(xyzw) == 0:
+        raise ValueError("empty grid")
+    gid = next(_ids)
+    _native.check("calchem_xc_upload_points", lib.calchem_xc_upload_points(
+        _native.ptr(sh), len(sh), _native.ptr(pr), len(pr), _native.ptr(co), len(co), _native.ptr(xyzw),
+        len(xyzw), basis.n_ao, gid, resolve_gpu_memory_limit()))
+    return gid
+
+
 class _EngineBase:
     def __init__(self, basis, grid, use_gpu=True, precision="fp64"):
         if not use_gpu:
@@ -121,16 +135,7 @@ class _EngineBase:
         self.gpu_fallback_invocations = 0
         self.grid_id = 0
         self.last_nelec = None
-        lib = _native.load()
-        sh, pr, co = basis.gpu_arrays()
-        xyzw = np.ascontiguousarray(grid.xyzw, dtype=np.float64)
-        if len(xyzw) == 0:
-            raise ValueError("empty grid")
-        gid = next(_ids)
-        _native.check("calchem_xc_upload_points", lib.calchem_xc_upload_points(
-            _native.ptr(sh), len(sh), _native.ptr(pr), len(pr), _native.ptr(co), len(co), _native.ptr(xyzw),
-            len(xyzw), self.n_ao, gid, resolve_gpu_memory_limit()))
-        self.grid_id = gid
+        self.grid_id = _upload_points(basis, grid)
 
     @classmethod
     def new_with_gpu(cls, basis, grid, use_gpu=True, precision="fp64"):
@@ -220,3 +225,112 @@ def evaluate_vxc_uks(basis, grid, func, pa, pb, precision="fp64"):
         return eng.evaluate(basis, grid, func, pa, pb)
     finally:
         eng.close()
+
+
+class VxcGroup:
+    """Many molecules, one persistent kernel launch per evaluation (calchem_xc_group_create).
+
+    ``members`` is a sequence of (basis, grid) pairs.  Every member's grid is batched as a single
+    engine would batch it, then all batches join one device work queue, so the per-member Exc and
+    Nelec equal a single engine's bit for bit and the members share the GPU without a launch each.
+    Densities and Vxc are exchanged as lists of per-member matrices (host) or as one packed device
+    vector whose member blocks start at ``offsets`` (device and graph paths).
+    """
+
+    def __init__(self, members, precision="fp64"):
+        lib = _native.load()
+        self.precision = _PRECISION[precision]
+        self.grid_id = 0
+        ids = []
+        try:
+            for basis, grid in members:
+                ids.append(_upload_points(basis, grid))
+            gid = next(_ids)
+            arr = np.array(ids, dtype=np.uint64)
+            _native.check("calchem_xc_group_create", lib.calchem_xc_group_create(
+                _native.ptr(arr), len(ids), gid, resolve_gpu_memory_limit()))
+            self.grid_id = gid
+        finally:
+            for i in ids:
+                lib.calchem_cuda_vxc_release(i)
+        nm = np.zeros(1, np.int32)
+        _native.check("calchem_xc_group_layout", lib.calchem_xc_group_layout(self.grid_id, _native.ptr(nm), None,
+                                                                              None))
+        self.n_mols = int(nm[0])
+        self.sizes = np.zeros(self.n_mols, np.int32)
+        self.offsets = np.zeros(self.n_mols, np.int64)
+        _native.check("calchem_xc_group_layout", lib.calchem_xc_group_layout(
+            self.grid_id, _native.ptr(nm), _native.ptr(self.sizes), _native.ptr(self.offsets)))
+        self.packed_size = int(np.sum(self.sizes.astype(np.int64) ** 2))
+
+    def pack(self, mats) -> np.ndarray:
+        if len(mats) != self.n_mols:
+            raise ValueError(f"expected {self.n_mols} matrices")
+        out = np.empty(self.packed_size, dtype=np.float64)
+        for i, m in enumerate(mats):
+            n = int(self.sizes[i])
+            out[self.offsets[i]:self.offsets[i] + n * n] = _as_matrix(m, n).ravel()
+        return out
+
+    def unpack(self, packed):
+        return [np.array(packed[o:o + int(n) * int(n)]).reshape(int(n), int(n)) for n, o in zip(self.sizes, self.offsets)]
+
+    def plan_stats(self):
+        lib = _native.load()
+        nb = np.zeros(1, np.int32)
+        s1 = np.zeros(1)
+        s2 = np.zeros(1)
+        mm = np.zeros(1, np.int32)
+        _native.check("calchem_xc_plan_stats", lib.calchem_xc_plan_stats(
+            self.grid_id, _native.ptr(nb), _native.ptr(s1), _native.ptr(s2), _native.ptr(mm)))
+        return int(nb[0]), float(s1[0]), float(s2[0]), int(mm[0])
+
+    def evaluate_rks(self, func, densities, precision=None):
+        """-> (exc[n_mols], nelec[n_mols], [Vxc per member])."""
+        lib = _native.load()
+        P = self.pack(densities)
+        V = np.zeros(self.packed_size)
+        exc = np.zeros(self.n_mols)
+        ne = np.zeros(self.n_mols)
+        prec = self.precision if precision is None else _PRECISION[precision]
+        _native.check("calchem_xc_evaluate_rks", lib.calchem_xc_evaluate_rks(
+            self.grid_id, _xc_code(func), prec, _native.ptr(P), _native.ptr(exc), _native.ptr(ne), _native.ptr(V)))
+        return exc, ne, self.unpack(V)
+
+    def evaluate_uks(self, func, pas, pbs, precision=None):
+        """-> (exc[n_mols], nelec[n_mols, 2], [Va], [Vb])."""
+        lib = _native.load()
+        Pa = self.pack(pas)
+        Pb = self.pack(pbs)
+        Va = np.zeros(self.packed_size)
+        Vb = np.zeros(self.packed_size)
+        exc = np.zeros(self.n_mols)
+        ne = np.zeros(2 * self.n_mols)
+        prec = self.precision if precision is None else _PRECISION[precision]
+        _native.check("calchem_xc_evaluate_uks", lib.calchem_xc_evaluate_uks(
+            self.grid_id, _xc_code(func), prec, _native.ptr(Pa), _native.ptr(Pb), _native.ptr(exc), _native.ptr(ne),
+            _native.ptr(Va), _native.ptr(Vb)))
+        return exc, ne.reshape(self.n_mols, 2), self.unpack(Va), self.unpack(Vb)
+
+    def capture_rks(self, func, d_total: int, d_result: int, d_v: int, precision=None):
+        """Captures one RKS evaluation on device buffers (addresses) into a CUDA graph."""
+        prec = self.precision if precision is None else _PRECISION[precision]
+        _native.check("calchem_xc_graph_capture", _native.load().calchem_xc_graph_capture(
+            self.grid_id, 0, _xc_code(func), prec, d_total, None, d_result, d_v, None))
+
+    def replay(self, stream: int = 0):
+        _native.check("calchem_xc_graph_launch", _native.load().calchem_xc_graph_launch(self.grid_id, stream))
+
+    def status(self) -> int:
+        return int(_native.load().calchem_xc_last_status(self.grid_id))
+
+    def close(self):
+        if self.grid_id:
+            _native.load().calchem_cuda_vxc_release(self.grid_id)
+            self.grid_id = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

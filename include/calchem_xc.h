@@ -136,7 +136,8 @@ int calchem_xc_grid_release(uint64_t grid_handle);
 /* One-call engine construction: chunks the points into batches of 128 (points with |w| < 1e-24
  * skipped), computes each batch's bounding sphere and candidate shells (vxc.rs:443-493), and
  * uploads everything -- including the weights, which the fused evaluators need -- under grid_id.
- * Returns -2 if grid_id exists. */
+ * The evaluation workspace (densities, Vxc, scratch) is allocated by the first evaluate, so a grid
+ * uploaded only to become part of a group (below) holds none.  Returns -2 if grid_id exists. */
 int calchem_xc_upload_points(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
                              const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
                              uint64_t grid_id, size_t memory_limit_bytes);
@@ -155,21 +156,55 @@ int calchem_xc_plan_stats(uint64_t grid_id, int* n_batches, double* sum_m2n, dou
 
 /* Closed shell.  d_total = P_total = 2 P_alpha (as RksVxcEngine::evaluate, vxc.rs:720-726).
  * exc_out = sum_g w_g f_xc; nelec_out = sum_g w_g rho_g (points with rho >= 1e-18);
- * v_out = full symmetric alpha-spin Vxc. */
+ * v_out = full symmetric alpha-spin Vxc.
+ * On a group (calchem_xc_group_create) the matrices are the members' blocks packed one after the
+ * other (calchem_xc_group_layout gives the offsets) and exc_out / nelec_out hold one value per
+ * member. */
 int calchem_xc_evaluate_rks(uint64_t grid_id, int xc_code, int precision, const double* h_d_total,
                             double* exc_out, double* nelec_out, double* h_v_out);
 
-/* Open shell (UksVxcEngine::evaluate, vxc.rs:1662-1669).  nelec_out[0..1] = (N_alpha, N_beta). */
+/* Open shell (UksVxcEngine::evaluate, vxc.rs:1662-1669).  nelec_out[0..1] = (N_alpha, N_beta);
+ * on a group, exc_out[i] and nelec_out[2 i .. 2 i + 1] for member i. */
 int calchem_xc_evaluate_uks(uint64_t grid_id, int xc_code, int precision, const double* h_pa, const double* h_pb,
                             double* exc_out, double* nelec_out, double* h_va_out, double* h_vb_out);
 
 /* Device-pointer variants (inputs and outputs already in device memory; enqueued on `stream`,
  * a cudaStream_t, 0 for the legacy stream).  d_result receives (Exc, N_alpha + N_beta) for RKS and
- * (Exc, N_alpha, N_beta) for UKS.  They return after enqueueing; the caller synchronises. */
+ * (Exc, N_alpha, N_beta) for UKS, once per member of a group.  They return after enqueueing; the
+ * caller synchronises and may then read the device status with calchem_xc_last_status. */
 int calchem_xc_evaluate_rks_device(uint64_t grid_id, int xc_code, int precision, const double* d_total,
                                    double* d_result, double* d_v, void* stream);
 int calchem_xc_evaluate_uks_device(uint64_t grid_id, int xc_code, int precision, const double* d_pa,
                                    const double* d_pb, double* d_result, double* d_va, double* d_vb, void* stream);
+
+/* ======================================================================================
+ * (3b) Many molecules in one launch, and CUDA-graph replay.  No counterpart in the reference.
+ * ====================================================================================== */
+
+/* Concatenates already-uploaded grids (calchem_xc_upload_points, weights attached) into one group
+ * under group_id: one work queue over every member's batches, processed by one persistent kernel
+ * launch per evaluate.  The members' device data are copied, so they may be released afterwards.
+ * Returns -2 for an unknown or grouped member id or an existing group_id, -1 for repeated ids,
+ * -3 over memory_limit_bytes, -4 / -5 on allocation / copy failure. */
+int calchem_xc_group_create(const uint64_t* member_ids, int n_members, uint64_t group_id, size_t memory_limit_bytes);
+
+/* Layout of the packed matrices of a group (also valid for a single grid: one member at offset 0):
+ * member i is the mol_n[i] x mol_n[i] block starting at element mol_off[i].  mol_n_out and
+ * mol_off_out may be NULL; otherwise they hold n_mols entries. */
+int calchem_xc_group_layout(uint64_t grid_id, int* n_mols_out, int* mol_n_out, long long* mol_off_out);
+
+/* Captures one device evaluation of grid_id (a single grid or a group) into a CUDA graph held by
+ * the library: mode 0 = RKS (d_pa = P_total, d_va), 1 = UKS (d_pa, d_pb, d_va, d_vb), arguments as
+ * the _device evaluators.  The graph keeps these device pointers; calchem_xc_graph_launch replays
+ * it on any stream (one kernel-launch latency for the whole sequence: density split, quadrature,
+ * reductions, symmetrisation).  Capturing again replaces the graph. */
+int calchem_xc_graph_capture(uint64_t grid_id, int mode, int xc_code, int precision, const double* d_pa,
+                             const double* d_pb, double* d_result, double* d_va, double* d_vb);
+int calchem_xc_graph_launch(uint64_t grid_id, void* stream);
+
+/* Device status of the last evaluation or graph replay of grid_id (synchronous read): 0, or -7 when
+ * a device-side wait expired. */
+int calchem_xc_last_status(uint64_t grid_id);
 
 /* Number of kernel launches the last evaluate on grid_id enqueued (for launch accounting). */
 int calchem_xc_last_launch_count(uint64_t grid_id);
