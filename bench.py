@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="octane_b3lyp",
+                    choices=["octane_b3lyp", "c54h18_pbe0_uks", "water_clusters_pbe"],
+                    help="octane_b3lyp is the headline; the others report the same line for the UKS flake "
+                         "and the 64-cluster batched launch")
     return ap.parse_args()
 
 
@@ -196,10 +200,136 @@ def run_reference(args):
     return 0
 
 
+class _Work:
+    """One benchmark workload: the GPU objects, device buffers and the three ways to run one build
+    (device step, host-buffer step, FP64 plain comparison)."""
+
+    def __init__(self, name, torch, dev, prec_name):
+        from calchem_gb300 import (BasisSet, GridLevel, MolecularGrid, RksVxcEngine, UksVxcEngine, VxcGroup,
+                                   _native, workloads)
+        self.name = name
+        self.torch = torch
+        self.dev = dev
+        self.lib = _native.load()
+        self.prec = 1 if prec_name == "mixed" else 0
+        self.prec_name = prec_name
+        self.graph = False
+        if name == "octane_b3lyp":
+            mol, basis, D = build_inputs()
+            grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
+            self.kind, self.func, self.xc = "rks", "b3lyp", 3
+            self.obj = RksVxcEngine(basis, grid)
+            self.mats = [D]
+            self.n_points = len(grid)
+            self.description = WORKLOAD
+            self.mol, self.basis = mol, basis
+        elif name == "c54h18_pbe0_uks":
+            mol, basis, func, (Pa, Pb) = workloads.build_workload("c54h18_pbe0_uks", SEED)
+            grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
+            self.kind, self.func, self.xc = "uks", "pbe0", 5
+            self.obj = UksVxcEngine(basis, grid)
+            self.mats = [Pa, Pb]
+            self.n_points = len(grid)
+            na, nb = mol.n_alpha_beta()
+            self.description = (f"C54H18 circumcoronene flake (C-C 1.42, C-H 1.09 A, planar), UKS PBE0, 6-31G(d) "
+                                f"Cartesian {basis.n_ao} AOs, Fine grid, seeded D (n_alpha {na}, n_beta {nb}, "
+                                f"seeds {SEED}/{SEED + 1})")
+        elif name == "water_clusters_pbe":
+            sizes = workloads.cluster_batch_sizes()
+            members, dens = [], []
+            for i, k in enumerate(sizes):
+                mol = workloads.water_cluster(k, 1000 + i)
+                basis = BasisSet.from_name("6-31g(d)", mol)
+                grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
+                members.append((basis, grid))
+                dens.append(workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, SEED + i))
+            self.kind, self.func, self.xc = "group", "pbe", 2
+            self.obj = VxcGroup(members, precision=prec_name)
+            self.mats = dens
+            self.n_points = sum(len(g) for _, g in members)
+            self.description = (f"{len(sizes)} water clusters of 1-32 rigid waters (sizes PCG64 seed 2024, total "
+                                f"{sum(sizes)} waters, 1 g/cm^3, O-O >= 2.6 A, placement seeds 1000+i), PBE, "
+                                f"6-31G(d) Cartesian, Fine grid, seeded D; one persistent launch per build, "
+                                f"replayed as a CUDA graph")
+        else:
+            raise ValueError(name)
+        self.n_batches, self.sum_m2n, _, self.max_m = self.obj.plan_stats()
+        self.flops = (8.0 if self.kind == "uks" else 4.0) * self.sum_m2n
+        # packed device buffers
+        if self.kind == "group":
+            self.packed = [self.obj.pack(self.mats)]
+            self.n_mols = self.obj.n_mols
+            nn = self.obj.packed_size
+        else:
+            self.packed = [np.ascontiguousarray(m).ravel() for m in self.mats]
+            self.n_mols = 1
+            nn = self.packed[0].size
+        self.nn = nn
+        self.dP = [torch.from_numpy(p).to(dev) for p in self.packed]
+        self.dV = [torch.zeros(nn, dtype=torch.float64, device=dev) for _ in self.packed]
+        self.dres = torch.zeros(3 * self.n_mols + 1, dtype=torch.float64, device=dev)
+
+    @property
+    def gid(self):
+        return self.obj.grid_id
+
+    def n_ao(self):
+        return int(np.sqrt(self.nn)) if self.kind != "group" else int(self.obj.sizes.max())
+
+    def enable_profiling(self):
+        from calchem_gb300 import _native
+        _native.check("calchem_xc_set_profiling", self.lib.calchem_xc_set_profiling(self.gid, 1))
+
+    def capture(self):
+        """The group's iteration is replayed from a CUDA graph (device buffers fixed)."""
+        from calchem_gb300 import _native
+        _native.check("calchem_xc_graph_capture", self.lib.calchem_xc_graph_capture(
+            self.gid, 0, self.xc, self.prec, self.dP[0].data_ptr(), None, self.dres.data_ptr(),
+            self.dV[0].data_ptr(), None))
+        self.graph = True
+
+    def device_step(self, stream, prec=None):
+        prec = self.prec if prec is None else prec
+        if self.graph and prec == self.prec:
+            return self.lib.calchem_xc_graph_launch(self.gid, stream.cuda_stream)
+        if self.kind == "uks":
+            return self.lib.calchem_xc_evaluate_uks_device(
+                self.gid, self.xc, prec, self.dP[0].data_ptr(), self.dP[1].data_ptr(), self.dres.data_ptr(),
+                self.dV[0].data_ptr(), self.dV[1].data_ptr(), stream.cuda_stream)
+        return self.lib.calchem_xc_evaluate_rks_device(self.gid, self.xc, prec, self.dP[0].data_ptr(),
+                                                       self.dres.data_ptr(), self.dV[0].data_ptr(),
+                                                       stream.cuda_stream)
+
+    def host_step(self, prec=None):
+        """The reference-facing host-buffer call (copies inside); returns (exc[], nelec[], [V...])."""
+        from calchem_gb300 import _native
+        prec = self.prec if prec is None else prec
+        exc = np.zeros(self.n_mols)
+        if self.kind == "uks":
+            ne = np.zeros(2)
+            Va, Vb = np.zeros(self.nn), np.zeros(self.nn)
+            _native.check("calchem_xc_evaluate_uks", self.lib.calchem_xc_evaluate_uks(
+                self.gid, self.xc, prec, _native.ptr(self.packed[0]), _native.ptr(self.packed[1]), _native.ptr(exc),
+                _native.ptr(ne), _native.ptr(Va), _native.ptr(Vb)))
+            return exc, ne, [Va, Vb]
+        ne = np.zeros(self.n_mols)
+        V = np.zeros(self.nn)
+        _native.check("calchem_xc_evaluate_rks", self.lib.calchem_xc_evaluate_rks(
+            self.gid, self.xc, prec, _native.ptr(self.packed[0]), _native.ptr(exc), _native.ptr(ne), _native.ptr(V)))
+        return exc, ne, [V]
+
+    def io_bytes(self):
+        k = len(self.packed)
+        return k * self.nn * 8, k * self.nn * 8 + (3 if self.kind == "uks" else 2) * 8 * self.n_mols
+
+    def close(self):
+        self.obj.close()
+
+
 def run_ours(args):
     import torch
 
-    from calchem_gb300 import GridLevel, MolecularGrid, RksVxcEngine, _native
+    from calchem_gb300 import _native
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -210,42 +340,22 @@ def run_ours(args):
     else:
         dist = None
     dev = torch.device("cuda", torch.cuda.current_device())
-    lib = _native.load()
-    mol, basis, D = build_inputs()
-    grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
-    prec_name = args.precision
-    mixed_ok = True
-    if prec_name == "auto":
-        prec_name = "mixed"
-    eng = RksVxcEngine(basis, grid)
-    n = basis.n_ao
-    n_batches, sum_m2n, _, max_m = eng.plan_stats()
-    flops = 4.0 * sum_m2n
-    prec = 1 if prec_name == "mixed" else 0
-    # probe the mixed path; fall back to reporting the FP64 form if it is not enabled
-    probe_V = np.zeros((n, n))
-    e1, n1 = np.zeros(1), np.zeros(1)
-    rc = lib.calchem_xc_evaluate_rks(eng.grid_id, 3, prec, _native.ptr(D), _native.ptr(e1), _native.ptr(n1),
-                                     _native.ptr(probe_V))
-    if rc != 0 and prec == 1:
-        mixed_ok = False
-        prec, prec_name = 0, "fp64"
+    prec_name = "mixed" if args.precision == "auto" else args.precision
+    W = _Work(args.workload, torch, dev, prec_name)
+    lib = W.lib
     stream = torch.cuda.Stream(device=dev)
-    dD = torch.from_numpy(D).to(dev)
-    dV = torch.zeros((n, n), dtype=torch.float64, device=dev)
-    dres = torch.zeros(4, dtype=torch.float64, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    _native.check("calchem_xc_set_profiling", lib.calchem_xc_set_profiling(eng.grid_id, 1))
+    W.enable_profiling()
+    if W.kind == "group":
+        W.host_step()  # allocates the workspace outside the capture
+        torch.cuda.synchronize()
+        W.capture()
     torch.cuda.synchronize()
-
-    def step_device():
-        return lib.calchem_xc_evaluate_rks_device(eng.grid_id, 3, prec, dD.data_ptr(), dres.data_ptr(),
-                                                  dV.data_ptr(), stream.cuda_stream)
 
     for _ in range(max(3, args.warmup)):
         with torch.cuda.stream(stream):
             flush.zero_()
-        _native.check("evaluate", step_device())
+        _native.check("evaluate", W.device_step(stream))
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -261,49 +371,52 @@ def run_ours(args):
             flush.zero_()
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record(stream)
-        _native.check("evaluate", step_device())
+        _native.check("evaluate", W.device_step(stream))
         e.record(stream)
-        km = np.zeros(1, np.float32)
-        _native.check("last_kernel_ms", lib.calchem_xc_last_kernel_ms(eng.grid_id, _native.ptr(km)))
         e.synchronize()
         step_ms.append(s.elapsed_time(e))
-        kern_ms.append(float(km[0]))
-        launches += eng.last_launch_count()
+        if not W.graph:
+            km = np.zeros(1, np.float32)
+            _native.check("last_kernel_ms", lib.calchem_xc_last_kernel_ms(W.gid, _native.ptr(km)))
+            kern_ms.append(float(km[0]))
+        launches += lib.calchem_xc_last_launch_count(W.gid)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall0
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     clk = clocks.stop()
-    exc_dev = float(dres[0].item())
-    nelec_dev = float(dres[1].item())
+    _native.check("device status", lib.calchem_xc_last_status(W.gid))
+    res_dev = W.dres.cpu().numpy()
     ms = statistics.mean(step_ms)
+    if not kern_ms:  # graph replays: time the kernel once outside the graph
+        for _ in range(3):
+            _native.check("evaluate", lib.calchem_xc_evaluate_rks_device(
+                W.gid, W.xc, W.prec, W.dP[0].data_ptr(), W.dres.data_ptr(), W.dV[0].data_ptr(), stream.cuda_stream))
+            km = np.zeros(1, np.float32)
+            _native.check("last_kernel_ms", lib.calchem_xc_last_kernel_ms(W.gid, _native.ptr(km)))
+            kern_ms.append(float(km[0]))
     kms = statistics.mean(kern_ms)
     if dist:
         t = torch.tensor([ms], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     # ---- e2e through the host-buffer C ABI call (copies inside the timed region)
-    Vh = np.zeros((n, n))
-    e_h, n_h = np.zeros(1), np.zeros(1)
     e2e = []
+    host = None
     for i in range(args.warmup + args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        _native.check("calchem_xc_evaluate_rks", lib.calchem_xc_evaluate_rks(
-            eng.grid_id, 3, prec, _native.ptr(D), _native.ptr(e_h), _native.ptr(n_h), _native.ptr(Vh)))
+        host = W.host_step()
         if i >= args.warmup:
             e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = statistics.mean(e2e)
     # ---- the FP64 plain form on the same build, for the mixed-vs-plain comparison
     ref_fp64 = {}
-    if prec == 1:
-        Vf = np.zeros((n, n))
-        ef, nf = np.zeros(1), np.zeros(1)
-        lib.calchem_xc_evaluate_rks(eng.grid_id, 3, 0, _native.ptr(D), _native.ptr(ef), _native.ptr(nf),
-                                    _native.ptr(Vf))
+    if W.prec == 1:
+        ef, nf, Vf = W.host_step(prec=0)
         fts = []
         for _ in range(3):
             with torch.cuda.stream(stream):
@@ -311,56 +424,61 @@ def run_ours(args):
             torch.cuda.synchronize()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record(stream)
-            lib.calchem_xc_evaluate_rks_device(eng.grid_id, 3, 0, dD.data_ptr(), dres.data_ptr(), dV.data_ptr(),
-                                               stream.cuda_stream)
+            _native.check("evaluate", W.device_step(stream, prec=0))
             e.record(stream)
             e.synchronize()
             fts.append(s.elapsed_time(e))
+        dexc = host[0] - ef
         ref_fp64 = {"fp64_plain_ms": round(statistics.mean(fts), 4),
                     "speedup_vs_fp64_plain": round(statistics.mean(fts) / ms, 3),
-                    "dExc_vs_fp64": float(e_h[0] - ef[0]), "dNelec_vs_fp64": float(n_h[0] - nf[0]),
-                    "max_abs_dV_vs_fp64": float(np.max(np.abs(Vh - Vf)))}
+                    "dExc_vs_fp64": float(dexc[np.argmax(np.abs(dexc))]),
+                    "dNelec_vs_fp64": float(np.max(np.abs(host[1] - nf))),
+                    "max_abs_dV_vs_fp64": float(max(np.max(np.abs(a - b)) for a, b in zip(host[2], Vf)))}
+        if W.n_mols > 1:
+            ref_fp64["dExc_vs_fp64_is"] = "largest |dExc| over the molecules"
     pk, pk_kind = peaks()
-    if prec == 1:
+    if W.prec == 1:
         peak, bound, unit = pk.get("bf16_tflops", 1900.0), "tensor", "TFLOP/s"
         peak_note = f"dense bf16 burst, {pk_kind}"
     else:
         peak = fp64_peak_tflops(torch, dev)
         bound, unit = "tensor", "TFLOP/s"
         peak_note = "FP64 pipe: cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in the measured peaks)"
-    achieved = flops / (kms * 1e-3) / 1e12
-    traffic = NCU_TRAFFIC_BYTES.get(prec_name)
+    achieved = W.flops / (kms * 1e-3) / 1e12
+    traffic = NCU_TRAFFIC_BYTES.get(prec_name) if W.name == "octane_b3lyp" else None
+    h2d, d2h = W.io_bytes()
     line = {
         "metric": METRIC, "value": round(ms, 4), "unit": "ms", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64" if prec == 0 else "bf16x3 split (f32 accumulate) contractions, f64 functional/sums",
+        "dtype": "f64" if W.prec == 0 else "bf16x3 split (f32 accumulate) contractions, f64 functional/sums",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "precision": prec_name, "n_ao": n, "grid_points": len(grid),
-                   "batches": n_batches, "max_m": max_m, "l2": "flushed before every timed step (256 MiB write)",
+        "config": {"workload": W.description, "name": W.name, "precision": prec_name, "n_ao": W.n_ao(),
+                   "molecules": W.n_mols, "grid_points": W.n_points, "batches": W.n_batches, "max_m": W.max_m,
+                   "l2": "flushed before every timed step (256 MiB write)",
+                   "graph": "CUDA-graph replay per step" if W.graph else "direct launches",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
-        "grid_points_per_s": round(len(grid) / (ms * 1e-3), 1),
-        "exc": exc_dev, "nelec": nelec_dev,
+        "grid_points_per_s": round(W.n_points / (ms * 1e-3), 1),
+        "exc": float(res_dev[0]), "nelec": float(res_dev[1]),
         "roofline": {"bound": bound, "achieved": round(achieved, 4), "peak": round(peak, 2), "unit": unit,
                      "frac": round(achieved / peak, 5), "traffic": traffic,
                      "kernel": "vxc quadrature kernel", "kernel_ms": round(kms, 4),
-                     "work": f"4*sum(m^2 n) = {flops:.4e} flop per launch", "peak_source": peak_note},
-        "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": n * n * 8,
-                "d2h_bytes_per_step": n * n * 8 + 16},
+                     "work": f"{'8' if W.kind == 'uks' else '4'}*sum(m^2 n) = {W.flops:.4e} flop per launch",
+                     "peak_source": peak_note},
+        "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "wall_s_timed": round(t_wall, 3),
         "clocks": clk,
     }
     line.update(ref_fp64)
-    if not mixed_ok:
-        line["note"] = "mixed-precision path not enabled in this build; FP64 form reported"
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cms, threads, sample, _, _ = cpu_reference_run(basis, mol, D, 3, 1, budget_s=25.0)
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline and W.name == "octane_b3lyp":
+        D = W.mats[0]
+        cms, threads, sample, _, _ = cpu_reference_run(W.basis, W.mol, D, 3, 1, budget_s=25.0)
         line["cpu_baseline"] = {"value": round(cms, 3), "unit": "ms", "cores": threads, "kind": "port",
                                 "sample": sample}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    eng.close()
+    W.close()
     if dist:
         dist.destroy_process_group()
     return 0

@@ -9,6 +9,7 @@ Rust call surface (``RksVxcEngine``, ``UksVxcEngine``, ``MolecularGrid``,
 from .basis import BasisSet
 from .grid import GridLevel, MolecularGrid
 from .molecule import ANGSTROM_TO_BOHR, Atom, Molecule
+from . import autotune
 from .vxc import (FP64, MIXED, GpuVxcGrid, RksVxcEngine, UksVxcEngine, VxcGroup, evaluate_vxc_rks,
                   evaluate_vxc_uks, is_cuda_available)
 from .xc import XcFunctional

@@ -696,22 +696,29 @@ int calchem_xc_grid_release(uint64_t grid_handle) {
   return 0;
 }
 
-int calchem_xc_upload_points(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
-                             const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
-                             uint64_t grid_id, size_t memory_limit_bytes) {
+int calchem_xc_upload_points_ex(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
+                                const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
+                                int batch_pts, uint64_t grid_id, size_t memory_limit_bytes) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!h_shells || !h_prims || !h_comps || !h_xyzw || n_shells <= 0 || n_prims <= 0 || n_comps <= 0 || n_pts <= 0 ||
-      n_ao <= 0 || grid_id == 0)
+      n_ao <= 0 || grid_id == 0 || batch_pts < 16 || batch_pts > kBlockPts)
     return -1;
   if (g_grids.count(grid_id)) return -2;
   for (int s = 0; s < n_shells; ++s)
     if (!(h_shells[s].r2_cutoff >= 0.0)) return -1;
   Plan plan;
-  plan_batches(h_shells, n_shells, h_xyzw, n_pts, plan);
+  plan_batches(h_shells, n_shells, h_xyzw, n_pts, plan, batch_pts);
   if (plan.pts.empty()) return -1;
   return upload_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, plan.pts.data(), (int)plan.pts.size(),
                      plan.cand_offsets.data(), (int)plan.cand_offsets.size(), plan.cand_shells.data(),
                      (int)plan.cand_shells.size(), n_ao, grid_id, memory_limit_bytes, plan.weights.data(), false);
+}
+
+int calchem_xc_upload_points(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
+                             const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
+                             uint64_t grid_id, size_t memory_limit_bytes) {
+  return calchem_xc_upload_points_ex(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, h_xyzw, n_pts, n_ao,
+                                     kBlockPts, grid_id, memory_limit_bytes);
 }
 
 int calchem_xc_set_weights(uint64_t grid_id, const double* h_weights, int n_pts) {

@@ -400,12 +400,12 @@ void becke_tables(int n, const int* z, const double* xyz, std::vector<double>& i
     }
 }
 
-int plan_batches(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan) {
+int plan_batches(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan, int batch_pts) {
   plan = Plan();
   std::vector<int> keep;
-  keep.reserve(kPlanBatch);
-  for (int s0 = 0; s0 < n_pts; s0 += kPlanBatch) {
-    const int len = std::min(kPlanBatch, n_pts - s0);
+  keep.reserve(batch_pts);
+  for (int s0 = 0; s0 < n_pts; s0 += batch_pts) {
+    const int len = std::min(batch_pts, n_pts - s0);
     double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     keep.clear();
     for (int g = 0; g < len; ++g) {

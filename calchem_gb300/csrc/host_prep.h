@@ -49,6 +49,8 @@ struct Plan {
   std::vector<int> cand_offsets;
   std::vector<int> cand_shells;
 };
-int plan_batches(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan);
+// Chunks of batch_pts consecutive points (kPlanBatch = 128 in the reference, vxc.rs:96).
+int plan_batches(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan,
+                 int batch_pts = kPlanBatch);
 
 }  // namespace cxc

@@ -15,6 +15,8 @@ functional themselves, as CalChem's Rust engine does (vxc.rs:728-799).
 import itertools
 import os
 
+import ctypes
+
 import numpy as np
 
 from . import _native
@@ -111,22 +113,25 @@ class GpuVxcGrid:
             pass
 
 
-def _upload_points(basis, grid) -> int:
-    """Batches and uploads one molecule's grid (calchem_xc_upload_points); returns its grid id."""
+def _upload_points(basis, grid, batch_pts: int = 128) -> int:
+    """Batches and uploads one molecule's grid (calchem_xc_upload_points_ex); returns its grid id."""
     lib = _native.load()
     sh, pr, co = basis.gpu_arrays()
     xyzw = np.ascontiguousarray(grid.xyzw, dtype=np.float64)
     if len(xyzw) == 0:
         raise ValueError("empty grid")
     gid = next(_ids)
-    _native.check("calchem_xc_upload_points", lib.calchem_xc_upload_points(
+    _native.check("calchem_xc_upload_points_ex", lib.calchem_xc_upload_points_ex(
         _native.ptr(sh), len(sh), _native.ptr(pr), len(pr), _native.ptr(co), len(co), _native.ptr(xyzw),
-        len(xyzw), basis.n_ao, gid, resolve_gpu_memory_limit()))
+        len(xyzw), basis.n_ao, int(batch_pts), gid, resolve_gpu_memory_limit()))
     return gid
 
 
 class _EngineBase:
-    def __init__(self, basis, grid, use_gpu=True, precision="fp64"):
+    """batch_pts: points per batch (16..128; the reference's 128 by default), or "auto" to take
+    the autotuner's choice for this workload (tuned on first use, then cached)."""
+
+    def __init__(self, basis, grid, use_gpu=True, precision="fp64", batch_pts=128, func="b3lyp"):
         if not use_gpu:
             raise NotImplementedError("calchem_gb300 evaluates Vxc on the GPU only; there is no CPU engine")
         self.n_ao = basis.n_ao
@@ -135,11 +140,25 @@ class _EngineBase:
         self.gpu_fallback_invocations = 0
         self.grid_id = 0
         self.last_nelec = None
-        self.grid_id = _upload_points(basis, grid)
+        if batch_pts == "auto":
+            from . import autotune
+            batch_pts = autotune.choose_batch_pts(basis, grid, func, precision,
+                                                  spin="uks" if isinstance(self, UksVxcEngine) else "rks")
+        self.batch_pts = int(batch_pts)
+        self.grid_id = _upload_points(basis, grid, self.batch_pts)
 
     @classmethod
-    def new_with_gpu(cls, basis, grid, use_gpu=True, precision="fp64"):
-        return cls(basis, grid, use_gpu, precision)
+    def new_with_gpu(cls, basis, grid, use_gpu=True, precision="fp64", batch_pts=128):
+        return cls(basis, grid, use_gpu, precision, batch_pts)
+
+    def set_profiling(self, enable: bool = True):
+        _native.check("calchem_xc_set_profiling", _native.load().calchem_xc_set_profiling(self.grid_id, int(enable)))
+
+    def last_kernel_ms(self) -> float:
+        """Duration of the quadrature kernel of the last evaluate (profiling enabled)."""
+        ms = (ctypes.c_float * 1)()
+        _native.check("calchem_xc_last_kernel_ms", _native.load().calchem_xc_last_kernel_ms(self.grid_id, ms))
+        return float(ms[0])
 
     def telemetry(self):
         """(gpu_kernel_invocations, gpu_fallback_invocations) as in vxc.rs:420-425."""
@@ -237,14 +256,14 @@ class VxcGroup:
     vector whose member blocks start at ``offsets`` (device and graph paths).
     """
 
-    def __init__(self, members, precision="fp64"):
+    def __init__(self, members, precision="fp64", batch_pts=128):
         lib = _native.load()
         self.precision = _PRECISION[precision]
         self.grid_id = 0
         ids = []
         try:
             for basis, grid in members:
-                ids.append(_upload_points(basis, grid))
+                ids.append(_upload_points(basis, grid, batch_pts))
             gid = next(_ids)
             arr = np.array(ids, dtype=np.uint64)
             _native.check("calchem_xc_group_create", lib.calchem_xc_group_create(

@@ -142,6 +142,13 @@ int calchem_xc_upload_points(const AoShellGpu* h_shells, int n_shells, const AoP
                              const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
                              uint64_t grid_id, size_t memory_limit_bytes);
 
+/* As calchem_xc_upload_points with chunks of batch_pts (16..128) consecutive points instead of
+ * 128: smaller chunks have smaller bounding spheres, hence fewer candidate AOs per point, at the cost
+ * of more batches.  Results are the same up to summation order; the autotuner picks batch_pts. */
+int calchem_xc_upload_points_ex(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
+                                const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
+                                int batch_pts, uint64_t grid_id, size_t memory_limit_bytes);
+
 /* Attaches quadrature weights to a grid uploaded with calchem_cuda_vxc_upload_grid
  * (weights in the uploaded point order). */
 int calchem_xc_set_weights(uint64_t grid_id, const double* h_weights, int n_pts);
