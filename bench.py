@@ -38,6 +38,7 @@ METRIC = "Vxc build ms/SCF iter on 1 GB300: mixed+pruned vs FP64 plain at dExc<=
 WORKLOAD = ("C8H18 all-trans, B3LYP (VWN_RPA), 6-31G(d,p) Cartesian 210 AOs, CalChem Fine grid "
             "(99 radial shells, pruned Lebedev, Becke), seeded S-orthonormal D (33 occ, seed 7)")
 SEED = 7
+PRUNE_TOL = 5e-7  # per-molecule quadrature tolerance of the learned grid against the Fine grid (Eh)
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # DRAM bytes (read + write) per launch of the quadrature kernel from one ncu capture of this
 # workload; see profiles/.  None until a capture exists for the precision.
@@ -52,6 +53,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", default="learned", choices=["learned", "fine"],
+                    help="learned: the MLP-pruned grid with the Fine-grid judge (headline workload only)")
     ap.add_argument("--workload", default="octane_b3lyp",
                     choices=["octane_b3lyp", "c54h18_pbe0_uks", "water_clusters_pbe"],
                     help="octane_b3lyp is the headline; the others report the same line for the UKS flake "
@@ -204,9 +207,9 @@ class _Work:
     """One benchmark workload: the GPU objects, device buffers and the three ways to run one build
     (device step, host-buffer step, FP64 plain comparison)."""
 
-    def __init__(self, name, torch, dev, prec_name):
+    def __init__(self, name, torch, dev, prec_name, grid_kind="fine"):
         from calchem_gb300 import (BasisSet, GridLevel, MolecularGrid, RksVxcEngine, UksVxcEngine, VxcGroup,
-                                   _native, workloads)
+                                   _native, pruner, workloads)
         self.name = name
         self.torch = torch
         self.dev = dev
@@ -214,15 +217,30 @@ class _Work:
         self.prec = 1 if prec_name == "mixed" else 0
         self.prec_name = prec_name
         self.graph = False
+        self.plain = None  # the FP64-plain comparison object when it differs (learned grid)
+        self.grid_info = {"grid": "Fine"}
         if name == "octane_b3lyp":
             mol, basis, D = build_inputs()
             grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
             self.kind, self.func, self.xc = "rks", "b3lyp", 3
-            self.obj = RksVxcEngine(basis, grid)
             self.mats = [D]
-            self.n_points = len(grid)
             self.description = WORKLOAD
             self.mol, self.basis = mol, basis
+            if grid_kind == "learned":
+                t0 = time.perf_counter()
+                lg = pruner.LearnedGrid(mol, basis, tol=PRUNE_TOL)
+                picked = lg.levels.copy()
+                reverted, _ = lg.check(D, self.func)
+                self.grid_info = {"grid": f"MLP-pruned (per-atom tolerance {lg.tol_atom:.2e}, molecule {PRUNE_TOL:g}), "
+                                          f"Fine-grid judge on this density",
+                                  "grid_points_fine": len(grid), "grid_points_pruned": len(lg.grid),
+                                  "atoms_reverted_by_judge": len(reverted),
+                                  "levels_picked": np.bincount(picked, minlength=len(pruner.LEVELS)).tolist(),
+                                  "pruner_setup_s": round(time.perf_counter() - t0, 3)}
+                self.plain = RksVxcEngine(basis, grid)
+                grid = lg.grid
+            self.obj = RksVxcEngine(basis, grid)
+            self.n_points = len(grid)
         elif name == "c54h18_pbe0_uks":
             mol, basis, func, (Pa, Pb) = workloads.build_workload("c54h18_pbe0_uks", SEED)
             grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
@@ -288,8 +306,12 @@ class _Work:
             self.dV[0].data_ptr(), None))
         self.graph = True
 
-    def device_step(self, stream, prec=None):
+    def device_step(self, stream, prec=None, plain=False):
         prec = self.prec if prec is None else prec
+        if plain and self.plain is not None:
+            return self.lib.calchem_xc_evaluate_rks_device(self.plain.grid_id, self.xc, 0, self.dP[0].data_ptr(),
+                                                           self.dres.data_ptr(), self.dV[0].data_ptr(),
+                                                           stream.cuda_stream)
         if self.graph and prec == self.prec:
             return self.lib.calchem_xc_graph_launch(self.gid, stream.cuda_stream)
         if self.kind == "uks":
@@ -300,10 +322,11 @@ class _Work:
                                                        self.dres.data_ptr(), self.dV[0].data_ptr(),
                                                        stream.cuda_stream)
 
-    def host_step(self, prec=None):
+    def host_step(self, prec=None, plain=False):
         """The reference-facing host-buffer call (copies inside); returns (exc[], nelec[], [V...])."""
         from calchem_gb300 import _native
         prec = self.prec if prec is None else prec
+        gid = self.plain.grid_id if (plain and self.plain is not None) else self.gid
         exc = np.zeros(self.n_mols)
         if self.kind == "uks":
             ne = np.zeros(2)
@@ -315,7 +338,7 @@ class _Work:
         ne = np.zeros(self.n_mols)
         V = np.zeros(self.nn)
         _native.check("calchem_xc_evaluate_rks", self.lib.calchem_xc_evaluate_rks(
-            self.gid, self.xc, prec, _native.ptr(self.packed[0]), _native.ptr(exc), _native.ptr(ne), _native.ptr(V)))
+            gid, self.xc, prec, _native.ptr(self.packed[0]), _native.ptr(exc), _native.ptr(ne), _native.ptr(V)))
         return exc, ne, [V]
 
     def io_bytes(self):
@@ -324,6 +347,8 @@ class _Work:
 
     def close(self):
         self.obj.close()
+        if self.plain is not None:
+            self.plain.close()
 
 
 def run_ours(args):
@@ -341,7 +366,7 @@ def run_ours(args):
         dist = None
     dev = torch.device("cuda", torch.cuda.current_device())
     prec_name = "mixed" if args.precision == "auto" else args.precision
-    W = _Work(args.workload, torch, dev, prec_name)
+    W = _Work(args.workload, torch, dev, prec_name, args.grid)
     lib = W.lib
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -415,8 +440,8 @@ def run_ours(args):
     e2e_ms = statistics.mean(e2e)
     # ---- the FP64 plain form on the same build, for the mixed-vs-plain comparison
     ref_fp64 = {}
-    if W.prec == 1:
-        ef, nf, Vf = W.host_step(prec=0)
+    if W.prec == 1 or W.plain is not None:
+        ef, nf, Vf = W.host_step(prec=0, plain=True)
         fts = []
         for _ in range(3):
             with torch.cuda.stream(stream):
@@ -424,10 +449,25 @@ def run_ours(args):
             torch.cuda.synchronize()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record(stream)
-            _native.check("evaluate", W.device_step(stream, prec=0))
+            _native.check("evaluate", W.device_step(stream, prec=0, plain=True))
             e.record(stream)
             e.synchronize()
             fts.append(s.elapsed_time(e))
+        if W.plain is not None:  # the same mixed build on the Fine grid, to separate the two gains
+            mts = []
+            for _ in range(3):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                torch.cuda.synchronize()
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+                _native.check("evaluate", lib.calchem_xc_evaluate_rks_device(
+                    W.plain.grid_id, W.xc, W.prec, W.dP[0].data_ptr(), W.dres.data_ptr(), W.dV[0].data_ptr(),
+                    stream.cuda_stream))
+                e.record(stream)
+                e.synchronize()
+                mts.append(s.elapsed_time(e))
+            W.grid_info["mixed_on_fine_grid_ms"] = round(statistics.mean(mts), 4)
         dexc = host[0] - ef
         ref_fp64 = {"fp64_plain_ms": round(statistics.mean(fts), 4),
                     "speedup_vs_fp64_plain": round(statistics.mean(fts) / ms, 3),
@@ -453,7 +493,7 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f64" if W.prec == 0 else "bf16x3 split (f32 accumulate) contractions, f64 functional/sums",
         "data": "synthetic",
-        "config": {"workload": W.description, "name": W.name, "precision": prec_name, "n_ao": W.n_ao(),
+        "config": {"workload": W.description, "name": W.name, "precision": prec_name, **W.grid_info, "n_ao": W.n_ao(),
                    "molecules": W.n_mols, "grid_points": W.n_points, "batches": W.n_batches, "max_m": W.max_m,
                    "l2": "flushed before every timed step (256 MiB write)",
                    "graph": "CUDA-graph replay per step" if W.graph else "direct launches",

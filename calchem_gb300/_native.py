@@ -36,6 +36,7 @@ SIGNATURES = {
     "calchem_xc_prepare_shells": (_I, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "calchem_xc_overlap": (_I, [_P, _I, _P, _P, _I, _P]),
     "calchem_xc_grid_build": (_I, [_I, _P, _P, _I, _I, _U64, _P]),
+    "calchem_xc_grid_build_atoms": (_I, [_I, _P, _P, _P, _P, _P, _U64, _P]),
     "calchem_xc_grid_fetch": (_I, [_U64, _P, _P, _P]),
     "calchem_xc_grid_release": (_I, [_U64]),
     "calchem_xc_upload_points": (_I, [_P, _I, _P, _I, _P, _I, _P, _I, _I, _U64, _SZ]),
@@ -43,6 +44,7 @@ SIGNATURES = {
     "calchem_xc_set_weights": (_I, [_U64, _P, _I]),
     "calchem_xc_plan_stats": (_I, [_U64, _P, _P, _P, _P]),
     "calchem_xc_evaluate_rks": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
+    "calchem_xc_evaluate_rks_points": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
     "calchem_xc_evaluate_uks": (_I, [_U64, _I, _I, _P, _P, _P, _P, _P, _P]),
     "calchem_xc_evaluate_rks_device": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
     "calchem_xc_evaluate_uks_device": (_I, [_U64, _I, _I, _P, _P, _P, _P, _P, _P]),
@@ -56,6 +58,11 @@ SIGNATURES = {
     "calchem_xc_graph_capture": (_I, [_U64, _I, _I, _I, _P, _P, _P, _P, _P]),
     "calchem_xc_graph_launch": (_I, [_U64, _P]),
     "calchem_xc_last_status": (_I, [_U64]),
+    "calchem_mlp_shape": (_I, [_P, _P, _P, _P, _P]),
+    "calchem_mlp_forward": (_I, [_P, _P, _I, _P, _P]),
+    "calchem_mlp_loss_grad": (_I, [_P, _P, _P, _P, _I, ctypes.c_float, _P, _P, _P, _P, _P]),
+    "calchem_mlp_adam": (_I, [_P, _P, _P, _P, _I, _I, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                              ctypes.c_float, _P]),
     "calchem_xc_version": (ctypes.c_char_p, []),
 }
 

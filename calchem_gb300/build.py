@@ -25,6 +25,7 @@ CUDA_UNITS = {
     "vxc_mixed.cu": [],
     "grid_build.cu": ["-fmad=false"],
     "noalloc.cu": [],
+    "mlp.cu": [],
 }
 CXX_UNITS = {"host_prep.cpp": []}
 

@@ -77,11 +77,14 @@ struct Entry {
   bool profiling = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaGraphExec_t graph = nullptr;  // captured evaluation (calchem_xc_graph_capture_*)
+  double* d_pt_out = nullptr;       // per-point outputs (calchem_xc_evaluate_rks_points), 2 per point
+  std::vector<int> h_orig;          // caller's index of every uploaded point (empty: identity)
+  int n_orig = 0;                   // points the caller passed (calchem_xc_upload_points*)
 
   void free_all() {
     void* ptrs[] = {d_shells, d_prims, d_comps, d_prim_f, d_comp_f, d_shell_cf, d_pts,  d_batches, d_cand,  d_cand_loc, d_bao,   d_order,
                     d_P,      d_Pb,    d_V,     d_Vb,   d_rg,      d_red,   d_res,      d_counter, d_slab,
-                    d_mixed_ws, d_mixed_slab, d_mol_n, d_mol_off, d_mol_ao_off, d_mol_boff};
+                    d_mixed_ws, d_mixed_slab, d_mol_n, d_mol_off, d_mol_ao_off, d_mol_boff, d_pt_out};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (graph) cudaGraphExecDestroy(graph);
@@ -401,7 +404,8 @@ DevGrid dev_grid(const Entry& e) {
 
 // Enqueues one evaluation.  Pa/Pb/Va/Vb are device pointers; result gets (exc, n_a[, n_b]).
 int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, const double* Pb, double* Va,
-                 double* Vb, const double* wv, double* rho_out, double* result, cudaStream_t st) {
+                 double* Vb, const double* wv, double* rho_out, double* result, cudaStream_t st,
+                 double* point_out = nullptr) {
   const size_t nn = (size_t)e.nn_total;
   int launches = 0;
   if (mode != kModeRho) {
@@ -421,6 +425,7 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
   A.batch_red = e.d_red;
   A.counter = e.d_counter;
   A.max_m = e.max_m;
+  A.point_out = point_out;
   const DevGrid G = dev_grid(e);
   cudaError_t err;
   const bool prof = e.profiling && e.ev0 && e.ev1;
@@ -478,6 +483,93 @@ bool valid_prec(int p, int mode) {
 Entry* find(uint64_t id) {
   auto it = g_grids.find(id);
   return it == g_grids.end() ? nullptr : it->second;
+}
+
+}  // namespace
+
+namespace {
+// Expands the radial shells into points on the device, Becke weights, compaction (caller holds g_mu).
+int grid_build_impl(int n_atoms, const int* z, const double* xyz_bohr, const std::vector<RadialShell>& rs,
+                    long long n_raw, uint64_t grid_handle, int* n_pts_out) {
+  std::vector<double> inv_r, a_ij;
+  becke_tables(n_atoms, z, xyz_bohr, inv_r, a_ij);
+  const LebedevTables& T = lebedev_tables();
+  const int ns = (int)rs.size();
+  if (ns == 0) return -1;
+  std::vector<RadialShellDev> rsd(ns);
+  for (int i = 0; i < ns; ++i) rsd[i] = {rs[i].atom, rs[i].leb_offset, rs[i].n_ang, 0, rs[i].r, rs[i].w_rad,
+                                         rs[i].raw_start};
+  GridBuildArgs a{};
+  double *d_xyz = nullptr, *d_inv = nullptr, *d_aij = nullptr, *d_leb = nullptr, *d_raw = nullptr, *d_raww = nullptr;
+  RadialShellDev* d_rs = nullptr;
+  unsigned char* d_flags = nullptr;
+  int* d_counts = nullptr;
+  long long* d_off = nullptr;
+  auto cleanup = [&]() {
+    void* p[] = {d_xyz, d_inv, d_aij, d_leb, d_raw, d_raww, d_rs, d_flags, d_counts, d_off};
+    for (void* q : p)
+      if (q) cudaFree(q);
+  };
+  bool ok = dalloc(&d_xyz, 3 * (size_t)n_atoms) && dalloc(&d_inv, inv_r.size()) && dalloc(&d_aij, a_ij.size()) &&
+            dalloc(&d_leb, T.xyzw.size()) && dalloc(&d_rs, ns) && dalloc(&d_raw, 4 * (size_t)n_raw) &&
+            dalloc(&d_raww, (size_t)n_raw) && dalloc(&d_flags, (size_t)n_raw) && dalloc(&d_counts, ns) &&
+            dalloc(&d_off, (size_t)ns + 1);
+  if (!ok) {
+    cudaGetLastError();
+    cleanup();
+    return -4;
+  }
+  ok = cudaMemcpy(d_xyz, xyz_bohr, 3 * n_atoms * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(d_inv, inv_r.data(), inv_r.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(d_aij, a_ij.data(), a_ij.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(d_leb, T.xyzw.data(), T.xyzw.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(d_rs, rsd.data(), ns * sizeof(RadialShellDev), cudaMemcpyHostToDevice) == cudaSuccess;
+  a.n_atoms = n_atoms;
+  a.xyz = d_xyz;
+  a.inv_r = d_inv;
+  a.a_ij = d_aij;
+  a.lebedev = d_leb;
+  a.shells = d_rs;
+  a.raw = d_raw;
+  a.raw_w = d_raww;
+  a.flags = d_flags;
+  a.counts = d_counts;
+  ok = ok && launch_grid_expand(a, ns, 0) == cudaSuccess && launch_grid_scan(d_counts, ns, d_off, 0) == cudaSuccess;
+  long long n_keep = 0;
+  ok = ok && cudaMemcpy(&n_keep, d_off + ns, sizeof(long long), cudaMemcpyDeviceToHost) == cudaSuccess;
+  if (!ok || n_keep > 0x7fffffffLL) {
+    cudaGetLastError();
+    cleanup();
+    return ok ? -2 : -5;
+  }
+  Built* b = new Built;
+  b->n = (int)n_keep;
+  if (!(dalloc(&b->d_xyzw, 4 * (size_t)n_keep) && dalloc(&b->d_raw_w, (size_t)n_keep) &&
+        dalloc(&b->d_host, (size_t)n_keep))) {
+    cudaGetLastError();
+    if (b->d_xyzw) cudaFree(b->d_xyzw);
+    if (b->d_raw_w) cudaFree(b->d_raw_w);
+    if (b->d_host) cudaFree(b->d_host);
+    delete b;
+    cleanup();
+    return -4;
+  }
+  a.out_xyzw = b->d_xyzw;
+  a.out_raw_w = b->d_raw_w;
+  a.out_host = b->d_host;
+  ok = launch_grid_compact(a, d_off, ns, 0) == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+  cleanup();
+  if (!ok) {
+    cudaGetLastError();
+    cudaFree(b->d_xyzw);
+    cudaFree(b->d_raw_w);
+    cudaFree(b->d_host);
+    delete b;
+    return -5;
+  }
+  g_built[grid_handle] = b;
+  *n_pts_out = b->n;
+  return 0;
 }
 
 }  // namespace
@@ -588,84 +680,27 @@ int calchem_xc_grid_build(int n_atoms, const int* z, const double* xyz_bohr, int
   std::vector<RadialShell> rs;
   long long n_raw = 0;
   radial_shells(n_atoms, z, level, radial_min, rs, &n_raw);
-  std::vector<double> inv_r, a_ij;
-  becke_tables(n_atoms, z, xyz_bohr, inv_r, a_ij);
-  const LebedevTables& T = lebedev_tables();
-  const int ns = (int)rs.size();
-  std::vector<RadialShellDev> rsd(ns);
-  for (int i = 0; i < ns; ++i) rsd[i] = {rs[i].atom, rs[i].leb_offset, rs[i].n_ang, 0, rs[i].r, rs[i].w_rad,
-                                         rs[i].raw_start};
-  GridBuildArgs a{};
-  double *d_xyz = nullptr, *d_inv = nullptr, *d_aij = nullptr, *d_leb = nullptr, *d_raw = nullptr, *d_raww = nullptr;
-  RadialShellDev* d_rs = nullptr;
-  unsigned char* d_flags = nullptr;
-  int* d_counts = nullptr;
-  long long* d_off = nullptr;
-  auto cleanup = [&]() {
-    void* p[] = {d_xyz, d_inv, d_aij, d_leb, d_raw, d_raww, d_rs, d_flags, d_counts, d_off};
-    for (void* q : p)
-      if (q) cudaFree(q);
-  };
-  bool ok = dalloc(&d_xyz, 3 * (size_t)n_atoms) && dalloc(&d_inv, inv_r.size()) && dalloc(&d_aij, a_ij.size()) &&
-            dalloc(&d_leb, T.xyzw.size()) && dalloc(&d_rs, ns) && dalloc(&d_raw, 4 * (size_t)n_raw) &&
-            dalloc(&d_raww, (size_t)n_raw) && dalloc(&d_flags, (size_t)n_raw) && dalloc(&d_counts, ns) &&
-            dalloc(&d_off, (size_t)ns + 1);
-  if (!ok) {
-    cudaGetLastError();
-    cleanup();
-    return -4;
+  return grid_build_impl(n_atoms, z, xyz_bohr, rs, n_raw, grid_handle, n_pts_out);
+}
+
+int calchem_xc_grid_build_atoms(int n_atoms, const int* z, const double* xyz_bohr, const int* n_rad,
+                                const int* region_leb, const double* x_max, uint64_t grid_handle, int* n_pts_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (n_atoms <= 0 || !z || !xyz_bohr || !n_rad || !region_leb || !x_max || grid_handle == 0 || !n_pts_out)
+    return -1;
+  for (int a = 0; a < n_atoms; ++a) {
+    if (z[a] < 1 || z[a] > 86 || !std::isfinite(xyz_bohr[3 * a]) || !std::isfinite(xyz_bohr[3 * a + 1]) ||
+        !std::isfinite(xyz_bohr[3 * a + 2]) || n_rad[a] > 4096 || !(x_max[a] == x_max[a]))
+      return -1;
+    for (int k = 0; k < 5; ++k)
+      if (region_leb[5 * a + k] > 0 && lebedev_index(region_leb[5 * a + k]) < 0) return -1;
   }
-  ok = cudaMemcpy(d_xyz, xyz_bohr, 3 * n_atoms * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
-       cudaMemcpy(d_inv, inv_r.data(), inv_r.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
-       cudaMemcpy(d_aij, a_ij.data(), a_ij.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
-       cudaMemcpy(d_leb, T.xyzw.data(), T.xyzw.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
-       cudaMemcpy(d_rs, rsd.data(), ns * sizeof(RadialShellDev), cudaMemcpyHostToDevice) == cudaSuccess;
-  a.n_atoms = n_atoms;
-  a.xyz = d_xyz;
-  a.inv_r = d_inv;
-  a.a_ij = d_aij;
-  a.lebedev = d_leb;
-  a.shells = d_rs;
-  a.raw = d_raw;
-  a.raw_w = d_raww;
-  a.flags = d_flags;
-  a.counts = d_counts;
-  ok = ok && launch_grid_expand(a, ns, 0) == cudaSuccess && launch_grid_scan(d_counts, ns, d_off, 0) == cudaSuccess;
-  long long n_keep = 0;
-  ok = ok && cudaMemcpy(&n_keep, d_off + ns, sizeof(long long), cudaMemcpyDeviceToHost) == cudaSuccess;
-  if (!ok || n_keep > 0x7fffffffLL) {
-    cudaGetLastError();
-    cleanup();
-    return ok ? -2 : -5;
-  }
-  Built* b = new Built;
-  b->n = (int)n_keep;
-  if (!(dalloc(&b->d_xyzw, 4 * (size_t)n_keep) && dalloc(&b->d_raw_w, (size_t)n_keep) &&
-        dalloc(&b->d_host, (size_t)n_keep))) {
-    cudaGetLastError();
-    if (b->d_xyzw) cudaFree(b->d_xyzw);
-    if (b->d_raw_w) cudaFree(b->d_raw_w);
-    if (b->d_host) cudaFree(b->d_host);
-    delete b;
-    cleanup();
-    return -4;
-  }
-  a.out_xyzw = b->d_xyzw;
-  a.out_raw_w = b->d_raw_w;
-  a.out_host = b->d_host;
-  ok = launch_grid_compact(a, d_off, ns, 0) == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
-  cleanup();
-  if (!ok) {
-    cudaGetLastError();
-    cudaFree(b->d_xyzw);
-    cudaFree(b->d_raw_w);
-    cudaFree(b->d_host);
-    delete b;
-    return -5;
-  }
-  g_built[grid_handle] = b;
-  *n_pts_out = b->n;
-  return 0;
+  if (!device_ok()) return -3;
+  if (g_built.count(grid_handle)) return -2;
+  std::vector<RadialShell> rs;
+  long long n_raw = 0;
+  radial_shells_atoms(n_atoms, z, n_rad, region_leb, x_max, rs, &n_raw);
+  return grid_build_impl(n_atoms, z, xyz_bohr, rs, n_raw, grid_handle, n_pts_out);
 }
 
 int calchem_xc_grid_fetch(uint64_t grid_handle, double* xyzw, double* raw_w, int* host_atom) {
@@ -709,9 +744,16 @@ int calchem_xc_upload_points_ex(const AoShellGpu* h_shells, int n_shells, const 
   Plan plan;
   plan_batches(h_shells, n_shells, h_xyzw, n_pts, plan, batch_pts);
   if (plan.pts.empty()) return -1;
-  return upload_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, plan.pts.data(), (int)plan.pts.size(),
-                     plan.cand_offsets.data(), (int)plan.cand_offsets.size(), plan.cand_shells.data(),
-                     (int)plan.cand_shells.size(), n_ao, grid_id, memory_limit_bytes, plan.weights.data(), false);
+  const int rc = upload_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, plan.pts.data(),
+                             (int)plan.pts.size(), plan.cand_offsets.data(), (int)plan.cand_offsets.size(),
+                             plan.cand_shells.data(), (int)plan.cand_shells.size(), n_ao, grid_id, memory_limit_bytes,
+                             plan.weights.data(), false);
+  if (rc == 0) {
+    Entry* e = find(grid_id);
+    e->h_orig = std::move(plan.orig);
+    e->n_orig = n_pts;
+  }
+  return rc;
 }
 
 int calchem_xc_upload_points(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
@@ -772,6 +814,56 @@ int calchem_xc_evaluate_rks(uint64_t grid_id, int xc_code, int precision, const 
     return -5;
   if (*h_status != 0) return -7;
   std::memcpy(h_v_out, e->h_stage, nn * sizeof(double));
+  for (int i = 0; i < M; ++i) {
+    exc_out[i] = h_res[2 * i];
+    nelec_out[i] = h_res[2 * i + 1];
+  }
+  return 0;
+}
+
+int calchem_xc_evaluate_rks_points(uint64_t grid_id, int xc_code, int precision, const double* h_d_total,
+                                   double* exc_out, double* nelec_out, double* h_point_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_d_total || !exc_out || !nelec_out || !h_point_out || !valid_xc(xc_code)) return -1;
+  if (!valid_prec(precision, kModeRks)) return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e || e->n_mols != 1) return -2;
+  if (!e->has_w) return -1;
+  if (int rc0 = ensure_ws(*e)) return rc0;
+  const size_t np2 = 2 * (size_t)e->n_pts;
+  if (!e->d_pt_out && !dalloc(&e->d_pt_out, np2)) {
+    cudaGetLastError();
+    return -4;
+  }
+  const size_t nn = (size_t)e->nn_total;
+  const int M = e->n_mols;
+  std::memcpy(e->h_stage, h_d_total, nn * sizeof(double));
+  if (cudaMemsetAsync(e->d_pt_out, 0, np2 * sizeof(double), e->stream) != cudaSuccess ||
+      cudaMemcpyAsync(e->d_P, e->h_stage, nn * sizeof(double), cudaMemcpyHostToDevice, e->stream) != cudaSuccess)
+    return -5;
+  int rc = enqueue_eval(*e, kModeRks, xc_code, precision, e->d_P, nullptr, e->d_V, nullptr, nullptr, nullptr,
+                        e->d_res, e->stream, e->d_pt_out);
+  if (rc) return rc;
+  double* h_res = e->h_stage + 2 * nn;
+  int* h_status = reinterpret_cast<int*>(h_res + 3 * (size_t)M + 1);
+  if (cudaMemcpyAsync(h_res, e->d_res, 2 * (size_t)M * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(h_status, e->d_counter + 2, sizeof(int), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
+      cudaStreamSynchronize(e->stream) != cudaSuccess)
+    return -5;
+  if (*h_status != 0) return -7;
+  if (e->h_orig.empty()) {
+    if (cudaMemcpy(h_point_out, e->d_pt_out, np2 * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) return -5;
+  } else {  // back to the caller's point order; points the plan dropped (no AO reaches them) get 0
+    std::vector<double> tmp(np2);
+    if (cudaMemcpy(tmp.data(), e->d_pt_out, np2 * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) return -5;
+    std::memset(h_point_out, 0, 2 * (size_t)e->n_orig * sizeof(double));
+    for (size_t k = 0; k < e->h_orig.size(); ++k) {
+      h_point_out[2 * (size_t)e->h_orig[k]] = tmp[2 * k];
+      h_point_out[2 * (size_t)e->h_orig[k] + 1] = tmp[2 * k + 1];
+    }
+  }
   for (int i = 0; i < M; ++i) {
     exc_out[i] = h_res[2 * i];
     nelec_out[i] = h_res[2 * i + 1];

@@ -79,6 +79,10 @@ struct EvalArgs {
   double* slab;       // per-CTA scratch
   size_t slab_stride; // doubles per CTA
   int max_m;
+  // Optional per-point output of the fused RKS modes (nullptr: none): point_out[2 g] = w_g f_g and
+  // point_out[2 g + 1] = w_g (v_rho rho + v_gamma |grad rho|^2), the point's share of Exc and of
+  // tr(D Vxc).  Points below the density floor are not written (the caller zeroes the buffer).
+  double* point_out;
 };
 
 }  // namespace cxc

@@ -383,6 +383,37 @@ void radial_shells(int n_atoms, const int* z, int level, int radial_min, std::ve
   *n_raw = raw;
 }
 
+void radial_shells_atoms(int n_atoms, const int* z, const int* n_rad, const int* region_leb, const double* x_max,
+                         std::vector<RadialShell>& out, long long* n_raw) {
+  static const int kFineRegion[5] = {50, 110, 194, 302, 194};
+  out.clear();
+  const LebedevTables& T = lebedev_tables();
+  long long raw = 0;
+  for (int a = 0; a < n_atoms; ++a) {
+    const double rbs = bragg_slater_bohr(z[a]);
+    const int nr = n_rad[a] > 0 ? n_rad[a] : std::max(radial_count(z[a], 2), 99);
+    const double m = (double)(nr + 1);
+    for (int i = 1; i <= nr; ++i) {
+      const double t = (double)i, mt = m - t;
+      RadialShell rs;
+      rs.atom = a;
+      rs.r = rbs * (t * t) / (mt * mt);
+      rs.w_rad = 2.0 * ipow(rbs, 3) * m * ipow(t, 5) / ipow(mt, 7);
+      const double x = rs.r / std::max(rbs, 0.3);
+      if (x_max[a] > 0.0 && x > x_max[a]) continue;
+      const int k = x < 0.18 ? 0 : x < 0.50 ? 1 : x < 0.95 ? 2 : x < 5.00 ? 3 : 4;
+      const int want = region_leb[5 * a + k] > 0 ? region_leb[5 * a + k] : kFineRegion[k];
+      const int li = lebedev_index(want);
+      rs.leb_offset = T.offset[li];
+      rs.n_ang = T.count[li];
+      rs.raw_start = raw;
+      raw += rs.n_ang;
+      out.push_back(rs);
+    }
+  }
+  *n_raw = raw;
+}
+
 void becke_tables(int n, const int* z, const double* xyz, std::vector<double>& inv_r, std::vector<double>& a_ij) {
   inv_r.assign((size_t)n * n, 0.0);
   a_ij.assign((size_t)n * n, 0.0);
@@ -442,6 +473,7 @@ int plan_batches(const AoShellGpu* shells, int n_shells, const double* xyzw, int
       gp.host_atom = 0;
       plan.pts.push_back(gp);
       plan.weights.push_back(p[3]);
+      plan.orig.push_back(g);
     }
   }
   if (plan.cand_offsets.empty()) plan.cand_offsets.push_back(0);

@@ -40,6 +40,12 @@ struct RadialShell {
 };
 void radial_shells(int n_atoms, const int* z, int level, int radial_min, std::vector<RadialShell>& out,
                    long long* n_raw);
+// Per-atom grids: atom a gets n_rad[a] Euler-Maclaurin shells (<= 0: the Fine count); a shell at
+// x = r / max(R_BS, 0.3) takes region_leb[5 a + k] Lebedev points in the Fine level's pruning region
+// k (x < 0.18, 0.5, 0.95, 5, beyond; <= 0: the Fine choice 50 / 110 / 194 / 302 / 194), and shells
+// with x > x_max[a] are left out (x_max[a] <= 0: none).
+void radial_shells_atoms(int n_atoms, const int* z, const int* n_rad, const int* region_leb, const double* x_max,
+                         std::vector<RadialShell>& out, long long* n_raw);
 void becke_tables(int n, const int* z, const double* xyz, std::vector<double>& inv_r, std::vector<double>& a_ij);
 
 // Reference-layout batch plan (what RksVxcEngine::new_with_gpu uploads, vxc.rs:497-545).
@@ -48,6 +54,7 @@ struct Plan {
   std::vector<double> weights;
   std::vector<int> cand_offsets;
   std::vector<int> cand_shells;
+  std::vector<int> orig;  // index of every kept point in the caller's point array
 };
 // Chunks of batch_pts consecutive points (kPlanBatch = 128 in the reference, vxc.rs:96).
 int plan_batches(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan,

@@ -321,6 +321,10 @@ __global__ void __launch_bounds__(kThreads, 1) vxc_fp64_kernel(DevGrid G, EvalAr
             S.coef[1][g] = us * gax;
             S.coef[2][g] = us * gay;
             S.coef[3][g] = us * gaz;
+            if (A.point_out) {
+              A.point_out[2 * pt] = e_loc;
+              A.point_out[2 * pt + 1] = w * o.vra * ra + us * (gax * gax + gay * gay + gaz * gaz);
+            }
           }
         } else {
           const double rb0 = S.dens[0][0][g];

@@ -481,6 +481,10 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
           coef[1][g] = (float)(us * gax);
           coef[2][g] = (float)(us * gay);
           coef[3][g] = (float)(us * gaz);
+          if (A.point_out) {
+            A.point_out[2 * pt] = e_loc;
+            A.point_out[2 * pt + 1] = w * o.vr * ra + us * (gax * gax + gay * gay + gaz * gaz);
+          }
         }
       } else {
         const double rb0 = spin_rho[1][0];

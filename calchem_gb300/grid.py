@@ -89,6 +89,36 @@ class MolecularGrid:
         return cls(xyzw, raw, host, level)
 
     @classmethod
+    def build_atoms(cls, mol: Molecule, n_rad, region_leb, x_max) -> "MolecularGrid":
+        """Per-atom grid (calchem_xc_grid_build_atoms): atom a gets n_rad[a] radial shells,
+        region_leb[a][k] Lebedev points in the Fine pruning region k and no shells beyond
+        x = r / R_BS > x_max[a] (zeros: the Fine choices)."""
+        lib = _native.load()
+        z = np.ascontiguousarray(mol.z, dtype=np.int32)
+        xyz = np.ascontiguousarray(mol.coords_bohr)
+        nr = np.ascontiguousarray(n_rad, dtype=np.int32)
+        leb = np.ascontiguousarray(region_leb, dtype=np.int32).reshape(-1, 5)
+        xm = np.ascontiguousarray(x_max, dtype=np.float64)
+        if nr.shape != z.shape or leb.shape[0] != len(z) or xm.shape != z.shape:
+            raise ValueError("one radial count, five region rules and one cut-off per atom")
+        h = next(_handles)
+        n = np.zeros(1, dtype=np.int32)
+        _native.check("calchem_xc_grid_build_atoms",
+                      lib.calchem_xc_grid_build_atoms(len(z), _native.ptr(z), _native.ptr(xyz), _native.ptr(nr),
+                                                      _native.ptr(leb), _native.ptr(xm), h, _native.ptr(n)))
+        try:
+            npts = int(n[0])
+            xyzw = np.zeros((npts, 4), dtype=np.float64)
+            raw = np.zeros(npts, dtype=np.float64)
+            host = np.zeros(npts, dtype=np.int32)
+            if npts:
+                _native.check("calchem_xc_grid_fetch",
+                              lib.calchem_xc_grid_fetch(h, _native.ptr(xyzw), _native.ptr(raw), _native.ptr(host)))
+        finally:
+            lib.calchem_xc_grid_release(h)
+        return cls(xyzw, raw, host, GridLevel.FINE)
+
+    @classmethod
     def build_for_basis(cls, mol: Molecule, basis, level: GridLevel) -> "MolecularGrid":
         """MolecularGrid::build_for_basis (grid.rs:623-634), materialised."""
         return cls.build(mol, level, cls.radial_min_for_basis(basis))

@@ -129,6 +129,14 @@ int calchem_xc_overlap(const AoShellGpu* shells, int n_shells, const AoPrimGpu* 
  * the device under grid_handle until calchem_xc_grid_release. */
 int calchem_xc_grid_build(int n_atoms, const int* z, const double* xyz_bohr, int level, int radial_min,
                           uint64_t grid_handle, int* n_pts_out);
+/* Per-atom variant (no counterpart in the reference; the learned grid pruner's grids): atom a gets
+ * n_rad[a] radial shells (<= 0: the Fine count); a shell at x = r / max(R_BS, 0.3 Bohr) takes
+ * region_leb[5 a + k] Lebedev points in the Fine level's pruning region k (x < 0.18, 0.5, 0.95, 5,
+ * beyond; each one of 26, 50, 110, 194, 302, 590, or <= 0 for the Fine choice 50 / 110 / 194 / 302 /
+ * 194), and shells with x > x_max[a] are left out (x_max[a] <= 0: none).  All zeros reproduce
+ * calchem_xc_grid_build(level = Fine). */
+int calchem_xc_grid_build_atoms(int n_atoms, const int* z, const double* xyz_bohr, const int* n_rad,
+                                const int* region_leb, const double* x_max, uint64_t grid_handle, int* n_pts_out);
 /* Copies a built grid to the host: xyzw[4*g] = (x, y, z, weight); raw_w and host_atom may be NULL. */
 int calchem_xc_grid_fetch(uint64_t grid_handle, double* xyzw, double* raw_w, int* host_atom);
 int calchem_xc_grid_release(uint64_t grid_handle);
@@ -169,6 +177,14 @@ int calchem_xc_plan_stats(uint64_t grid_id, int* n_batches, double* sum_m2n, dou
  * member. */
 int calchem_xc_evaluate_rks(uint64_t grid_id, int xc_code, int precision, const double* h_d_total,
                             double* exc_out, double* nelec_out, double* h_v_out);
+
+/* Closed shell with per-point shares instead of V (no counterpart in the reference; used to measure
+ * per-atom quadrature errors): point_out[2 g] = w_g f_g (summing to Exc) and point_out[2 g + 1] =
+ * w_g (v_rho rho_g + v_gamma |grad rho_g|^2) (summing to tr(D Vxc)), for every point the caller
+ * uploaded, in its order (2 x n_pts values); points below the density floor, and points no AO
+ * reaches, get 0.  Single grids only (-2 for a group). */
+int calchem_xc_evaluate_rks_points(uint64_t grid_id, int xc_code, int precision, const double* h_d_total,
+                                   double* exc_out, double* nelec_out, double* h_point_out);
 
 /* Open shell (UksVxcEngine::evaluate, vxc.rs:1662-1669).  nelec_out[0..1] = (N_alpha, N_beta);
  * on a group, exc_out[i] and nelec_out[2 i .. 2 i + 1] for member i. */
@@ -221,6 +237,27 @@ int calchem_xc_last_launch_count(uint64_t grid_id);
  * returns that kernel's duration in milliseconds. */
 int calchem_xc_set_profiling(uint64_t grid_id, int enable);
 int calchem_xc_last_kernel_ms(uint64_t grid_id, float* ms_out);
+
+/* ======================================================================================
+ * (5) The learned grid pruner's network (no counterpart in the reference).  A fixed MLP
+ * (16 inputs, two tanh layers of 64, 16 linear outputs; parameters one float buffer
+ * W1 [16][64], b1, W2 [64][64], b2, W3 [64][16], b3) maps an atom's environment features to the
+ * predicted log10 quadrature error of each candidate grid level.  All pointers are device
+ * pointers; work is enqueued on `stream` (a cudaStream_t) and not synchronised.
+ * ====================================================================================== */
+
+int calchem_mlp_shape(int* n_in, int* n_hidden, int* n_out, int* n_params, int* work_per_sample);
+/* y [n][16] = network(x [n][16]). */
+int calchem_mlp_forward(const float* d_params, const float* d_x, int n, float* d_y, void* stream);
+/* Masked mean squared error L = inv_count * sum mask (y - t)^2 over t, mask [n][16]:
+ * d_grad [n_params] = dL/dparams (summed over samples in a fixed order), *d_loss = L;
+ * d_work [n][work_per_sample] and d_loss_part [n] are scratch. */
+int calchem_mlp_loss_grad(const float* d_params, const float* d_x, const float* d_t, const float* d_mask, int n,
+                          float inv_count, float* d_work, float* d_loss_part, float* d_grad, float* d_loss,
+                          void* stream);
+/* One Adam update (bias-corrected, step >= 1) of d_params with moment buffers d_m, d_v. */
+int calchem_mlp_adam(float* d_params, const float* d_grad, float* d_m, float* d_v, int n_params, int step, float lr,
+                     float beta1, float beta2, float eps, void* stream);
 
 /* ======================================================================================
  * (4) Evaluation without device allocation.  No counterpart in the reference: it exists for

@@ -1,0 +1,78 @@
+"""GPU tests of the learned grid pruner: per-atom grids, per-atom quadrature shares, and the pruned
+grid against the Fine grid as judge."""
+
+import os
+
+import numpy as np
+import pytest
+
+from calchem_gb300 import BasisSet, GridLevel, MolecularGrid, RksVxcEngine, pruner, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lib(native_lib):
+    assert native_lib.calchem_cuda_is_available() == 1, "no sm_103a device"
+    return native_lib
+
+
+def test_all_fine_levels_reproduce_the_fine_grid(lib):
+    mol = workloads.water_cluster(3, 4)
+    g0 = MolecularGrid.build(mol, GridLevel.FINE)
+    g1 = pruner.grid_for_levels(mol, [pruner.FINE] * len(mol.atoms))
+    assert len(g0) == len(g1)
+    assert np.array_equal(g0.xyzw, g1.xyzw) and np.array_equal(g0.host_atom, g1.host_atom)
+
+
+def test_level_grids_shrink_and_per_atom_levels_mix(lib):
+    mol = workloads.water_cluster(2, 9)
+    sizes = [len(pruner.grid_for_levels(mol, [l] * len(mol.atoms))) for l in range(len(pruner.LEVELS))]
+    assert sizes[0] < sizes[-1] and sizes == sorted(sizes)
+    mixed = [0, pruner.FINE] * (len(mol.atoms) // 2) + [3] * (len(mol.atoms) % 2)
+    g = pruner.grid_for_levels(mol, mixed)
+    per_atom = np.bincount(g.host_atom, minlength=len(mol.atoms))
+    fine = np.bincount(pruner.grid_for_levels(mol, [pruner.FINE] * len(mol.atoms)).host_atom)
+    assert np.all(per_atom[np.array(mixed) == pruner.FINE] == fine[np.array(mixed) == pruner.FINE])
+
+
+def test_atom_shares_sum_to_the_engine_results(lib):
+    mol = workloads.water_cluster(2, 3)
+    basis = BasisSet.from_name("6-31g(d)", mol)
+    grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
+    D = workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, 4)
+    E, T = pruner.atom_shares(mol, basis, grid, "b3lyp", D)
+    eng = RksVxcEngine(basis, grid)
+    exc, V = eng.evaluate(basis, grid, "b3lyp", D)
+    assert abs(E.sum() - exc) < 1e-10
+    assert abs(T.sum() - np.sum(D * V)) < 1e-9
+    eng.close()
+
+
+def test_level_errors_shrink_towards_fine(lib):
+    mol = workloads.water_cluster(2, 3)
+    basis = BasisSet.from_name("6-31g(d)", mol)
+    D = workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, 4)
+    err = pruner.level_errors(mol, basis, "pbe", D)
+    assert np.all(err[:, pruner.FINE] == 0)
+    assert np.all(np.isfinite(err))
+    assert np.median(err[:, 0]) > np.median(err[:, pruner.FINE - 1])
+
+
+@pytest.mark.skipif(not os.path.exists(pruner.MODEL_PATH), reason="no trained pruner model")
+def test_learned_grid_meets_tolerance_with_fewer_points(lib):
+    """Held-out geometry: the network prunes, the Fine-grid judge reverts what exceeds the per-atom
+    tolerance, and the pruned grid then meets the per-molecule tolerance with fewer points."""
+    mol = workloads.water_cluster(10, 4242)
+    basis = BasisSet.from_name("6-31g(d)", mol)
+    D = workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, 11)
+    tol = 5e-7
+    lg = pruner.LearnedGrid(mol, basis, tol=tol)
+    bad, err = lg.check(D, "b3lyp")
+    fine = lg.fine_grid
+    assert len(lg.grid) < len(fine)
+    E0, T0 = pruner.atom_shares(mol, basis, fine, "b3lyp", D)
+    E1, T1 = pruner.atom_shares(mol, basis, lg.grid, "b3lyp", D)
+    assert np.all(np.abs(E1 - E0) <= lg.tol_atom * (1 + 1e-9))
+    assert abs(E1.sum() - E0.sum()) <= tol
+    assert abs(T1.sum() - T0.sum()) <= tol
