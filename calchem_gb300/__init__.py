@@ -10,12 +10,12 @@ from .basis import BasisSet
 from .grid import GridLevel, MolecularGrid
 from .molecule import ANGSTROM_TO_BOHR, Atom, Molecule
 from . import autotune
-from .vxc import (FP64, MIXED, GpuVxcGrid, RksVxcEngine, UksVxcEngine, VxcGroup, evaluate_vxc_rks,
+from .vxc import (FP64, MIXED, FxcKernel, GpuVxcGrid, RksVxcEngine, UksVxcEngine, VxcGroup, evaluate_vxc_rks,
                   evaluate_vxc_uks, is_cuda_available)
 from .xc import XcFunctional
 
 __all__ = [
     "ANGSTROM_TO_BOHR", "Atom", "Molecule", "BasisSet", "GridLevel", "MolecularGrid", "XcFunctional",
-    "RksVxcEngine", "UksVxcEngine", "VxcGroup", "GpuVxcGrid", "evaluate_vxc_rks", "evaluate_vxc_uks", "is_cuda_available",
+    "RksVxcEngine", "UksVxcEngine", "VxcGroup", "FxcKernel", "GpuVxcGrid", "evaluate_vxc_rks", "evaluate_vxc_uks", "is_cuda_available",
     "FP64", "MIXED",
 ]

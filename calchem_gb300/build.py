@@ -26,6 +26,7 @@ CUDA_UNITS = {
     "grid_build.cu": ["-fmad=false"],
     "noalloc.cu": [],
     "mlp.cu": [],
+    "fxc.cu": [],
 }
 CXX_UNITS = {"host_prep.cpp": []}
 

@@ -78,13 +78,19 @@ struct Entry {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaGraphExec_t graph = nullptr;  // captured evaluation (calchem_xc_graph_capture_*)
   double* d_pt_out = nullptr;       // per-point outputs (calchem_xc_evaluate_rks_points), 2 per point
+  double* d_fxc = nullptr;          // TD-DFT kernel coefficients, 11 per point (calchem_xc_fxc_prepare)
+  int fxc_code = -1;                // functional of d_fxc (-1: not prepared)
+  double* d_fxc_m = nullptr;        // trial matrices / results of host-buffer contractions
+  double* d_fxc_v = nullptr;
+  int fxc_cap = 0;                  // trial matrices d_fxc_m and d_fxc_v hold
   std::vector<int> h_orig;          // caller's index of every uploaded point (empty: identity)
   int n_orig = 0;                   // points the caller passed (calchem_xc_upload_points*)
 
   void free_all() {
     void* ptrs[] = {d_shells, d_prims, d_comps, d_prim_f, d_comp_f, d_shell_cf, d_pts,  d_batches, d_cand,  d_cand_loc, d_bao,   d_order,
                     d_P,      d_Pb,    d_V,     d_Vb,   d_rg,      d_red,   d_res,      d_counter, d_slab,
-                    d_mixed_ws, d_mixed_slab, d_mol_n, d_mol_off, d_mol_ao_off, d_mol_boff, d_pt_out};
+                    d_mixed_ws, d_mixed_slab, d_mol_n, d_mol_off, d_mol_ao_off, d_mol_boff, d_pt_out,
+                    d_fxc, d_fxc_m, d_fxc_v};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (graph) cudaGraphExecDestroy(graph);
@@ -471,6 +477,32 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
     }
   }
   e.last_launches = launches;
+  return 0;
+}
+
+// TD-DFT kernel contraction of n_trials symmetric matrices d_m (each n x n) into d_v.
+int enqueue_fxc(Entry& e, int triplet, const double* d_m, int n_trials, double* d_v, cudaStream_t st) {
+  const size_t nn = (size_t)e.n_ao * e.n_ao;
+  if (cudaMemsetAsync(d_v, 0, nn * n_trials * sizeof(double), st) != cudaSuccess ||
+      cudaMemsetAsync(e.d_counter, 0, 4 * sizeof(int), st) != cudaSuccess)
+    return -5;
+  EvalArgs A{};
+  A.mode = kModeFxc;
+  A.xc = e.fxc_code;
+  A.Pa = d_m;
+  A.Va = d_v;
+  A.n_trials = n_trials;
+  A.triplet = triplet ? 1 : 0;
+  A.fxc_coef = e.d_fxc;
+  A.batch_red = e.d_red;
+  A.counter = e.d_counter;
+  A.max_m = e.max_m;
+  A.slab = e.d_slab;
+  A.slab_stride = e.slab_stride;
+  if (launch_fp64(dev_grid(e), A, e.n_ctas, st) != cudaSuccess) return -5;
+  for (int t = 0; t < n_trials; ++t)
+    if (launch_mirror(d_v + t * nn, e.n_ao, 0, st) != cudaSuccess) return -5;
+  e.last_launches = 1 + n_trials;
   return 0;
 }
 
@@ -936,6 +968,75 @@ int calchem_xc_evaluate_uks_device(uint64_t grid_id, int xc_code, int precision,
   if (int rc0 = ensure_ws(*e)) return rc0;
   return enqueue_eval(*e, kModeUks, xc_code, precision, d_pa, d_pb, d_va, d_vb, nullptr, nullptr, d_result,
                       (cudaStream_t)stream);
+}
+
+int calchem_xc_fxc_prepare(uint64_t grid_id, int xc_code, const double* h_d_total) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_d_total || !valid_xc(xc_code)) return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e || e->n_mols != 1) return -2;
+  if (!e->has_w) return -1;
+  if (int rc0 = ensure_ws(*e)) return rc0;
+  if (!e->d_fxc && !dalloc(&e->d_fxc, 11 * (size_t)e->n_pts)) {
+    cudaGetLastError();
+    return -4;
+  }
+  const size_t nn = (size_t)e->n_ao * e->n_ao;
+  std::memcpy(e->h_stage, h_d_total, nn * sizeof(double));
+  if (cudaMemcpyAsync(e->d_P, e->h_stage, nn * sizeof(double), cudaMemcpyHostToDevice, e->stream) != cudaSuccess)
+    return -5;
+  int rc = enqueue_eval(*e, kModeRho, 0, CALCHEM_XC_FP64, e->d_P, nullptr, nullptr, nullptr, nullptr, e->d_rg,
+                        nullptr, e->stream);
+  if (rc) return rc;
+  if (launch_fxc_coef(e->d_rg, e->d_pts + 3 * (size_t)e->n_pts, e->n_pts, xc_code, e->d_fxc, e->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(e->stream) != cudaSuccess)
+    return -5;
+  e->fxc_code = xc_code;
+  return 0;
+}
+
+int calchem_xc_fxc_contract_device(uint64_t grid_id, int triplet, const double* d_m, int n_trials, double* d_v_out,
+                                   void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_m || !d_v_out || n_trials <= 0) return -1;
+  Entry* e = find(grid_id);
+  if (!e || e->n_mols != 1) return -2;
+  if (e->fxc_code < 0) return -1;
+  return enqueue_fxc(*e, triplet, d_m, n_trials, d_v_out, (cudaStream_t)stream);
+}
+
+int calchem_xc_fxc_contract(uint64_t grid_id, int triplet, const double* h_m, int n_trials, double* h_v_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_m || !h_v_out || n_trials <= 0) return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e || e->n_mols != 1) return -2;
+  if (e->fxc_code < 0) return -1;
+  const size_t nn = (size_t)e->n_ao * e->n_ao;
+  if (n_trials > e->fxc_cap) {
+    if (e->d_fxc_m) cudaFree(e->d_fxc_m);
+    if (e->d_fxc_v) cudaFree(e->d_fxc_v);
+    e->d_fxc_m = e->d_fxc_v = nullptr;
+    e->fxc_cap = 0;
+    if (!dalloc(&e->d_fxc_m, nn * n_trials) || !dalloc(&e->d_fxc_v, nn * n_trials)) {
+      cudaGetLastError();
+      return -4;
+    }
+    e->fxc_cap = n_trials;
+  }
+  int st = 0;
+  if (cudaMemcpyAsync(e->d_fxc_m, h_m, nn * n_trials * sizeof(double), cudaMemcpyHostToDevice, e->stream) !=
+      cudaSuccess)
+    return -5;
+  if (int rc = enqueue_fxc(*e, triplet, e->d_fxc_m, n_trials, e->d_fxc_v, e->stream)) return rc;
+  if (cudaMemcpyAsync(h_v_out, e->d_fxc_v, nn * n_trials * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(&st, e->d_counter + 2, sizeof(int), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
+      cudaStreamSynchronize(e->stream) != cudaSuccess)
+    return -5;
+  return st != 0 ? -7 : 0;
 }
 
 int calchem_xc_group_create(const uint64_t* member_ids, int n_members, uint64_t group_id, size_t memory_limit_bytes) {

@@ -28,7 +28,8 @@ enum Mode : int {
   kModeRho = 0,   // drop-in eval_rho: write rho and grad rho per point
   kModeAccum = 1, // drop-in accum: read (w v_rho / 2, w u) per point, add into V (lower triangle)
   kModeRks = 2,   // fused closed shell
-  kModeUks = 3    // fused open shell
+  kModeUks = 3,   // fused open shell
+  kModeFxc = 4    // TD-DFT kernel contraction: per trial matrix M_b, dV_b = f_xc[M_b] (fxc.rs:374-645)
 };
 
 struct DevGrid {
@@ -83,6 +84,11 @@ struct EvalArgs {
   // point_out[2 g + 1] = w_g (v_rho rho + v_gamma |grad rho|^2), the point's share of Exc and of
   // tr(D Vxc).  Points below the density floor are not written (the caller zeroes the buffer).
   double* point_out;
+  // kModeFxc: n_trials matrices at Pa + b n^2, results at Va + b n^2; per-point kernel coefficients
+  // fxc_coef[11 g ..] = (g_s x, y, z, singlet k_rr, k_rg, k_gg, u_iso, triplet k_rr, k_rg, k_gg, u_iso).
+  int n_trials;
+  int triplet;
+  const double* fxc_coef;
 };
 
 }  // namespace cxc

@@ -26,6 +26,9 @@ int mixed_max_m();
 cudaError_t launch_mixed(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st);
 cudaError_t launch_mixed_prepare(const double* P, int n_total, const int* mol_n, const long long* mol_off,
                                  const int* mol_ao_off, int n_mols, void* out, int* fexp, cudaStream_t st);
+// TD-DFT kernel coefficients per point (fxc.cu): rho_grad [n][4] of the total density -> out [n][11].
+cudaError_t launch_fxc_coef(const double* rho_grad, const double* w, int n_pts, int code, double* out,
+                            cudaStream_t st);
 // Dynamic shared-memory limits of the persistent kernels, set once per process (the launchers call
 // these; a graph capture calls them first so that no attribute is set while capturing).
 cudaError_t fp64_set_attributes();

@@ -278,6 +278,39 @@ __global__ void __launch_bounds__(kThreads, 1) vxc_fp64_kernel(DevGrid G, EvalAr
     const BatchDesc bd = G.batches[b];
     eval_batch_aos(G, bd, slab, m_pad);
     __syncthreads();
+    if (A.mode == kModeFxc) {
+      // The batch's AOs serve every trial matrix: response density eta = sum M phi phi and its
+      // gradient xi, the kernel-weighted coefficients, then dV_b += Z Phi^T + Phi Z^T.
+      const size_t nn = (size_t)G.n_ao * G.n_ao;
+      for (int t = 0; t < A.n_trials; ++t) {
+        batch_density(G, bd, A.Pa + t * nn, slab, m_pad, S);
+        if (tid < kBlockPts) {
+          const bool live = g < bd.n_pts;
+          const size_t pt = (size_t)bd.pt_start + g;
+          for (int k = 0; k < 4; ++k) S.coef[k][g] = 0.0;
+          if (live) {
+            const double* c = A.fxc_coef + 11 * pt;
+            const double* kc = c + (A.triplet ? 7 : 3);
+            const double w = G.pw[pt];
+            const double eta = S.dens[0][0][g];
+            const double xi[3] = {2.0 * S.dens[0][1][g], 2.0 * S.dens[0][2][g], 2.0 * S.dens[0][3][g]};
+            const double sigma = c[0] * xi[0] + c[1] * xi[1] + c[2] * xi[2];
+            const double dv = kc[0] * eta + kc[1] * sigma;
+            const double gc = kc[1] * eta + kc[2] * sigma;
+            S.coef[0][g] = 0.5 * w * dv;
+            S.coef[1][g] = w * (kc[3] * xi[0] + gc * c[0]);
+            S.coef[2][g] = w * (kc[3] * xi[1] + gc * c[1]);
+            S.coef[3][g] = w * (kc[3] * xi[2] + gc * c[2]);
+          }
+        }
+        __syncthreads();
+        build_z(bd, slab, m_pad, 4, S, 0);
+        __syncthreads();
+        accumulate_v(G, bd, slab, m_pad, 4, A.Va + t * nn, S);
+        __syncthreads();
+      }
+      continue;
+    }
 
     double e_loc = 0, na_loc = 0, nb_loc = 0;
     if (A.mode == kModeAccum) {

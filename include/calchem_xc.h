@@ -200,6 +200,19 @@ int calchem_xc_evaluate_rks_device(uint64_t grid_id, int xc_code, int precision,
 int calchem_xc_evaluate_uks_device(uint64_t grid_id, int xc_code, int precision, const double* d_pa,
                                    const double* d_pb, double* d_result, double* d_va, double* d_vb, void* stream);
 
+/* TD-DFT exchange-correlation kernel (FxcKernel, crates/calchem-dft/src/fxc.rs:176-647), batched over
+ * trial matrices.  calchem_xc_fxc_prepare (FxcKernel::new) evaluates the ground-state density
+ * d_total = P_total on the grid and stores 11 kernel coefficients per point (finite differences of
+ * the FP64 functional, as the reference); calchem_xc_fxc_contract (contract_batch) returns, for each
+ * of n_trials symmetric n x n matrices M_b packed one after the other in h_m, the full symmetric
+ * dV_b = f_xc[M_b] (singlet, or triplet when triplet != 0) in h_v_out.  The grid's AOs are evaluated
+ * once per batch for all trial matrices.  -1 when the kernel was not prepared; single grids only. */
+int calchem_xc_fxc_prepare(uint64_t grid_id, int xc_code, const double* h_d_total);
+int calchem_xc_fxc_contract(uint64_t grid_id, int triplet, const double* h_m, int n_trials, double* h_v_out);
+/* Device-pointer variant of the contraction (enqueued on `stream`, not synchronised). */
+int calchem_xc_fxc_contract_device(uint64_t grid_id, int triplet, const double* d_m, int n_trials, double* d_v_out,
+                                   void* stream);
+
 /* ======================================================================================
  * (3b) Many molecules in one launch, and CUDA-graph replay.  No counterpart in the reference.
  * ====================================================================================== */
