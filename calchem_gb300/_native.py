@@ -66,6 +66,9 @@ SIGNATURES = {
     "calchem_mlp_loss_grad": (_I, [_P, _P, _P, _P, _I, ctypes.c_float, _P, _P, _P, _P, _P]),
     "calchem_mlp_adam": (_I, [_P, _P, _P, _P, _I, _I, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                               ctypes.c_float, _P]),
+    "calchem_scf_boys": (_I, [_I, ctypes.c_double, _P]),
+    "calchem_scf_one_electron": (_I, [_P, _I, _P, _P, _I, _I, _P, _P, _P, _P, _P]),
+    "calchem_scf_eri": (_I, [_P, _I, _P, _P, _I, _P]),
     "calchem_xc_version": (ctypes.c_char_p, []),
 }
 

@@ -28,7 +28,7 @@ CUDA_UNITS = {
     "mlp.cu": [],
     "fxc.cu": [],
 }
-CXX_UNITS = {"host_prep.cpp": []}
+CXX_UNITS = {"host_prep.cpp": [], "integrals.cpp": []}
 
 
 def _nvcc() -> str:

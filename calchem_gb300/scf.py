@@ -1,0 +1,221 @@
+"""SCF harness around the GPU XC quadrature: restricted and unrestricted Kohn-Sham (and Hartree-Fock
+when no functional is given), mirroring the entry points of calchem-scf (``rks`` / ``uks``,
+crates/calchem-scf/src/rks.rs:255-300, uks.rs).
+
+Integrals come from the library's host code (McMurchie-Davidson, ``calchem_scf_one_electron`` /
+``calchem_scf_eri``) over the same shells the quadrature uses; J and K are contracted from the dense
+ERI tensor (small molecules).  Every iteration calls the GPU Vxc engine once.  Convergence is
+accelerated by DIIS on the orbital gradient F D S - S D F (Pulay).  With ``learned=True`` the grid
+is the MLP-pruned grid, checked against the Fine grid every ``judge_every`` iterations on the current
+density (atoms over tolerance revert to Fine, and the engine is rebuilt).
+"""
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native
+from .grid import GridLevel, MolecularGrid
+from .vxc import RksVxcEngine, UksVxcEngine
+from .xc import XcFunctional
+
+_EXACT_EXCHANGE = {XcFunctional.B3LYP: 0.20, XcFunctional.B3LYP5: 0.20, XcFunctional.PBE0: 0.25}
+
+
+def exact_exchange_fraction(func) -> float:
+    """exact_exchange_fraction (xc.rs:116-125); Hartree-Fock (func None) is 1."""
+    if func is None:
+        return 1.0
+    f = XcFunctional.from_name(func) if isinstance(func, str) else XcFunctional(func)
+    return _EXACT_EXCHANGE.get(f, 0.0)
+
+
+def nuclear_repulsion(mol) -> float:
+    z = np.asarray(mol.z, float)
+    x = np.asarray(mol.coords_bohr)
+    e = 0.0
+    for i in range(len(z)):
+        for j in range(i):
+            e += z[i] * z[j] / np.linalg.norm(x[i] - x[j])
+    return float(e)
+
+
+def core_matrices(basis, mol):
+    """(S, T, V) over the basis (calchem_scf_one_electron)."""
+    lib = _native.load()
+    sh, pr, co = basis.gpu_arrays()
+    n = basis.n_ao
+    S, T, V = (np.zeros((n, n)) for _ in range(3))
+    z = np.ascontiguousarray(mol.z, dtype=np.float64)
+    xyz = np.ascontiguousarray(mol.coords_bohr)
+    _native.check("calchem_scf_one_electron", lib.calchem_scf_one_electron(
+        _native.ptr(sh), len(sh), _native.ptr(pr), _native.ptr(co), n, len(z), _native.ptr(z), _native.ptr(xyz),
+        _native.ptr(S), _native.ptr(T), _native.ptr(V)))
+    return S, T, V
+
+
+def eri_tensor(basis) -> np.ndarray:
+    """Dense (pq|rs) tensor (calchem_scf_eri)."""
+    lib = _native.load()
+    sh, pr, co = basis.gpu_arrays()
+    n = basis.n_ao
+    eri = np.zeros((n, n, n, n))
+    _native.check("calchem_scf_eri", lib.calchem_scf_eri(_native.ptr(sh), len(sh), _native.ptr(pr), _native.ptr(co),
+                                                         n, _native.ptr(eri)))
+    return eri
+
+
+class _Diis:
+    def __init__(self, size=8):
+        self.size = size
+        self.F, self.E = [], []
+
+    def push(self, F, err):
+        self.F.append(F)
+        self.E.append(err)
+        if len(self.F) > self.size:
+            self.F.pop(0)
+            self.E.pop(0)
+
+    def extrapolate(self):
+        k = len(self.F)
+        if k < 2:
+            return self.F[-1]
+        B = -np.ones((k + 1, k + 1))
+        B[k, k] = 0.0
+        for i in range(k):
+            for j in range(k):
+                B[i, j] = sum(np.vdot(a, b) for a, b in zip(self.E[i], self.E[j]))
+        rhs = np.zeros(k + 1)
+        rhs[k] = -1.0
+        try:
+            c = np.linalg.solve(B, rhs)[:k]
+        except np.linalg.LinAlgError:
+            return self.F[-1]
+        return tuple(sum(ci * Fi[s] for ci, Fi in zip(c, self.F)) for s in range(len(self.F[-1])))
+
+
+@dataclass
+class ScfResult:
+    total_energy_hartree: float
+    converged: bool
+    iterations: int
+    mo_energies: np.ndarray
+    densities: tuple
+    exc: float = 0.0
+    nuclear_repulsion: float = 0.0
+    s_squared: float = 0.0          # <S^2> - S(S+1) (UKS spin contamination)
+    grid_points: int = 0
+    energies: list = field(default_factory=list)
+    reverted_atoms: list = field(default_factory=list)
+
+
+def _orthogonaliser(S):
+    w, U = np.linalg.eigh(S)
+    keep = w > 1e-8
+    return U[:, keep] / np.sqrt(w[keep])
+
+
+def _diag(F, X):
+    e, C = np.linalg.eigh(X.T @ F @ X)
+    return e, X @ C
+
+
+def _grid_and_engine(mol, basis, func, level, precision, learned, tol, spin):
+    if func is None:
+        return None, None, None
+    if learned:
+        from . import pruner
+        lg = pruner.LearnedGrid(mol, basis, tol=tol)
+        grid = lg.grid
+    else:
+        lg = None
+        grid = MolecularGrid.build_for_basis(mol, basis, level)
+    cls = RksVxcEngine if spin == "rks" else UksVxcEngine
+    return lg, grid, cls(basis, grid, precision=precision)
+
+
+def _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter, e_tol, g_tol, spin):
+    S, T, Vn = core_matrices(basis, mol)
+    H = T + Vn
+    eri = eri_tensor(basis)
+    X = _orthogonaliser(S)
+    ax = exact_exchange_fraction(func)
+    e_nuc = nuclear_repulsion(mol)
+    n_a, n_b = mol.n_alpha_beta()
+    lg, grid, eng = _grid_and_engine(mol, basis, func, level, precision, learned, tol, spin)
+    diis = _Diis()
+    e_orb, C = _diag(H, X)
+    Ca = Cb = C
+    Da = Ca[:, :n_a] @ Ca[:, :n_a].T
+    Db = Cb[:, :n_b] @ Cb[:, :n_b].T
+    energies, reverted = [], []
+    e_old = None
+    converged = False
+    exc = 0.0
+    it = 0
+    for it in range(1, max_iter + 1):
+        if lg is not None and judge_every and it % judge_every == 0:
+            bad, _ = lg.check(Da + Db, func) if spin == "rks" else lg.check(Da + Db, func)
+            if bad:
+                reverted.extend(bad)
+                eng.close()
+                grid = lg.grid
+                eng = (RksVxcEngine if spin == "rks" else UksVxcEngine)(basis, grid, precision=precision)
+        Dt = Da + Db
+        J = np.einsum("pqrs,rs->pq", eri, Dt, optimize=True)
+        Ka = np.einsum("prqs,rs->pq", eri, Da, optimize=True)
+        Kb = np.einsum("prqs,rs->pq", eri, Db, optimize=True)
+        if func is None:
+            exc, Va, Vb = 0.0, 0.0, 0.0
+        elif spin == "rks":
+            exc, Va = eng.evaluate(basis, grid, func, Dt)
+            Vb = Va
+        else:
+            exc, Va, Vb = eng.evaluate(basis, grid, func, Da, Db)
+        Fa = H + J - ax * Ka + Va
+        Fb = H + J - ax * Kb + Vb
+        e = (np.sum(Dt * H) + 0.5 * np.sum(Dt * J) - 0.5 * ax * (np.sum(Da * Ka) + np.sum(Db * Kb)) + exc + e_nuc)
+        energies.append(float(e))
+        errs = (X.T @ (Fa @ Da @ S - S @ Da @ Fa) @ X, X.T @ (Fb @ Db @ S - S @ Db @ Fb) @ X)
+        g = max(float(np.max(np.abs(errs[0]))), float(np.max(np.abs(errs[1]))))
+        if e_old is not None and abs(e - e_old) < e_tol and g < g_tol:
+            converged = True
+            break
+        e_old = e
+        diis.push((Fa, Fb), errs)
+        Fa_x, Fb_x = diis.extrapolate()
+        ea, Ca = _diag(Fa_x, X)
+        if spin == "rks":
+            eb, Cb = ea, Ca
+        else:
+            eb, Cb = _diag(Fb_x, X)
+        Da = Ca[:, :n_a] @ Ca[:, :n_a].T
+        Db = Cb[:, :n_b] @ Cb[:, :n_b].T
+        e_orb = ea
+    s2 = 0.0
+    if spin == "uks":
+        ov = Ca[:, :n_a].T @ S @ Cb[:, :n_b]
+        sz = 0.5 * (n_a - n_b)
+        s2 = float(sz * (sz + 1) + n_b - np.sum(ov * ov) - sz * (sz + 1))
+    if eng is not None:
+        eng.close()
+    dens = (Da + Db,) if spin == "rks" else (Da, Db)
+    return ScfResult(energies[-1], converged, it, e_orb, dens, float(exc), e_nuc, s2,
+                     0 if grid is None else len(grid), energies, reverted)
+
+
+def rks(mol, basis, func="b3lyp", level=GridLevel.FINE, precision="fp64", learned=False, tol=5e-7, judge_every=5,
+        max_iter=128, e_tol=1e-10, g_tol=1e-7):
+    """Restricted Kohn-Sham (restricted Hartree-Fock for func=None) to tight convergence."""
+    return _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter, e_tol, g_tol, "rks")
+
+
+def uks(mol, basis, func="b3lyp", level=GridLevel.FINE, precision="fp64", learned=False, tol=5e-7, judge_every=5,
+        max_iter=128, e_tol=1e-10, g_tol=1e-7):
+    """Unrestricted Kohn-Sham (unrestricted Hartree-Fock for func=None)."""
+    return _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter, e_tol, g_tol, "uks")
+
+
+def rhf(mol, basis, **kw):
+    return rks(mol, basis, None, **kw)

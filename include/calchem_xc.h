@@ -273,6 +273,23 @@ int calchem_mlp_adam(float* d_params, const float* d_grad, float* d_m, float* d_
                      float beta1, float beta2, float eps, void* stream);
 
 /* ======================================================================================
+ * (6) Integrals for the SCF harness around the quadrature (host code, McMurchie-Davidson), over
+ * the same prepared shells: crates/calchem-int/src/one_electron.rs, eri.rs, boys.rs provide these
+ * to the reference's SCF.  Matrices are n_ao x n_ao row-major; the ERI tensor is dense n_ao^4
+ * (chemists' order (pq|rs) at ((p n + q) n + r) n + s), for n_ao <= 400 (-3 beyond).
+ * ====================================================================================== */
+
+/* Boys function F_0 .. F_n_max at t (n_max <= 17). */
+int calchem_scf_boys(int n_max, double t, double* f_out);
+/* Overlap, kinetic and nuclear-attraction matrices (any output may be NULL); charges / xyz_bohr
+ * give the nuclei. */
+int calchem_scf_one_electron(const AoShellGpu* shells, int n_shells, const AoPrimGpu* prims, const AoCompGpu* comps,
+                             int n_ao, int n_atoms, const double* charges, const double* xyz_bohr, double* s_out,
+                             double* t_out, double* v_out);
+int calchem_scf_eri(const AoShellGpu* shells, int n_shells, const AoPrimGpu* prims, const AoCompGpu* comps, int n_ao,
+                    double* eri_out);
+
+/* ======================================================================================
  * (4) Evaluation without device allocation.  No counterpart in the reference: it exists for
  * callers that cannot call cudaMalloc -- a framework that owns all device memory through its own
  * pool, or a serving loop that must not take cudaMalloc's implicit device synchronisation in the
