@@ -266,6 +266,22 @@ __device__ void produce_g2(unsigned char* stage, const __nv_bfloat16* __restrict
   }
 }
 
+// Compensated sum of double-float products: s collects the FP32 parts by TwoSum, c every rounding
+// and low-order term (Ogita-Rump-Oishi Sum2 applied to the TwoProd pieces).
+struct CompSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+__device__ __forceinline__ void acc_prod(CompSum& A, df32 x, df32 t) {
+  const float p = __fmul_rn(x.hi, t.hi);
+  float e = __fmaf_rn(x.hi, t.hi, -p);
+  e = __fmaf_rn(x.hi, t.lo, __fmaf_rn(x.lo, t.hi, e));
+  const df32 q = two_sum(A.s, p);
+  A.s = q.hi;
+  A.c = __fadd_rn(A.c, __fadd_rn(q.lo, e));
+}
+
 __device__ __forceinline__ double cta_sum(double v, double* red_row) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -290,6 +306,7 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
   uint64_t* mbar = reinterpret_cast<uint64_t*>(base + kOffMisc);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffMisc + 8);
   int* s_batch = reinterpret_cast<int*>(base + kOffMisc + 12);
+  uint64_t* ring = reinterpret_cast<uint64_t*>(base + kOffMisc + 16);  // 3 barriers of the epilogue ring
   int* s_eg = reinterpret_cast<int*>(base + kOffEg);
   df32* s_tab = reinterpret_cast<df32*>(base + kOffTab);
 
@@ -300,6 +317,7 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
 
   if (tid == 0) {
     mbar_init(mbar, 1);
+    for (int r = 0; r < 3; ++r) mbar_init(ring + r, 1);
     fence_mbar_init();
   }
   if (tid < 64) s_tab[tid] = df_from_double(exp2(-(double)tid / 64.0));
@@ -318,6 +336,8 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
   const uint32_t tW = tmem;
   const uint32_t tWc = tmem + 128;
   uint32_t phase = 0;
+  uint32_t ring_uses[3] = {0, 0, 0};   // completed phases of each ring barrier
+  bool ring_busy[3] = {false, false, false};  // a copy issued and not yet waited for
   bool failed = false;
 
   const int m_pad_all = (A.max_m + 127) / 128 * 128;
@@ -374,7 +394,7 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
       const uint2* Dhl = (s ? Dhl_b0 : Dhl_a0) + moff;
       const int* fexp = (s ? fexp_b0 : fexp_a0) + roff;
       const int eg = s_eg[g];
-      df32 dr = {0.f, 0.f}, dgx = {0.f, 0.f}, dgy = {0.f, 0.f}, dgz = {0.f, 0.f};
+      CompSum sr, sgx, sgy, sgz;
       const int nkb = m_pad / 64;
       const uint32_t idesc = idesc_bf16_f32(128, 128);
       for (int nc = 0; nc < m_pad && !failed; nc += 128) {
@@ -411,43 +431,82 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
           const bool group_end = ((kb & 15) == 15) || kb == nkb - 1;
           if (!group_end) continue;
           const bool first_group = kb < 16, last_group = kb == nkb - 1;
-          // this thread: point g, columns [kGroupCols h, kGroupCols (h + 1)) of the chunk.
-          // T = S + hh + corrections: hh is exact, the corrections are >= 2^8 smaller, so T is
-          // formed as a double-float.
-          for (int c0 = h * kGroupCols; c0 < (h + 1) * kGroupCols; c0 += 16) {
-            float a[16], b[16];
-            tmem_ld16(tH + lane_base + (uint32_t)c0, a);
-            tmem_ld16(tC1 + lane_base + (uint32_t)c0, b);
-            float cc[16];
-            tmem_ld16(tC2 + lane_base + (uint32_t)c0, cc);
+          if (!last_group) {
+            // running sum S += hh + corrections (contractions longer than 1024 AOs)
+            for (int c0 = h * kGroupCols; c0 < (h + 1) * kGroupCols; c0 += 16) {
+              float a[16], b[16], cc[16];
+              tmem_ld16(tH + lane_base + (uint32_t)c0, a);
+              tmem_ld16(tC1 + lane_base + (uint32_t)c0, b);
+              tmem_ld16(tC2 + lane_base + (uint32_t)c0, cc);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) b[j] += cc[j];  // corrections (small)
-            if (!first_group) {
-              tmem_ld16(tS + lane_base + (uint32_t)c0, cc);
-            }
-            if (!last_group) {
+              for (int j = 0; j < 16; ++j) b[j] += cc[j];
+              if (!first_group) tmem_ld16(tS + lane_base + (uint32_t)c0, cc);
 #pragma unroll
               for (int j = 0; j < 16; ++j) a[j] = (first_group ? 0.f : cc[j]) + a[j] + b[j];
               tmem_st16(tS + lane_base + (uint32_t)c0, a);
-            } else {
+            }
+          } else {
+            // rho = sum Phi T and grad rho terms over the chunk's 128 AOs.  The eight planes of the
+            // chunk's rows stream through the (now idle) operand stage in steps of 16 rows (64 KB),
+            // three steps in flight (bulk copies on the TMA engine); in step s the group h takes the
+            // four columns 16 s + 4 h .. + 3.  Sums are compensated (the hi parts by TwoSum, the
+            // rounding terms collected separately).
+            const uint32_t sb = smem_addr(stage);
+            const int n_steps = min(8, (m - nc + 15) / 16);
+            auto issue = [&](int st) {
+              const int r = st % 3;
+              mbar_arrive_expect_tx(ring + r, 8 * 16 * 512);
 #pragma unroll
-              for (int j = 0; j < 16; ++j) {
+              for (int pl = 0; pl < 8; ++pl)
+                bulk_g2s(sb + r * 65536 + pl * 8192, planes + pl * P + (size_t)(nc + 16 * st) * 128, 8192, ring + r);
+              ring_busy[r] = true;
+            };
+            if (tid == 0) {
+              fence_proxy_async_smem();
+              for (int st = 0; st < min(3, n_steps); ++st) issue(st);
+            }
+            for (int st = 0; st < n_steps; ++st) {
+              const int r = st % 3;
+              const bool ok = mbar_wait_bounded(ring + r, ring_uses[r] & 1u, kWaitLimit);
+              if (ok) {  // on expiry the copy stays pending and teardown waits for it again
+                ring_uses[r]++;
+                ring_busy[r] = false;
+              }
+              if (__syncthreads_or(!ok)) { failed = true; break; }
+              const int c0 = 16 * st + 4 * h;
+              float a[4], b[4], c2[4], cc[4];
+              // hh, the two correction classes and (after a first group of 16 K blocks) the running sum
+              tmem_ld4x4(tH + lane_base + (uint32_t)c0, tC1 + lane_base + (uint32_t)c0, tC2 + lane_base + (uint32_t)c0,
+                         (first_group ? tH : tS) + lane_base + (uint32_t)c0, a, b, c2, cc);
+#pragma unroll
+              for (int j = 0; j < 4; ++j) b[j] += c2[j];
+              const float* buf = reinterpret_cast<const float*>(stage + r * 65536);
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
                 const int nu = nc + c0 + j;
-                df32 t = first_group ? two_sum(a[j], b[j]) : df_add_f(two_sum(cc[j], a[j]), b[j]);
-                t = nu < m ? df_ldexp(t, eg + fexp[s_ao[nu]]) : df32{0.f, 0.f};
-                const size_t o = (size_t)nu * 128 + g;
-                dr = df_add(dr, df_mul(df32{planes[o], planes[4 * P + o]}, t));
-                dgx = df_add(dgx, df_mul(df32{planes[P + o], planes[5 * P + o]}, t));
-                dgy = df_add(dgy, df_mul(df32{planes[2 * P + o], planes[6 * P + o]}, t));
-                dgz = df_add(dgz, df_mul(df32{planes[3 * P + o], planes[7 * P + o]}, t));
+                if (nu < m) {
+                  df32 t = first_group ? two_sum(a[j], b[j]) : df_add_f(two_sum(cc[j], a[j]), b[j]);
+                  t = df_ldexp(t, eg + fexp[s_ao[nu]]);
+                  const int o = (4 * h + j) * 128 + g;  // row within the step, point g
+                  acc_prod(sr, df32{buf[o], buf[4 * 2048 + o]}, t);
+                  acc_prod(sgx, df32{buf[2048 + o], buf[5 * 2048 + o]}, t);
+                  acc_prod(sgy, df32{buf[2 * 2048 + o], buf[6 * 2048 + o]}, t);
+                  acc_prod(sgz, df32{buf[3 * 2048 + o], buf[7 * 2048 + o]}, t);
+                }
+              }
+              __syncthreads();  // buffer r is free
+              if (tid == 0 && st + 3 < n_steps) {
+                fence_proxy_async_smem();
+                issue(st + 3);
               }
             }
+            if (failed) break;
           }
           tc_fence_before();
           __syncthreads();
         }
       }
-      double acc[4] = {df_to_double(dr), df_to_double(dgx), df_to_double(dgy), df_to_double(dgz)};
+      double acc[4] = {sr.value(), sgx.value(), sgy.value(), sgz.value()};
       if (failed) break;
       for (int k = 0; k < 4; ++k) dens[h][k][g] = acc[k];
       __syncthreads();
@@ -632,6 +691,8 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
   if (failed) {
     if (tid == 0) atomicExch(A.counter + 2, 1);
     mbar_wait_bounded(mbar, phase ^ 1u, kWaitLimit);  // the round that timed out
+    for (int r = 0; r < 3; ++r)  // bulk copies still in flight into shared memory
+      if (ring_busy[r]) mbar_wait_bounded(ring + r, ring_uses[r] & 1u, kWaitLimit);
   }
   tc_fence_before();
   __syncthreads();
