@@ -1,36 +1,36 @@
 // vxc_mixed.cu -- tensor-core (tcgen05) XC quadrature: the mixed-precision form.
 //
-// One persistent CTA (512 threads, one per SM) takes 128-point batches from a device queue.  For
-// each batch of m candidate AOs (padded to m_pad, a multiple of 128):
+// Two persistent CTAs of 256 threads per SM (each 256 TMEM columns, ~110 KB of shared memory) take
+// 128-point batches from a device queue, so that one CTA's SIMT and FP64 phases run under the
+// other's contractions.  For each batch of m candidate AOs (padded to m_pad, a multiple of 128):
 //   (A) AO values and gradients in double-float arithmetic on the FP32 pipe (48-bit: error-free
 //       transformations, a table-driven exp, basis constants and coordinates as float pairs) into
 //       the CTA's scratch slab as eight [m_pad][128] planes (hi and lo of phi, d/dx, d/dy, d/dz),
 //       with the reference's screening (ao_grid.rs:182-230).  Plain FP32 AO values carry errors of
 //       a few ulp that are identical at the 302 angular points of a radial shell and so do not
 //       average out; at 48 bits they are negligible;
-//   (B) GEMM1  T[g][nu] = sum_mu Phi[g][mu] D[mu][nu]  on tcgen05: M = 128 points, N = 128 AOs
-//       per TMEM chunk, K = AOs in blocks of 64.  Every Phi row (point) and every D row is scaled
-//       by a power of two to |x| < 1 and cut into BF16 fixed-point pieces: three for Phi
-//       (multiples of 2^-7, 2^-15, 2^-23, 2^-31) and four for D, 32 bits each, and the ten products
-//       with weight down to 2^-24 are formed.  The hh products are integer multiples of 2^-14 and
-//       a 1024-term sum stays below 2^24 units,
-//       so the tensor core's FP32 accumulation (which truncates) adds them EXACTLY; the correction
-//       classes (i + j = 1; i + j = 2 and 3 for slice indices i of Phi and j of D) are at least
-//       2^8 smaller, so their truncation is below 2^-32 of T.  The three classes accumulate in
-//       separate TMEM accumulators over up to 16 K blocks (the hh sum stays exact up to K = 1024);
-//       longer contractions are combined into a fourth accumulator, and T is scaled back exactly;
-//   (C) epilogue: each thread owns one point (its TMEM lane); T = hh + corrections is kept as a
-//       double-float and rho = sum Phi T, grad rho = 2 sum grad Phi T are accumulated in
-//       double-float;
-//   (D) the functional in FP64 per point, Exc and Nelec partial sums in FP64 (vxc.rs:890-920);
-//   (E) GEMM2  W = Z^T Phi + Phi^T Z  (Z = (w v_rho / 2) Phi + (w u) . grad Phi) on lower
-//       128 x 128 AO tile pairs, K = 128 points: each operand split into three BF16 pieces
-//       x = hi + mid + lo (floating, 24 bits), twelve products per K step, the hh products in one
-//       accumulator and the corrections in another;
-//   (F) the W tile is drained from TMEM and added to V's upper triangle with FP64 atomics,
+//   (B) every Phi row (point) is scaled by a power of two to |x| < 1 and cut into four fixed-point
+//       BF16 pieces (multiples of 2^-7, 2^-15, 2^-23, 2^-31), written once per batch into the slab
+//       as 128-byte-swizzled operand tiles (the GEMM1 A operand, loaded by bulk copies);
+//   (C) GEMM1  T[g][nu] = sum_mu Phi[g][mu] D[mu][nu]  on tcgen05: M = 128 points, N = 64 AOs per
+//       TMEM chunk, K = AOs in blocks of 64; D rows are cut the same way (four pieces, gathered per
+//       block); the ten products with weight down to 2^-24 are formed.  The hh products are integer
+//       multiples of 2^-14 and a 1024-term sum stays below 2^24 units, so the tensor core's FP32
+//       accumulation (which truncates) adds them EXACTLY; the correction classes (i + j = 1;
+//       i + j = 2 and 3) are at least 2^8 smaller and accumulate separately, over up to 16 K
+//       blocks; longer contractions are combined into a fourth accumulator;
+//   (D) epilogue: each thread owns one point (its TMEM lane); T = hh + corrections is kept as a
+//       double-float; the planes stream through shared memory by bulk copies and rho,
+//       grad rho = 2 sum grad Phi T are compensated sums of double-float products;
+//   (E) the functional in FP64 per point, Exc and Nelec partial sums in FP64 (vxc.rs:890-920);
+//   (F) GEMM2  W = Z^T Phi + Phi^T Z  (Z = (w v_rho / 2) Phi + (w u) . grad Phi) on lower
+//       128 x 128 AO tile pairs, K = 64 points per step: Phi and Z split into three BF16 pieces
+//       (floating, 24 bits), written as swizzled tiles and loaded by bulk copies, six products per
+//       half step, the hh products in one accumulator and the corrections in another;
+//   (G) the W tile is drained from TMEM and added to V's upper triangle with FP64 atomics,
 //       coalesced across lanes; a final kernel mirrors the upper triangle into the lower.
-// Shared-memory operand tiles use the 128-byte-swizzled K-major layout; every mbarrier wait is
-// bounded, and a wait that expires sets the status flag, drains, frees TMEM and returns.
+// Every mbarrier wait is bounded, and a wait that expires sets the status flag, waits (bounded) for
+// the CTA's own MMAs and copies in flight, frees TMEM and returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -45,21 +45,23 @@ namespace cxc {
 
 namespace {
 
-constexpr int kMT = 512;              // threads per CTA
+constexpr int kMT = 256;              // threads per CTA (two CTAs per SM)
 constexpr int kGroups = kMT / 128;    // thread groups of 128 (one thread per point in each)
-constexpr int kGroupCols = 128 / kGroups;  // TMEM columns of a 128-column chunk per group
 constexpr int kMaxMixedM = 2048;      // AOs per batch held in shared memory
 constexpr uint32_t kWaitLimit = 1u << 26;
-constexpr uint32_t kTmemCols = 512;
-constexpr int kStageBytes = 196608;   // operand staging area (12 tiles of 16 KB)
+constexpr uint32_t kTmemCols = 256;
+constexpr int kNc = 64;               // GEMM1 N chunk (AOs) per TMEM accumulator
+constexpr int kStageBytes = 98304;    // operand staging area: GEMM1 A 64 KB + B 32 KB; GEMM2 6 x 16 KB
 constexpr int kOffCoef = kStageBytes;                    // float [8][128]
-constexpr int kOffDens = kOffCoef + 8 * 128 * 4;         // double [kGroups][4][128]
-constexpr int kOffAo = kOffDens + kGroups * 4 * 128 * 8; // int [kMaxMixedM]
+constexpr int kOffAo = kOffCoef + 8 * 128 * 4;           // int [kMaxMixedM]
 constexpr int kOffRed = kOffAo + kMaxMixedM * 4;         // double [3][kMT / 32]
 constexpr int kOffEg = kOffRed + 3 * (kMT / 32) * 8;     // int [128]: per-point power-of-two scale
 constexpr int kOffTab = kOffEg + 128 * 4;                // df32 [64]: 2^(-j/64)
-constexpr int kOffMisc = kOffTab + 64 * 8;               // mbarrier, tmem slot, batch, flags
+constexpr int kOffMisc = kOffTab + 64 * 8;               // mbarriers, tmem slot, batch
 constexpr int kSmemBytes = kOffMisc + 64 + 1024;         // + alignment slack
+// dens [kGroups][4][128] doubles (8 KB) lives in the stage at +64 KB while the stage is idle
+constexpr int kOffDensInStage = 65536;
+static_assert(2 * (kSmemBytes + 1024) <= 233472, "two CTAs must fit in one SM's shared memory");
 
 __device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
   return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
@@ -196,18 +198,13 @@ __device__ void ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restr
   }
 }
 
-// GEMM1 operands for K block kb and N chunk [nc, nc + 128):
-//   A = Phi[g][mu] 2^-e_g (double-float planes) in fixed-point pieces hi / mid / lo / q at
-//       +0 / +16K / +32K / +112K,
-//   B = D[nu][mu] 2^-f_nu pieces hi / mid / lo / lo2 at +48K / +64K / +80K / +96K,
-// B gathered from the packed fixed-point density (x = hi | mid << 16, y = lo | lo2 << 16).
-__device__ void produce_g1(unsigned char* stage, const float* __restrict__ planes, size_t P,
-                           const uint2* __restrict__ Dp, const int* s_ao, const int* s_eg, int n, int m, int kb,
-                           int nc) {
-  const int tid = threadIdx.x;
-  const uint32_t sbase = smem_addr(stage);
-  for (int e = tid; e < 128 * 8; e += kMT) {
-    const int g = e & 127, c = e >> 7;
+// (B) the GEMM1 A operand of the whole batch: for K block kb, tile q (q = 0..3: pieces of weight
+// 2^-7, 2^-15, 2^-23, 2^-31) at apack + (4 kb + q) * 16 KB, 128 points x 64 AOs, 128-byte swizzle.
+// Phi[g][mu] 2^-e_g from the double-float planes.
+__device__ void pack_a(unsigned char* __restrict__ apack, const float* __restrict__ planes, size_t P,
+                       const int* s_eg, int nkb) {
+  for (int e = threadIdx.x; e < nkb * 128 * 8; e += kMT) {
+    const int kb = e >> 10, g = e & 127, c = (e >> 7) & 7;
     const int mu0 = kb * 64 + c * 8;
     const int eg = s_eg[g];
     __nv_bfloat16 h[8], md[8], l[8], q[8];
@@ -216,13 +213,21 @@ __device__ void produce_g1(unsigned char* stage, const float* __restrict__ plane
       const size_t o = (size_t)(mu0 + k) * 128 + g;
       fixsplit4(ldexpf(planes[o], -eg), ldexpf(planes[4 * P + o], -eg), h[k], md[k], l[k], q[k]);
     }
-    const uint32_t off = sw128(g, c);
-    st_shared_v4(sbase + off, pack8v(h));
-    st_shared_v4(sbase + 16384 + off, pack8v(md));
-    st_shared_v4(sbase + 32768 + off, pack8v(l));
-    st_shared_v4(sbase + 114688 + off, pack8v(q));
+    unsigned char* t = apack + (size_t)kb * 65536 + sw128(g, c);
+    *reinterpret_cast<uint4*>(t) = pack8v(h);
+    *reinterpret_cast<uint4*>(t + 16384) = pack8v(md);
+    *reinterpret_cast<uint4*>(t + 32768) = pack8v(l);
+    *reinterpret_cast<uint4*>(t + 49152) = pack8v(q);
   }
-  for (int e = tid; e < 128 * 8; e += kMT) {
+}
+
+// GEMM1 B operand for K block kb and N chunk [nc, nc + 64): D[nu][mu] 2^-f_nu pieces hi / mid / lo
+// / lo2 at stage + 64 KB + q * 8 KB (64 rows x 64 K, 128-byte swizzle), gathered from the packed
+// fixed-point density (x = hi | mid << 16, y = lo | lo2 << 16).
+__device__ void gather_b(unsigned char* stage, const uint2* __restrict__ Dp, const int* s_ao, int n, int m, int kb,
+                         int nc) {
+  const uint32_t sbase = smem_addr(stage) + 65536;
+  for (int e = threadIdx.x; e < kNc * 8; e += kMT) {
     const int c = e & 7, r = e >> 3;
     const int nu = nc + r;
     const int mu0 = kb * 64 + c * 8;
@@ -240,30 +245,17 @@ __device__ void produce_g1(unsigned char* stage, const float* __restrict__ plane
       }
     }
     const uint32_t off = sw128(r, c);
-    st_shared_v4(sbase + 49152 + off, make_uint4(hw[0], hw[1], hw[2], hw[3]));
-    st_shared_v4(sbase + 65536 + off, make_uint4(mw[0], mw[1], mw[2], mw[3]));
-    st_shared_v4(sbase + 81920 + off, make_uint4(lw[0], lw[1], lw[2], lw[3]));
-    st_shared_v4(sbase + 98304 + off, make_uint4(qw[0], qw[1], qw[2], qw[3]));
+    st_shared_v4(sbase + off, make_uint4(hw[0], hw[1], hw[2], hw[3]));
+    st_shared_v4(sbase + 8192 + off, make_uint4(mw[0], mw[1], mw[2], mw[3]));
+    st_shared_v4(sbase + 16384 + off, make_uint4(lw[0], lw[1], lw[2], lw[3]));
+    st_shared_v4(sbase + 24576 + off, make_uint4(qw[0], qw[1], qw[2], qw[3]));
   }
 }
 
-// GEMM2 operands for AO tiles I (rows of A) and J (rows of B), points [64 kb2, 64 kb2 + 64).
-// Images in the slab: 0..2 = Phi^T hi/mid/lo, 3..5 = Z^T hi/mid/lo, each [m_pad][128] BF16.
-// Stage tiles (16 KB each): 0..2 Z_I, 3..5 Phi_I, 6..8 Phi_J, 9..11 Z_J (hi, mid, lo).
-__device__ void produce_g2(unsigned char* stage, const __nv_bfloat16* __restrict__ img, size_t IP, int I, int J,
-                           int kb2) {
-  const int tid = threadIdx.x;
-  const uint32_t sbase = smem_addr(stage);
-  const int n_tiles = I == J ? 6 : 12;  // a diagonal pair reads Z_I and Phi_I only
-  for (int e = tid; e < n_tiles * 128 * 8; e += kMT) {
-    const int t = e >> 10, r = (e >> 3) & 127, c = e & 7;
-    const int piece = t % 3, group = t / 3;               // group: 0 Z_I, 1 Phi_I, 2 Phi_J, 3 Z_J
-    const int img_id = ((group == 0 || group == 3) ? 3 : 0) + piece;
-    const int row = (group < 2 ? I : J) + r;
-    // plain (coherent) load: the images are written earlier in this kernel by this CTA
-    const uint4 v = *reinterpret_cast<const uint4*>(img + img_id * IP + (size_t)row * 128 + kb2 * 64 + c * 8);
-    st_shared_v4(sbase + t * 16384 + sw128(r, c), v);
-  }
+// Byte offset of GEMM2 image tile (piece p: 0..2 Phi^T, 3..5 Z^T; AO row block ib; point block kb2)
+// in the slab's image area; each tile is 128 AO rows x 64 points, 128-byte swizzle.
+__device__ __forceinline__ size_t img_tile(int p, int ib, int kb2, int n_ib) {
+  return (((size_t)p * n_ib + ib) * 2 + kb2) * 16384;
 }
 
 // Compensated sum of double-float products: s collects the FP32 parts by TwoSum, c every rounding
@@ -295,18 +287,19 @@ __device__ __forceinline__ double cta_sum(double v, double* red_row) {
 
 }  // namespace
 
-__global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A) {
+__global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* stage = base;
   float(*coef)[128] = reinterpret_cast<float(*)[128]>(base + kOffCoef);
-  double(*dens)[4][128] = reinterpret_cast<double(*)[4][128]>(base + kOffDens);  // [kGroups]
+  double(*dens)[4][128] = reinterpret_cast<double(*)[4][128]>(base + kOffDensInStage);  // [kGroups], stage idle
   int* s_ao = reinterpret_cast<int*>(base + kOffAo);
   double(*red)[kMT / 32] = reinterpret_cast<double(*)[kMT / 32]>(base + kOffRed);
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(base + kOffMisc);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffMisc + 8);
-  int* s_batch = reinterpret_cast<int*>(base + kOffMisc + 12);
-  uint64_t* ring = reinterpret_cast<uint64_t*>(base + kOffMisc + 16);  // 3 barriers of the epilogue ring
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(base + kOffMisc);      // MMA commits
+  uint64_t* tbar = reinterpret_cast<uint64_t*>(base + kOffMisc + 8);  // operand bulk copies
+  uint64_t* ring = reinterpret_cast<uint64_t*>(base + kOffMisc + 16); // 2 barriers of the epilogue ring
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffMisc + 32);
+  int* s_batch = reinterpret_cast<int*>(base + kOffMisc + 36);
   int* s_eg = reinterpret_cast<int*>(base + kOffEg);
   df32* s_tab = reinterpret_cast<df32*>(base + kOffTab);
 
@@ -317,7 +310,9 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
 
   if (tid == 0) {
     mbar_init(mbar, 1);
-    for (int r = 0; r < 3; ++r) mbar_init(ring + r, 1);
+    mbar_init(tbar, 1);
+    mbar_init(ring, 1);
+    mbar_init(ring + 1, 1);
     fence_mbar_init();
   }
   if (tid < 64) s_tab[tid] = df_from_double(exp2(-(double)tid / 64.0));
@@ -330,31 +325,42 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-  // TMEM: GEMM1 uses four 128-column accumulators (hh, hm+mh, hl+mm+lh, running sum); GEMM2, which
-  // runs after GEMM1 is finished, reuses the first two for its hh products and its corrections.
-  const uint32_t tH = tmem, tC1 = tmem + 128, tC2 = tmem + 256, tS = tmem + 384;
-  const uint32_t tW = tmem;
-  const uint32_t tWc = tmem + 128;
-  uint32_t phase = 0;
-  uint32_t ring_uses[3] = {0, 0, 0};   // completed phases of each ring barrier
-  bool ring_busy[3] = {false, false, false};  // a copy issued and not yet waited for
+  // TMEM: GEMM1 uses four 64-column accumulators (hh, hm+mh, hl+mm+lh, running sum); GEMM2, which
+  // runs after GEMM1 is finished, uses 128 columns for its hh products and 128 for its corrections.
+  const uint32_t tH = tmem, tC1 = tmem + 64, tC2 = tmem + 128, tS = tmem + 192;
+  const uint32_t tW = tmem, tWc = tmem + 128;
+  uint32_t phase = 0, tphase = 0;
+  uint32_t ring_uses[2] = {0, 0};
+  bool ring_busy[2] = {false, false};  // a bulk copy issued and not yet waited for
+  bool tma_busy = false;
   bool failed = false;
 
   const int m_pad_all = (A.max_m + 127) / 128 * 128;
+  const int n_ib = m_pad_all / 128;
   const size_t P = (size_t)m_pad_all * 128;  // floats per plane
   float* planes = reinterpret_cast<float*>(A.slab + (size_t)blockIdx.x * A.slab_stride);
-  __nv_bfloat16* img = reinterpret_cast<__nv_bfloat16*>(planes + 8 * P);  // 6 images of P bf16
-  // split densities: [alpha nn_total][beta nn_total] uint2, then row exponents [alpha n_total][beta n_total]
+  unsigned char* apack = reinterpret_cast<unsigned char*>(planes + 8 * P);  // m_pad_all / 64 x 64 KB
+  unsigned char* img = apack + (size_t)m_pad_all * 1024;                    // 6 x n_ib x 2 x 16 KB
   const uint2* Dhl_a0 = reinterpret_cast<const uint2*>(A.Pa);
   const uint2* Dhl_b0 = Dhl_a0 + G.nn_total;
   const int* fexp_a0 = reinterpret_cast<const int*>(Dhl_a0 + 2 * G.nn_total);
   const int* fexp_b0 = fexp_a0 + G.n_total;
+  const uint32_t sb = smem_addr(stage);
 
-  // one MMA round: wait for the commit of the phase just issued
+  // one MMA round: wait for the commit of the round just issued
   auto wait_mma = [&]() -> bool {
-    bool ok = mbar_wait_bounded(mbar, phase, kWaitLimit);
+    const bool ok = mbar_wait_bounded(mbar, phase, kWaitLimit);
     phase ^= 1u;
     tc_fence_after();
+    return __syncthreads_or(!ok) == 0;
+  };
+  // operand bulk copies of this round (issued by thread 0 with expect_tx)
+  auto wait_tma = [&]() -> bool {
+    const bool ok = mbar_wait_bounded(tbar, tphase, kWaitLimit);
+    if (ok) {
+      tphase ^= 1u;
+      tma_busy = false;
+    }
     return __syncthreads_or(!ok) == 0;
   };
 
@@ -371,6 +377,7 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
     const long long moff = mol_mat(G, bd.mol);
     const int roff = mol_row(G, bd.mol);
     const int m_pad = (m + 127) / 128 * 128;
+    const int nkb = (m + 63) / 64;
     for (int i = tid; i < m; i += kMT) s_ao[i] = G.batch_ao[bd.ao_start + i];
     ao_eval_df(G, bd, planes, P, m_pad, s_tab);
     __syncthreads();
@@ -388,6 +395,9 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
       }
       __syncthreads();
     }
+    pack_a(apack, planes, P, s_eg, nkb);
+    fence_proxy_async_global();  // the packed tiles are read by bulk copies
+    __syncthreads();
 
     double spin_rho[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     for (int s = 0; s < nspin && !failed; ++s) {
@@ -395,20 +405,24 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
       const int* fexp = (s ? fexp_b0 : fexp_a0) + roff;
       const int eg = s_eg[g];
       CompSum sr, sgx, sgy, sgz;
-      const int nkb = m_pad / 64;
-      const uint32_t idesc = idesc_bf16_f32(128, 128);
-      for (int nc = 0; nc < m_pad && !failed; nc += 128) {
+      const uint32_t idesc = idesc_bf16_f32(128, kNc);
+      for (int nc = 0; nc < m && !failed; nc += kNc) {
         for (int kb = 0; kb < nkb; ++kb) {
-          produce_g1(stage, planes, P, Dhl, s_ao, s_eg, n, m, kb, nc);
+          if (tid == 0) {  // A operand of this K block: four 16 KB tiles
+            mbar_arrive_expect_tx(tbar, 65536);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) bulk_g2s(sb + t * 16384, apack + (size_t)kb * 65536 + t * 16384, 16384, tbar);
+            tma_busy = true;
+          }
+          gather_b(stage, Dhl, s_ao, n, m, kb, nc);
           fence_proxy_async_smem();
-          __syncthreads();
+          if (!wait_tma()) { failed = true; break; }
           if (tid == 0) {
             tc_fence_after();
-            const uint32_t sb = smem_addr(stage);
             const uint64_t ah = sdesc_sw128(sb), am = sdesc_sw128(sb + 16384), al = sdesc_sw128(sb + 32768);
-            const uint64_t aq = sdesc_sw128(sb + 114688);
-            const uint64_t bh = sdesc_sw128(sb + 49152), bm = sdesc_sw128(sb + 65536), bl = sdesc_sw128(sb + 81920);
-            const uint64_t bq = sdesc_sw128(sb + 98304);
+            const uint64_t aq = sdesc_sw128(sb + 49152);
+            const uint64_t bh = sdesc_sw128(sb + 65536), bm = sdesc_sw128(sb + 73728), bl = sdesc_sw128(sb + 81920);
+            const uint64_t bq = sdesc_sw128(sb + 90112);
             const bool group_start = (kb & 15) == 0;
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks) {
@@ -433,71 +447,67 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
           const bool first_group = kb < 16, last_group = kb == nkb - 1;
           if (!last_group) {
             // running sum S += hh + corrections (contractions longer than 1024 AOs)
-            for (int c0 = h * kGroupCols; c0 < (h + 1) * kGroupCols; c0 += 16) {
-              float a[16], b[16], cc[16];
+            for (int c0 = h * (kNc / kGroups); c0 < (h + 1) * (kNc / kGroups); c0 += 16) {
+              float a[16], bb[16], cc[16];
               tmem_ld16(tH + lane_base + (uint32_t)c0, a);
-              tmem_ld16(tC1 + lane_base + (uint32_t)c0, b);
+              tmem_ld16(tC1 + lane_base + (uint32_t)c0, bb);
               tmem_ld16(tC2 + lane_base + (uint32_t)c0, cc);
 #pragma unroll
-              for (int j = 0; j < 16; ++j) b[j] += cc[j];
+              for (int j = 0; j < 16; ++j) bb[j] += cc[j];
               if (!first_group) tmem_ld16(tS + lane_base + (uint32_t)c0, cc);
 #pragma unroll
-              for (int j = 0; j < 16; ++j) a[j] = (first_group ? 0.f : cc[j]) + a[j] + b[j];
+              for (int j = 0; j < 16; ++j) a[j] = (first_group ? 0.f : cc[j]) + a[j] + bb[j];
               tmem_st16(tS + lane_base + (uint32_t)c0, a);
             }
           } else {
-            // rho = sum Phi T and grad rho terms over the chunk's 128 AOs.  The eight planes of the
-            // chunk's rows stream through the (now idle) operand stage in steps of 16 rows (64 KB),
-            // three steps in flight (bulk copies on the TMA engine); in step s the group h takes the
-            // four columns 16 s + 4 h .. + 3.  Sums are compensated (the hi parts by TwoSum, the
-            // rounding terms collected separately).
-            const uint32_t sb = smem_addr(stage);
-            const int n_steps = min(8, (m - nc + 15) / 16);
+            // rho = sum Phi T and grad rho terms over the chunk's 64 AOs.  The eight planes of the
+            // chunk's rows stream through the (now idle) stage in steps of 8 rows (32 KB), two
+            // steps in flight; in step st group h takes the four columns 8 st + 4 h .. + 3.
+            const int n_steps = min(kNc / 8, (m - nc + 7) / 8);
             auto issue = [&](int st) {
-              const int r = st % 3;
-              mbar_arrive_expect_tx(ring + r, 8 * 16 * 512);
+              const int r = st & 1;
+              mbar_arrive_expect_tx(ring + r, 8 * 8 * 512);
 #pragma unroll
               for (int pl = 0; pl < 8; ++pl)
-                bulk_g2s(sb + r * 65536 + pl * 8192, planes + pl * P + (size_t)(nc + 16 * st) * 128, 8192, ring + r);
+                bulk_g2s(sb + r * 32768 + pl * 4096, planes + pl * P + (size_t)(nc + 8 * st) * 128, 4096, ring + r);
               ring_busy[r] = true;
             };
             if (tid == 0) {
               fence_proxy_async_smem();
-              for (int st = 0; st < min(3, n_steps); ++st) issue(st);
+              for (int st = 0; st < min(2, n_steps); ++st) issue(st);
             }
             for (int st = 0; st < n_steps; ++st) {
-              const int r = st % 3;
+              const int r = st & 1;
               const bool ok = mbar_wait_bounded(ring + r, ring_uses[r] & 1u, kWaitLimit);
               if (ok) {  // on expiry the copy stays pending and teardown waits for it again
                 ring_uses[r]++;
                 ring_busy[r] = false;
               }
               if (__syncthreads_or(!ok)) { failed = true; break; }
-              const int c0 = 16 * st + 4 * h;
-              float a[4], b[4], c2[4], cc[4];
-              // hh, the two correction classes and (after a first group of 16 K blocks) the running sum
+              const int c0 = 8 * st + 4 * h;
+              float a[4], bb[4], c2[4], cc[4];
               tmem_ld4x4(tH + lane_base + (uint32_t)c0, tC1 + lane_base + (uint32_t)c0, tC2 + lane_base + (uint32_t)c0,
-                         (first_group ? tH : tS) + lane_base + (uint32_t)c0, a, b, c2, cc);
+                         (first_group ? tH : tS) + lane_base + (uint32_t)c0, a, bb, c2, cc);
 #pragma unroll
-              for (int j = 0; j < 4; ++j) b[j] += c2[j];
-              const float* buf = reinterpret_cast<const float*>(stage + r * 65536);
+              for (int j = 0; j < 4; ++j) bb[j] += c2[j];
+              const float* buf = reinterpret_cast<const float*>(stage + r * 32768);
 #pragma unroll
               for (int j = 0; j < 4; ++j) {
                 const int nu = nc + c0 + j;
                 if (nu < m) {
-                  df32 t = first_group ? two_sum(a[j], b[j]) : df_add_f(two_sum(cc[j], a[j]), b[j]);
+                  df32 t = first_group ? two_sum(a[j], bb[j]) : df_add_f(two_sum(cc[j], a[j]), bb[j]);
                   t = df_ldexp(t, eg + fexp[s_ao[nu]]);
                   const int o = (4 * h + j) * 128 + g;  // row within the step, point g
-                  acc_prod(sr, df32{buf[o], buf[4 * 2048 + o]}, t);
-                  acc_prod(sgx, df32{buf[2048 + o], buf[5 * 2048 + o]}, t);
-                  acc_prod(sgy, df32{buf[2 * 2048 + o], buf[6 * 2048 + o]}, t);
-                  acc_prod(sgz, df32{buf[3 * 2048 + o], buf[7 * 2048 + o]}, t);
+                  acc_prod(sr, df32{buf[o], buf[4 * 1024 + o]}, t);
+                  acc_prod(sgx, df32{buf[1024 + o], buf[5 * 1024 + o]}, t);
+                  acc_prod(sgy, df32{buf[2 * 1024 + o], buf[6 * 1024 + o]}, t);
+                  acc_prod(sgz, df32{buf[3 * 1024 + o], buf[7 * 1024 + o]}, t);
                 }
               }
               __syncthreads();  // buffer r is free
-              if (tid == 0 && st + 3 < n_steps) {
+              if (tid == 0 && st + 2 < n_steps) {
                 fence_proxy_async_smem();
-                issue(st + 3);
+                issue(st + 2);
               }
             }
             if (failed) break;
@@ -519,7 +529,7 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
     }
     if (failed) break;
 
-    // (D) functional, one thread per point (threads with h == 0)
+    // (E) functional, one thread per point (threads with h == 0)
     double e_loc = 0, na_loc = 0, nb_loc = 0;
     if (h == 0) {
       const bool live = g < bd.n_pts;
@@ -581,11 +591,11 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
       }
     }
 
-    // (E)+(F) per spin: images Phi^T / Z^T, then lower tile pairs of W
+    // (F)+(G) per spin: image tiles Phi^T / Z^T, then lower tile pairs of W
     for (int s = 0; s < nspin && !failed; ++s) {
       for (int e = tid; e < m_pad * 16; e += kMT) {
-        const int mu = e >> 4, c = e & 15;
-        const size_t o = (size_t)mu * 128 + c * 8;
+        const int mu = e >> 4, c16 = e & 15;
+        const size_t o = (size_t)mu * 128 + c16 * 8;
         float ph[8], zz[8];
         const float4 p0 = *reinterpret_cast<const float4*>(planes + o);
         const float4 p1 = *reinterpret_cast<const float4*>(planes + o + 4);
@@ -601,67 +611,69 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
         const float dzv[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-          const int gg = c * 8 + k;
+          const int gg = c16 * 8 + k;
           zz[k] = coef[4 * s][gg] * ph[k] + coef[4 * s + 1][gg] * dxv[k] + coef[4 * s + 2][gg] * dyv[k] +
                   coef[4 * s + 3][gg] * dzv[k];
         }
+        const int ib = mu >> 7, r = mu & 127, kb2 = c16 >> 3, cc = c16 & 7;
+        const uint32_t sw = sw128(r, cc);
         uint4 hi, mid, lo;
         if (s == 0) {
           pack8x3(ph, hi, mid, lo);
-          *reinterpret_cast<uint4*>(img + o) = hi;
-          *reinterpret_cast<uint4*>(img + P + o) = mid;
-          *reinterpret_cast<uint4*>(img + 2 * P + o) = lo;
+          *reinterpret_cast<uint4*>(img + img_tile(0, ib, kb2, n_ib) + sw) = hi;
+          *reinterpret_cast<uint4*>(img + img_tile(1, ib, kb2, n_ib) + sw) = mid;
+          *reinterpret_cast<uint4*>(img + img_tile(2, ib, kb2, n_ib) + sw) = lo;
         }
         pack8x3(zz, hi, mid, lo);
-        *reinterpret_cast<uint4*>(img + 3 * P + o) = hi;
-        *reinterpret_cast<uint4*>(img + 4 * P + o) = mid;
-        *reinterpret_cast<uint4*>(img + 5 * P + o) = lo;
+        *reinterpret_cast<uint4*>(img + img_tile(3, ib, kb2, n_ib) + sw) = hi;
+        *reinterpret_cast<uint4*>(img + img_tile(4, ib, kb2, n_ib) + sw) = mid;
+        *reinterpret_cast<uint4*>(img + img_tile(5, ib, kb2, n_ib) + sw) = lo;
       }
+      fence_proxy_async_global();  // the tiles are read by bulk copies
       __syncthreads();
       double* V = (s ? A.Vb : A.Va) + moff;
       const uint32_t idesc = idesc_bf16_f32(128, 128);
-      for (int I = 0; I < m_pad && !failed; I += 128) {
+      for (int I = 0; I < m && !failed; I += 128) {
         for (int J = 0; J <= I && !failed; J += 128) {
-          for (int kb2 = 0; kb2 < 2; ++kb2) {
-            produce_g2(stage, img, P, I, J, kb2);
-            fence_proxy_async_smem();
-            __syncthreads();
+          // four rounds: (kb2, half); half 0 A = Z_I, B = Phi_J; half 1 A = Phi_I, B = Z_J
+          for (int rnd = 0; rnd < 4; ++rnd) {
+            const int kb2 = rnd >> 1, half = rnd & 1;
+            if (tid == 0) {
+              mbar_arrive_expect_tx(tbar, 6 * 16384);
+              const int pa = half ? 0 : 3, pb = half ? 3 : 0;  // first piece of the A and B images
+#pragma unroll
+              for (int t = 0; t < 3; ++t) {
+                bulk_g2s(sb + t * 16384, img + img_tile(pa + t, I >> 7, kb2, n_ib), 16384, tbar);
+                bulk_g2s(sb + (3 + t) * 16384, img + img_tile(pb + t, J >> 7, kb2, n_ib), 16384, tbar);
+              }
+              tma_busy = true;
+            }
+            if (!wait_tma()) { failed = true; break; }
             if (tid == 0) {
               tc_fence_after();
-              const uint32_t sb = smem_addr(stage);
-              uint64_t d[12];
+              uint64_t d[6];
 #pragma unroll
-              for (int t = 0; t < 12; ++t) d[t] = sdesc_sw128(sb + t * 16384);
-              if (I == J) {
-#pragma unroll
-                for (int t = 0; t < 3; ++t) { d[6 + t] = d[3 + t]; d[9 + t] = d[t]; }
-              }
-              // d[0..2] Z_I, d[3..5] Phi_I, d[6..8] Phi_J, d[9..11] Z_J (hi, mid, lo)
+              for (int t = 0; t < 6; ++t) d[t] = sdesc_sw128(sb + t * 16384);
+              // d[0..2] A (hi, mid, lo), d[3..5] B (hi, mid, lo)
 #pragma unroll
               for (int ks = 0; ks < 4; ++ks) {
                 const uint64_t o = (uint64_t)(ks * 2);
-                const uint32_t acc = (kb2 > 0 || ks > 0) ? 1u : 0u;
-                mma_bf16_ss(tW, d[0] + o, d[6] + o, idesc, acc);
-                mma_bf16_ss(tW, d[3] + o, d[9] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[0] + o, d[7] + o, idesc, acc);
-                mma_bf16_ss(tWc, d[1] + o, d[6] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[0] + o, d[8] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[1] + o, d[7] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[2] + o, d[6] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[3] + o, d[10] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[4] + o, d[9] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[3] + o, d[11] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[4] + o, d[10] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[5] + o, d[9] + o, idesc, 1u);
+                const uint32_t acc = (rnd > 0 || ks > 0) ? 1u : 0u;
+                mma_bf16_ss(tW, d[0] + o, d[3] + o, idesc, acc);
+                mma_bf16_ss(tWc, d[0] + o, d[4] + o, idesc, acc);
+                mma_bf16_ss(tWc, d[1] + o, d[3] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[0] + o, d[5] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[1] + o, d[4] + o, idesc, 1u);
+                mma_bf16_ss(tWc, d[2] + o, d[3] + o, idesc, 1u);
               }
               mma_commit(mbar);
             }
             if (!wait_mma()) { failed = true; break; }
           }
           if (failed) break;
-          // drain: lane = AO row i of tile I, this group's columns of tile J
+          // drain: lane = AO row i of tile I, this group's 64 columns of tile J
           const int i = I + g;
-          for (int c0 = h * kGroupCols; c0 < (h + 1) * kGroupCols; c0 += 32) {
+          for (int c0 = h * 64; c0 < h * 64 + 64; c0 += 32) {
             float wv[32], wc[32];
             tmem_ld32(tW + lane_base + (uint32_t)c0, wv);
             tmem_ld32(tWc + lane_base + (uint32_t)c0, wc);
@@ -687,11 +699,12 @@ __global__ void __launch_bounds__(kMT, 1) vxc_mixed_kernel(DevGrid G, EvalArgs A
     }
   }
 
-  // teardown: on failure, give any in-flight MMA a bounded chance to finish before freeing TMEM
+  // teardown: on failure, give the MMAs and bulk copies in flight a bounded chance to finish
   if (failed) {
     if (tid == 0) atomicExch(A.counter + 2, 1);
     mbar_wait_bounded(mbar, phase ^ 1u, kWaitLimit);  // the round that timed out
-    for (int r = 0; r < 3; ++r)  // bulk copies still in flight into shared memory
+    if (tma_busy) mbar_wait_bounded(tbar, tphase, kWaitLimit);
+    for (int r = 0; r < 2; ++r)
       if (ring_busy[r]) mbar_wait_bounded(ring + r, ring_uses[r] & 1u, kWaitLimit);
   }
   tc_fence_before();
@@ -751,12 +764,13 @@ __global__ void __launch_bounds__(256) split_density_kernel(const double* __rest
 
 int mixed_supported(int mode) { return (mode == kModeRks || mode == kModeUks) ? 1 : 0; }
 
+// Per-CTA slab: 8 planes (32 B / AO / point), the packed A operand (8 B), the GEMM2 image tiles (12 B).
 size_t mixed_slab_doubles(int max_m) {
   const size_t m_pad = (size_t)(max_m + 127) / 128 * 128;
-  return m_pad * 128 * (8 * sizeof(float) + 6 * sizeof(__nv_bfloat16)) / sizeof(double);
+  return m_pad * 128 * (8 * sizeof(float) + 4 * sizeof(__nv_bfloat16) + 6 * sizeof(__nv_bfloat16)) / sizeof(double);
 }
 
-int mixed_ctas_per_sm() { return 1; }
+int mixed_ctas_per_sm() { return 2; }
 
 int mixed_max_m() { return kMaxMixedM; }
 
