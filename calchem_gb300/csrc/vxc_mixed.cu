@@ -5,7 +5,7 @@
 // other's contractions.  For each batch of m candidate AOs (padded to m_pad, a multiple of 128):
 //   (A) AO values and gradients in double-float arithmetic on the FP32 pipe (48-bit: error-free
 //       transformations, a table-driven exp, basis constants and coordinates as float pairs) into
-//       the CTA's scratch slab as eight [m_pad][128] planes (hi and lo of phi, d/dx, d/dy, d/dz),
+//       the CTA's scratch slab as [m_pad][128] planes (FP32 hi and BF16 lo of phi, d/dx, d/dy, d/dz),
 //       with the reference's screening (ao_grid.rs:182-230).  Plain FP32 AO values carry errors of
 //       a few ulp that are identical at the 302 angular points of a radial shell and so do not
 //       average out; at 48 bits they are negligible;
@@ -115,9 +115,10 @@ __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint4 v) {
 }
 
 // (A) AO values and gradients in double-float.  Planes p = 0..3 (phi, d/dx, d/dy, d/dz) hold the
-// hi parts at planes + p * P and the lo parts at planes + (4 + p) * P; row = local AO, column = point.
-__device__ void ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restrict__ planes, size_t P, int m_pad,
-                           const df32* tab) {
+// FP32 hi parts at planes + p * P and the lo parts, rounded to BF16 (lo <= ulp(hi) / 2, so hi + lo
+// keeps ~32 significant bits), at lo_planes + p * P; row = local AO, column = point.
+__device__ void ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restrict__ planes,
+                           __nv_bfloat16* __restrict__ lo_planes, size_t P, int m_pad, const df32* tab) {
   const int tid = threadIdx.x;
   const int g = tid & 127;
   const bool live = g < bd.n_pts;
@@ -183,10 +184,10 @@ __device__ void ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restr
       planes[P + o] = gx.hi;
       planes[2 * P + o] = gy.hi;
       planes[3 * P + o] = gz.hi;
-      planes[4 * P + o] = v.lo;
-      planes[5 * P + o] = gx.lo;
-      planes[6 * P + o] = gy.lo;
-      planes[7 * P + o] = gz.lo;
+      lo_planes[o] = __float2bfloat16_rn(v.lo);
+      lo_planes[P + o] = __float2bfloat16_rn(gx.lo);
+      lo_planes[2 * P + o] = __float2bfloat16_rn(gy.lo);
+      lo_planes[3 * P + o] = __float2bfloat16_rn(gz.lo);
     }
   }
   // zero the padding rows [m, m_pad)
@@ -194,15 +195,18 @@ __device__ void ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restr
   for (int e = tid; e < pad; e += kMT) {
     const size_t o = (size_t)bd.m * 128 + e;
 #pragma unroll
-    for (int p = 0; p < 8; ++p) planes[p * P + o] = 0.f;
+    for (int p = 0; p < 4; ++p) {
+      planes[p * P + o] = 0.f;
+      lo_planes[p * P + o] = __float2bfloat16_rn(0.f);
+    }
   }
 }
 
 // (B) the GEMM1 A operand of the whole batch: for K block kb, tile q (q = 0..3: pieces of weight
 // 2^-7, 2^-15, 2^-23, 2^-31) at apack + (4 kb + q) * 16 KB, 128 points x 64 AOs, 128-byte swizzle.
 // Phi[g][mu] 2^-e_g from the double-float planes.
-__device__ void pack_a(unsigned char* __restrict__ apack, const float* __restrict__ planes, size_t P,
-                       const int* s_eg, int nkb) {
+__device__ void pack_a(unsigned char* __restrict__ apack, const float* __restrict__ planes,
+                       const __nv_bfloat16* __restrict__ lo_planes, const int* s_eg, int nkb) {
   for (int e = threadIdx.x; e < nkb * 128 * 8; e += kMT) {
     const int kb = e >> 10, g = e & 127, c = (e >> 7) & 7;
     const int mu0 = kb * 64 + c * 8;
@@ -211,7 +215,7 @@ __device__ void pack_a(unsigned char* __restrict__ apack, const float* __restric
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       const size_t o = (size_t)(mu0 + k) * 128 + g;
-      fixsplit4(ldexpf(planes[o], -eg), ldexpf(planes[4 * P + o], -eg), h[k], md[k], l[k], q[k]);
+      fixsplit4(ldexpf(planes[o], -eg), ldexpf(__bfloat162float(lo_planes[o]), -eg), h[k], md[k], l[k], q[k]);
     }
     unsigned char* t = apack + (size_t)kb * 65536 + sw128(g, c);
     *reinterpret_cast<uint4*>(t) = pack8v(h);
@@ -339,7 +343,8 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
   const int n_ib = m_pad_all / 128;
   const size_t P = (size_t)m_pad_all * 128;  // floats per plane
   float* planes = reinterpret_cast<float*>(A.slab + (size_t)blockIdx.x * A.slab_stride);
-  unsigned char* apack = reinterpret_cast<unsigned char*>(planes + 8 * P);  // m_pad_all / 64 x 64 KB
+  __nv_bfloat16* lo_planes = reinterpret_cast<__nv_bfloat16*>(planes + 4 * P);
+  unsigned char* apack = reinterpret_cast<unsigned char*>(lo_planes + 4 * P);  // m_pad_all / 64 x 64 KB
   unsigned char* img = apack + (size_t)m_pad_all * 1024;                    // 6 x n_ib x 2 x 16 KB
   const uint2* Dhl_a0 = reinterpret_cast<const uint2*>(A.Pa);
   const uint2* Dhl_b0 = Dhl_a0 + G.nn_total;
@@ -379,7 +384,7 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
     const int m_pad = (m + 127) / 128 * 128;
     const int nkb = (m + 63) / 64;
     for (int i = tid; i < m; i += kMT) s_ao[i] = G.batch_ao[bd.ao_start + i];
-    ao_eval_df(G, bd, planes, P, m_pad, s_tab);
+    ao_eval_df(G, bd, planes, lo_planes, P, m_pad, s_tab);
     __syncthreads();
     {  // e_g: power-of-two exponent with max_mu |Phi[g][mu]| 2^-e_g < 1
       float mx = 0.f;
@@ -395,7 +400,7 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
       }
       __syncthreads();
     }
-    pack_a(apack, planes, P, s_eg, nkb);
+    pack_a(apack, planes, lo_planes, s_eg, nkb);
     fence_proxy_async_global();  // the packed tiles are read by bulk copies
     __syncthreads();
 
@@ -464,12 +469,15 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
             // chunk's rows stream through the (now idle) stage in steps of 8 rows (32 KB), two
             // steps in flight; in step st group h takes the four columns 8 st + 4 h .. + 3.
             const int n_steps = min(kNc / 8, (m - nc + 7) / 8);
-            auto issue = [&](int st) {
+            auto issue = [&](int st) {  // 8 rows: 4 FP32 hi planes (4 KB each), 4 BF16 lo planes (2 KB)
               const int r = st & 1;
-              mbar_arrive_expect_tx(ring + r, 8 * 8 * 512);
+              mbar_arrive_expect_tx(ring + r, 4 * 4096 + 4 * 2048);
+              const size_t row0 = (size_t)(nc + 8 * st) * 128;
 #pragma unroll
-              for (int pl = 0; pl < 8; ++pl)
-                bulk_g2s(sb + r * 32768 + pl * 4096, planes + pl * P + (size_t)(nc + 8 * st) * 128, 4096, ring + r);
+              for (int pl = 0; pl < 4; ++pl) {
+                bulk_g2s(sb + r * 32768 + pl * 4096, planes + pl * P + row0, 4096, ring + r);
+                bulk_g2s(sb + r * 32768 + 16384 + pl * 2048, lo_planes + pl * P + row0, 2048, ring + r);
+              }
               ring_busy[r] = true;
             };
             if (tid == 0) {
@@ -491,6 +499,7 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
 #pragma unroll
               for (int j = 0; j < 4; ++j) bb[j] += c2[j];
               const float* buf = reinterpret_cast<const float*>(stage + r * 32768);
+              const __nv_bfloat16* lbuf = reinterpret_cast<const __nv_bfloat16*>(stage + r * 32768 + 16384);
 #pragma unroll
               for (int j = 0; j < 4; ++j) {
                 const int nu = nc + c0 + j;
@@ -498,10 +507,10 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
                   df32 t = first_group ? two_sum(a[j], bb[j]) : df_add_f(two_sum(cc[j], a[j]), bb[j]);
                   t = df_ldexp(t, eg + fexp[s_ao[nu]]);
                   const int o = (4 * h + j) * 128 + g;  // row within the step, point g
-                  acc_prod(sr, df32{buf[o], buf[4 * 1024 + o]}, t);
-                  acc_prod(sgx, df32{buf[1024 + o], buf[5 * 1024 + o]}, t);
-                  acc_prod(sgy, df32{buf[2 * 1024 + o], buf[6 * 1024 + o]}, t);
-                  acc_prod(sgz, df32{buf[3 * 1024 + o], buf[7 * 1024 + o]}, t);
+                  acc_prod(sr, df32{buf[o], __bfloat162float(lbuf[o])}, t);
+                  acc_prod(sgx, df32{buf[1024 + o], __bfloat162float(lbuf[1024 + o])}, t);
+                  acc_prod(sgy, df32{buf[2 * 1024 + o], __bfloat162float(lbuf[2 * 1024 + o])}, t);
+                  acc_prod(sgz, df32{buf[3 * 1024 + o], __bfloat162float(lbuf[3 * 1024 + o])}, t);
                 }
               }
               __syncthreads();  // buffer r is free
@@ -764,10 +773,12 @@ __global__ void __launch_bounds__(256) split_density_kernel(const double* __rest
 
 int mixed_supported(int mode) { return (mode == kModeRks || mode == kModeUks) ? 1 : 0; }
 
-// Per-CTA slab: 8 planes (32 B / AO / point), the packed A operand (8 B), the GEMM2 image tiles (12 B).
+// Per-CTA slab: 4 FP32 + 4 BF16 planes (24 B / AO / point), the packed A operand (8 B), the GEMM2
+// image tiles (12 B).
 size_t mixed_slab_doubles(int max_m) {
   const size_t m_pad = (size_t)(max_m + 127) / 128 * 128;
-  return m_pad * 128 * (8 * sizeof(float) + 4 * sizeof(__nv_bfloat16) + 6 * sizeof(__nv_bfloat16)) / sizeof(double);
+  return m_pad * 128 * (4 * sizeof(float) + 4 * sizeof(__nv_bfloat16) + 4 * sizeof(__nv_bfloat16) +
+                        6 * sizeof(__nv_bfloat16)) / sizeof(double);
 }
 
 int mixed_ctas_per_sm() { return 2; }
