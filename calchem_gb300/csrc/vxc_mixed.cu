@@ -51,16 +51,21 @@ constexpr int kMaxMixedM = 2048;      // AOs per batch held in shared memory
 constexpr uint32_t kWaitLimit = 1u << 26;
 constexpr uint32_t kTmemCols = 256;
 constexpr int kNc = 64;               // GEMM1 N chunk (AOs) per TMEM accumulator
+constexpr int kRing = 4;              // epilogue bulk-copy buffers in the stage
+constexpr int kRingBytes = 24576;     // one 8-row step: 4 x 4 KB FP32 + 4 x 2 KB BF16
 constexpr int kStageBytes = 98304;    // operand staging area: GEMM1 A 64 KB + B 32 KB; GEMM2 6 x 16 KB
 constexpr int kOffCoef = kStageBytes;                    // float [8][128]
 constexpr int kOffAo = kOffCoef + 8 * 128 * 4;           // int [kMaxMixedM]
 constexpr int kOffRed = kOffAo + kMaxMixedM * 4;         // double [3][kMT / 32]
 constexpr int kOffEg = kOffRed + 3 * (kMT / 32) * 8;     // int [128]: per-point power-of-two scale
 constexpr int kOffTab = kOffEg + 128 * 4;                // df32 [64]: 2^(-j/64)
-constexpr int kOffMisc = kOffTab + 64 * 8;               // mbarriers, tmem slot, batch
+constexpr int kOffFx = kOffTab + 64 * 8;                 // int [kNc]: row exponents of the chunk's AOs
+constexpr int kOffMisc = kOffFx + kNc * 4;               // mbarriers, tmem slot, batch
 constexpr int kSmemBytes = kOffMisc + 64 + 1024;         // + alignment slack
 // dens [kGroups][4][128] doubles (8 KB) lives in the stage at +64 KB while the stage is idle
 constexpr int kOffDensInStage = 65536;
+static_assert(kRing * kRingBytes <= kStageBytes, "the epilogue ring lives in the stage");
+static_assert(20 + 8 * kRing + 4 <= 64, "misc area holds the barriers, the TMEM slot and the batch index");
 static_assert(2 * (kSmemBytes + 1024) <= 233472, "two CTAs must fit in one SM's shared memory");
 
 __device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
@@ -301,11 +306,12 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
   double(*red)[kMT / 32] = reinterpret_cast<double(*)[kMT / 32]>(base + kOffRed);
   uint64_t* mbar = reinterpret_cast<uint64_t*>(base + kOffMisc);      // MMA commits
   uint64_t* tbar = reinterpret_cast<uint64_t*>(base + kOffMisc + 8);  // operand bulk copies
-  uint64_t* ring = reinterpret_cast<uint64_t*>(base + kOffMisc + 16); // 2 barriers of the epilogue ring
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffMisc + 32);
-  int* s_batch = reinterpret_cast<int*>(base + kOffMisc + 36);
+  uint64_t* ring = reinterpret_cast<uint64_t*>(base + kOffMisc + 16); // kRing barriers of the epilogue ring
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffMisc + 16 + 8 * kRing);
+  int* s_batch = reinterpret_cast<int*>(base + kOffMisc + 20 + 8 * kRing);
   int* s_eg = reinterpret_cast<int*>(base + kOffEg);
   df32* s_tab = reinterpret_cast<df32*>(base + kOffTab);
+  int* s_fx = reinterpret_cast<int*>(base + kOffFx);
 
   const int tid = threadIdx.x, warp = tid >> 5;
   const int g = tid & 127, h = tid >> 7;
@@ -315,8 +321,7 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
   if (tid == 0) {
     mbar_init(mbar, 1);
     mbar_init(tbar, 1);
-    mbar_init(ring, 1);
-    mbar_init(ring + 1, 1);
+    for (int r = 0; r < kRing; ++r) mbar_init(ring + r, 1);
     fence_mbar_init();
   }
   if (tid < 64) s_tab[tid] = df_from_double(exp2(-(double)tid / 64.0));
@@ -334,8 +339,8 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
   const uint32_t tH = tmem, tC1 = tmem + 64, tC2 = tmem + 128, tS = tmem + 192;
   const uint32_t tW = tmem, tWc = tmem + 128;
   uint32_t phase = 0, tphase = 0;
-  uint32_t ring_uses[2] = {0, 0};
-  bool ring_busy[2] = {false, false};  // a bulk copy issued and not yet waited for
+  uint32_t ring_uses[kRing] = {0, 0, 0, 0};
+  bool ring_busy[kRing] = {false, false, false, false};  // a bulk copy issued and not yet waited for
   bool tma_busy = false;
   bool failed = false;
 
@@ -412,6 +417,9 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
       CompSum sr, sgx, sgy, sgz;
       const uint32_t idesc = idesc_bf16_f32(128, kNc);
       for (int nc = 0; nc < m && !failed; nc += kNc) {
+        // the density rows' power-of-two exponents for this chunk's AOs (read in the epilogue; the
+        // barriers of the K loop order the writes before it)
+        if (tid < kNc) s_fx[tid] = nc + tid < m ? fexp[s_ao[nc + tid]] : 0;
         for (int kb = 0; kb < nkb; ++kb) {
           if (tid == 0) {  // A operand of this K block: four 16 KB tiles
             mbar_arrive_expect_tx(tbar, 65536);
@@ -465,27 +473,27 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
               tmem_st16(tS + lane_base + (uint32_t)c0, a);
             }
           } else {
-            // rho = sum Phi T and grad rho terms over the chunk's 64 AOs.  The eight planes of the
-            // chunk's rows stream through the (now idle) stage in steps of 8 rows (32 KB), two
-            // steps in flight; in step st group h takes the four columns 8 st + 4 h .. + 3.
+            // rho = sum Phi T and grad rho terms over the chunk's 64 AOs.  The planes of the chunk's
+            // rows stream through the (now idle) stage in steps of 8 rows (24 KB), kRing steps in
+            // flight; in step st group h takes the four columns 8 st + 4 h .. + 3.
             const int n_steps = min(kNc / 8, (m - nc + 7) / 8);
             auto issue = [&](int st) {  // 8 rows: 4 FP32 hi planes (4 KB each), 4 BF16 lo planes (2 KB)
-              const int r = st & 1;
+              const int r = st % kRing;
               mbar_arrive_expect_tx(ring + r, 4 * 4096 + 4 * 2048);
               const size_t row0 = (size_t)(nc + 8 * st) * 128;
 #pragma unroll
               for (int pl = 0; pl < 4; ++pl) {
-                bulk_g2s(sb + r * 32768 + pl * 4096, planes + pl * P + row0, 4096, ring + r);
-                bulk_g2s(sb + r * 32768 + 16384 + pl * 2048, lo_planes + pl * P + row0, 2048, ring + r);
+                bulk_g2s(sb + r * kRingBytes + pl * 4096, planes + pl * P + row0, 4096, ring + r);
+                bulk_g2s(sb + r * kRingBytes + 16384 + pl * 2048, lo_planes + pl * P + row0, 2048, ring + r);
               }
               ring_busy[r] = true;
             };
             if (tid == 0) {
               fence_proxy_async_smem();
-              for (int st = 0; st < min(2, n_steps); ++st) issue(st);
+              for (int st = 0; st < min(kRing, n_steps); ++st) issue(st);
             }
             for (int st = 0; st < n_steps; ++st) {
-              const int r = st & 1;
+              const int r = st % kRing;
               const bool ok = mbar_wait_bounded(ring + r, ring_uses[r] & 1u, kWaitLimit);
               if (ok) {  // on expiry the copy stays pending and teardown waits for it again
                 ring_uses[r]++;
@@ -498,14 +506,14 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
                          (first_group ? tH : tS) + lane_base + (uint32_t)c0, a, bb, c2, cc);
 #pragma unroll
               for (int j = 0; j < 4; ++j) bb[j] += c2[j];
-              const float* buf = reinterpret_cast<const float*>(stage + r * 32768);
-              const __nv_bfloat16* lbuf = reinterpret_cast<const __nv_bfloat16*>(stage + r * 32768 + 16384);
+              const float* buf = reinterpret_cast<const float*>(stage + r * kRingBytes);
+              const __nv_bfloat16* lbuf = reinterpret_cast<const __nv_bfloat16*>(stage + r * kRingBytes + 16384);
 #pragma unroll
               for (int j = 0; j < 4; ++j) {
                 const int nu = nc + c0 + j;
                 if (nu < m) {
                   df32 t = first_group ? two_sum(a[j], bb[j]) : df_add_f(two_sum(cc[j], a[j]), bb[j]);
-                  t = df_ldexp(t, eg + fexp[s_ao[nu]]);
+                  t = df_ldexp(t, eg + s_fx[c0 + j]);
                   const int o = (4 * h + j) * 128 + g;  // row within the step, point g
                   acc_prod(sr, df32{buf[o], __bfloat162float(lbuf[o])}, t);
                   acc_prod(sgx, df32{buf[1024 + o], __bfloat162float(lbuf[1024 + o])}, t);
@@ -514,9 +522,9 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
                 }
               }
               __syncthreads();  // buffer r is free
-              if (tid == 0 && st + 2 < n_steps) {
+              if (tid == 0 && st + kRing < n_steps) {
                 fence_proxy_async_smem();
-                issue(st + 2);
+                issue(st + kRing);
               }
             }
             if (failed) break;
@@ -713,7 +721,7 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
     if (tid == 0) atomicExch(A.counter + 2, 1);
     mbar_wait_bounded(mbar, phase ^ 1u, kWaitLimit);  // the round that timed out
     if (tma_busy) mbar_wait_bounded(tbar, tphase, kWaitLimit);
-    for (int r = 0; r < 2; ++r)
+    for (int r = 0; r < kRing; ++r)
       if (ring_busy[r]) mbar_wait_bounded(ring + r, ring_uses[r] & 1u, kWaitLimit);
   }
   tc_fence_before();
