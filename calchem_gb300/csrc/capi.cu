@@ -506,7 +506,7 @@ int enqueue_fxc(Entry& e, int triplet, const double* d_m, int n_trials, double* 
   return 0;
 }
 
-bool valid_xc(int xc) { return xc >= 0 && xc <= 5; }
+bool valid_xc(int xc) { return xc >= 0 && xc <= 8; }
 bool valid_prec(int p, int mode) {
   if (p == CALCHEM_XC_FP64) return true;
   return p == CALCHEM_XC_MIXED && mixed_supported(mode);

@@ -177,7 +177,7 @@ extern "C" int calchem_xc_evaluate_rks_static(const AoShellGpu* d_shells, int n_
   std::lock_guard<std::mutex> lk(g_static_mu);
   if (!d_shells || !d_prims || !d_comps || !d_pts || !d_weights || !d_cand_offsets || !d_cand_shells || !d_total ||
       !d_result || !d_v || n_shells <= 0 || n_prims <= 0 || n_comps <= 0 || n_pts <= 0 || n_batches <= 0 ||
-      n_cand_shells <= 0 || n_ao <= 0 || max_batch_ao <= 0 || xc_code < 0 || xc_code > 5)
+      n_cand_shells <= 0 || n_ao <= 0 || max_batch_ao <= 0 || xc_code < 0 || xc_code > 8)
     return -1;
   void* base = nullptr;
   if (static_scratch(&base) != 0) return -3;

@@ -3,7 +3,8 @@
 // Same functional forms and constants as CalChem's eval_xc_spin
 // (crates/calchem-dft/src/xc.rs:136-828): Slater exchange, VWN5 / VWN_RPA correlation,
 // Becke-88 gradient correction, LYP (Miehlich form), PBE exchange and PBE correlation on PW92,
-// and the SVWN5 / BLYP / PBE / B3LYP / B3LYP5 / PBE0 mixtures.  Every function returns the
+// and the SVWN5 / BLYP / PBE / B3LYP / B3LYP5 / PBE0 mixtures; the range-separated CAM-B3LYP
+// (ITYH-attenuated B88) and wB97X / wB97X-D (attenuated LDA exchange with B97 series) semilocal parts.  Every function returns the
 // energy density f (so that Exc = sum_g w_g f) and its partials with respect to
 // (rho_a, rho_b, gamma_aa, gamma_ab, gamma_bb).
 #pragma once
@@ -278,6 +279,166 @@ __host__ __device__ __forceinline__ XcVal pbe_corr(double ra, double rb, double 
   return o;
 }
 
+// -------------------------------------------------------------------------- CAM-B3LYP (xc.rs:860-960)
+// Short-range attenuation of LDA-type exchange, F(a) = 1 - (8/3) a [sqrt(pi) erf(1/(2a)) +
+// (2a - 4a^3) exp(-1/(4a^2)) - 3a + 4a^3], with its small-a series and its large-a expansion in
+// 1/a^2 (through a^-12, avoiding the cancellation of O(a^4) terms).
+__host__ __device__ __forceinline__ void camb3lyp_attenuation(double a, double& f, double& df) {
+  const double sqrt_pi = 1.7724538509055160273;
+  if (a < 1e-5) {
+    f = fmin(fmax(1.0 - (8.0 / 3.0) * a * sqrt_pi + 8.0 * a * a, 0.0), 1.0);
+    df = -(8.0 / 3.0) * sqrt_pi + 16.0 * a;
+    return;
+  }
+  if (a >= 2.0) {
+    const double z = 1.0 / (a * a);
+    const double c[6] = {1.0 / 36.0, -1.0 / 960.0, 1.0 / 26880.0, -1.0 / 829440.0, 1.0 / 28385280.0,
+                         -1.0 / 1073479680.0};
+    double pw = z;
+    f = 0.0;
+    df = 0.0;
+    for (int k = 0; k < 6; ++k) {
+      f += c[k] * pw;
+      df -= (2 * (k + 1)) * c[k] * pw / a;
+      pw *= z;
+    }
+    return;
+  }
+  const double a2 = a * a, a3 = a2 * a;
+  const double ev = exp(-0.25 / a2);
+  const double bracket = sqrt_pi * erf(0.5 / a) + (2.0 * a - 4.0 * a3) * ev - 3.0 * a + 4.0 * a3;
+  f = fmin(fmax(1.0 - (8.0 / 3.0) * a * bracket, 0.0), 1.0);
+  const double db = -3.0 + 12.0 * a2 * (1.0 - ev);
+  df = -(8.0 / 3.0) * (bracket + a * db);
+}
+
+// ITYH-attenuated Slater + B88 exchange of one spin, w(a) = 0.35 + 0.46 F(a) with the gradient-
+// dependent Fermi wave vector k = sqrt(9 pi / (2 K)) rho^(1/3), K = -f_x / rho^(4/3), mu = 0.33.
+__host__ __device__ __forceinline__ void camb3lyp_x_spin(double r, double g, double& f, double& vr, double& vg) {
+  f = vr = vg = 0.0;
+  if (r < kRhoFloor) return;
+  double fs, vs, fb, vb, gb;
+  slater_spin(r, fs, vs);
+  b88_spin(r, g, fb, vb, gb);
+  const double fx = fs + fb, vrt = vs + vb, vgt = gb;
+  const double kb = -fx / pow(r, 4.0 / 3.0);
+  const double kf = sqrt(9.0 * kPiD / (2.0 * kb)) * cbrt(r);
+  const double a = 0.33 / (2.0 * kf);
+  double fa, dfa;
+  camb3lyp_attenuation(a, fa, dfa);
+  const double w = 0.35 + 0.46 * fa, dw = 0.46 * dfa;
+  const double da_dr = a * (0.5 * vrt / fx - 1.0 / r);
+  const double da_dg = 0.5 * a * vgt / fx;
+  f = w * fx;
+  vr = w * vrt + dw * da_dr * fx;
+  vg = w * vgt + dw * da_dg * fx;
+}
+
+// -------------------------------------------------------------------------- wB97X(-D) (xc.rs:960-1103)
+struct Wb97Params {
+  double omega, cx[5], css[5], cab[5];
+};
+// Chai & Head-Gordon, J. Chem. Phys. 128, 084106 (2008) and Phys. Chem. Chem. Phys. 10, 6615 (2008).
+__host__ __device__ __forceinline__ Wb97Params wb97_params(bool d) {
+  if (!d)
+    return Wb97Params{0.30, {0.842294, 0.726479, 1.04760, -5.70635, 13.2794},
+                      {1.0, -4.33879, 18.2308, -31.7430, 17.2901}, {1.0, 2.37031, -11.3995, 6.58405, -3.78132}};
+  return Wb97Params{0.20, {0.777964, 0.661160, 0.574541, -5.25671, 11.6386},
+                    {1.0, -6.90539, 31.3343, -51.0533, 26.4423}, {1.0, 1.79413, -12.0477, 14.0847, -8.50809}};
+}
+
+// B97 power series in u = gamma x^2 / (1 + gamma x^2); returns g and dg/dx^2.
+__host__ __device__ __forceinline__ void b97_poly(double gp, const double* c, double x2, double& gv, double& dg) {
+  const double gx2 = gp * fmax(x2, 0.0);
+  const double den = 1.0 + gx2;
+  const double u = gx2 / den;
+  const double du = gp / (den * den);
+  gv = c[0] + u * (c[1] + u * (c[2] + u * (c[3] + u * c[4])));
+  dg = (c[1] + u * (2.0 * c[2] + u * (3.0 * c[3] + 4.0 * u * c[4]))) * du;
+}
+
+// PW92 LSDA correlation: (rho eps_c, v_rho_a, v_rho_b).
+__host__ __device__ __forceinline__ void pw92_lsda(double ra, double rb, double& f, double& va, double& vb) {
+  f = va = vb = 0.0;
+  const double rho = ra + rb;
+  if (rho < kRhoFloor) return;
+  const double rs = cbrt(3.0 / (4.0 * kPiD * rho));
+  const double drs = -rs / (3.0 * rho);
+  const double zeta = fmin(fmax((ra - rb) / rho, -1.0), 1.0);
+  double e0, de0, e1, de1, mac, dmac;
+  pw92(rs, Pw92Channel{0.0310907, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294}, e0, de0);
+  pw92(rs, Pw92Channel{0.01554535, 0.20548, 14.1189, 6.1977, 3.3662, 0.62517}, e1, de1);
+  pw92(rs, Pw92Channel{0.0168869, 0.11125, 10.357, 3.6231, 0.88026, 0.49671}, mac, dmac);
+  const double ac = -mac, dac = -dmac;
+  double fz, dfz, ifdd;
+  spin_f(zeta, fz, dfz, ifdd);
+  const double z2 = zeta * zeta, z3 = z2 * zeta, z4 = z2 * z2, om = 1.0 - z4;
+  const double ec = e0 + ac * fz * ifdd * om + (e1 - e0) * fz * z4;
+  const double dec_drs = de0 + dac * fz * ifdd * om + (de1 - de0) * fz * z4;
+  const double dec_dz = ac * ifdd * (dfz * om - 4.0 * z3 * fz) + (e1 - e0) * (dfz * z4 + 4.0 * z3 * fz);
+  f = rho * ec;
+  va = ec + rho * dec_drs * drs + (1.0 - zeta) * dec_dz;
+  vb = ec + rho * dec_drs * drs - (1.0 + zeta) * dec_dz;
+}
+
+__host__ __device__ __forceinline__ void wb97_x_spin(double r, double g, const Wb97Params& P, double& f, double& vr,
+                                                     double& vg) {
+  f = vr = vg = 0.0;
+  if (r < kRhoFloor) return;
+  double fs, vs;
+  slater_spin(r, fs, vs);
+  const double r13 = cbrt(r), r43 = r * r13, r83 = r43 * r43;
+  const double kf = cbrt(6.0 * kPiD * kPiD * r);
+  const double a = P.omega / (2.0 * kf);
+  double fa, dfa;
+  camb3lyp_attenuation(a, fa, dfa);
+  const double da_dr = -a / (3.0 * r);
+  const double fsr = fs * fa;
+  const double vsr = vs * fa + fs * dfa * da_dr;
+  const double x2 = fmax(g, 0.0) / r83;
+  double gx, dgx;
+  b97_poly(0.004, P.cx, x2, gx, dgx);
+  f = fsr * gx;
+  vr = vsr * gx + fsr * dgx * (-(8.0 / 3.0) * x2 / r);
+  vg = fsr * dgx / r83;
+}
+
+__host__ __device__ __forceinline__ XcVal wb97_xc(double ra, double rb, double gaa, double gbb, bool d) {
+  const Wb97Params P = wb97_params(d);
+  XcVal o = xc_zero();
+  double fxa, vxa, gxa, fxb, vxb, gxb;
+  wb97_x_spin(ra, gaa, P, fxa, vxa, gxa);
+  wb97_x_spin(rb, gbb, P, fxb, vxb, gxb);
+  double ft, vta, vtb, fpa, vpa, dum, fpb, vpb;
+  pw92_lsda(ra, rb, ft, vta, vtb);
+  pw92_lsda(ra, 0.0, fpa, vpa, dum);
+  pw92_lsda(0.0, rb, fpb, dum, vpb);
+  const double fperp = ft - fpa - fpb, vperp_a = vta - vpa, vperp_b = vtb - vpb;
+  double xa2 = 0.0, dxa_r = 0.0, dxa_g = 0.0, xb2 = 0.0, dxb_r = 0.0, dxb_g = 0.0;
+  if (ra >= kRhoFloor) {
+    const double r83 = pow(ra, 8.0 / 3.0);
+    xa2 = fmax(gaa, 0.0) / r83;
+    dxa_r = -(8.0 / 3.0) * xa2 / ra;
+    dxa_g = 1.0 / r83;
+  }
+  if (rb >= kRhoFloor) {
+    const double r83 = pow(rb, 8.0 / 3.0);
+    xb2 = fmax(gbb, 0.0) / r83;
+    dxb_r = -(8.0 / 3.0) * xb2 / rb;
+    dxb_g = 1.0 / r83;
+  }
+  double gsa, dgsa, gsb, dgsb, gab, dgab;
+  b97_poly(0.2, P.css, xa2, gsa, dgsa);
+  b97_poly(0.2, P.css, xb2, gsb, dgsb);
+  b97_poly(0.006, P.cab, 0.5 * (xa2 + xb2), gab, dgab);
+  o.f = fxa + fxb + fpa * gsa + fpb * gsb + fperp * gab;
+  o.vra = vxa + vpa * gsa + fpa * dgsa * dxa_r + vperp_a * gab + fperp * dgab * 0.5 * dxa_r;
+  o.vrb = vxb + vpb * gsb + fpb * dgsb * dxb_r + vperp_b * gab + fperp * dgab * 0.5 * dxb_r;
+  o.vgaa = gxa + fpa * dgsa * dxa_g + fperp * dgab * 0.5 * dxa_g;
+  o.vgbb = gxb + fpb * dgsb * dxb_g + fperp * dgab * 0.5 * dxb_g;
+  return o;
+}
+
 // -------------------------------------------------------------------------- mixtures (xc.rs:159-223)
 __host__ __device__ __forceinline__ XcVal xc_eval(int code, double rho_a, double rho_b, double g_aa, double g_ab,
                                          double g_bb) {
@@ -322,6 +483,18 @@ __host__ __device__ __forceinline__ XcVal xc_eval(int code, double rho_a, double
   if (code == 1) xc_axpy(o, 1.0, lyp_corr(ra, rb, gaa, gab, gbb));
   if (code == 3 || code == 4) xc_axpy(o, 0.81, lyp_corr(ra, rb, gaa, gab, gbb));
   if (code == 2 || code == 5) xc_axpy(o, 1.0, pbe_corr(ra, rb, gaa, gab, gbb));
+  if (code == 6) {  // CAM-B3LYP: attenuated Slater + B88 per spin, 0.19 VWN5, 0.81 LYP
+    camb3lyp_x_spin(ra, gaa, fa, va, ga);
+    camb3lyp_x_spin(rb, gbb, fb, vb, gb);
+    o.f += fa + fb;
+    o.vra += va;
+    o.vrb += vb;
+    o.vgaa += ga;
+    o.vgbb += gb;
+    xc_axpy(o, 0.19, vwn_corr(ra, rb, false));
+    xc_axpy(o, 0.81, lyp_corr(ra, rb, gaa, gab, gbb));
+  }
+  if (code == 7 || code == 8) o = wb97_xc(ra, rb, gaa, gbb, code == 8);
   return o;
 }
 
@@ -357,6 +530,10 @@ constexpr VwnPara kVwnRpaPara{0.0310907, -0.409286, 13.0720, 42.7198,
                               0.0448998886415768, 582.2731590427809, -0.14253052416798392, 545.8110641572265};
 
 __host__ __device__ __forceinline__ XcCs xc_eval_cs(int code, double r_in, double g_in) {
+  if (code >= 6) {  // range-separated functionals: the spin form at rho_a = rho_b
+    const XcVal v = xc_eval(code, r_in, r_in, g_in, g_in, g_in);
+    return XcCs{v.f, v.vra, v.vgaa + 0.5 * v.vgab};
+  }
   XcCs o{0.0, 0.0, 0.0};
   const double r = fmax(r_in, 0.0);
   const double rho = r + r;

@@ -27,6 +27,9 @@ def exact_exchange_fraction(func) -> float:
     if func is None:
         return 1.0
     f = XcFunctional.from_name(func) if isinstance(func, str) else XcFunctional(func)
+    if f.is_range_separated():
+        raise NotImplementedError("range-separated exact exchange (erf-attenuated K) is not in this SCF harness; "
+                                  "their semilocal XC part is evaluated by the engines")
     return _EXACT_EXCHANGE.get(f, 0.0)
 
 

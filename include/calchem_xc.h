@@ -64,7 +64,10 @@ enum {
   CALCHEM_XC_PBE = 2,
   CALCHEM_XC_B3LYP = 3,  /* 0.80 Slater + 0.72 dB88 + 0.19 VWN_RPA + 0.81 LYP */
   CALCHEM_XC_B3LYP5 = 4, /* as B3LYP with VWN5 */
-  CALCHEM_XC_PBE0 = 5    /* 0.75 PBE_X + 1.00 PBE_C */
+  CALCHEM_XC_PBE0 = 5,   /* 0.75 PBE_X + 1.00 PBE_C */
+  CALCHEM_XC_CAMB3LYP = 6, /* ITYH-attenuated Slater + B88, 0.19 VWN5 + 0.81 LYP (exact exchange: caller) */
+  CALCHEM_XC_WB97X = 7,    /* wB97X semilocal part (omega 0.30) */
+  CALCHEM_XC_WB97XD = 8    /* wB97X-D semilocal part (omega 0.20) */
 };
 
 /* Precision of the two dense contractions (rho = Phi D Phi^T and V = Phi^T (w v) Phi). */

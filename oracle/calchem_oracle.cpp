@@ -895,8 +895,146 @@ XcOut pbe_c(double ra, double rb, double gaa, double gab, double gbb) {
   return o;
 }
 
+// Short-range attenuation F(a) of LDA-type exchange (xc.rs:863-907).  The reference evaluates erf
+// with calchem_int::erf_approx (boys.rs:5, Cody's rational approximations); std::erf is used here,
+// both accurate to ~1e-16.
+void atten(double a, double& f, double& df) {
+  const double sp = std::sqrt(kPi);
+  if (a < 1e-5) {
+    f = clampd(1.0 - (8.0 / 3.0) * a * sp + 8.0 * a * a, 0.0, 1.0);
+    df = -(8.0 / 3.0) * sp + 16.0 * a;
+    return;
+  }
+  if (a >= 2.0) {
+    const double z = 1.0 / (a * a);
+    const double c[6] = {1.0 / 36.0, -1.0 / 960.0, 1.0 / 26880.0, -1.0 / 829440.0, 1.0 / 28385280.0,
+                         -1.0 / 1073479680.0};
+    f = 0.0; df = 0.0;
+    double pw = z;
+    for (int k = 0; k < 6; ++k) {
+      f += c[k] * pw;
+      df -= (2 * (k + 1)) * c[k] * pw / a;
+      pw *= z;
+    }
+    return;
+  }
+  const double a2 = a * a, a3 = a2 * a;
+  const double ev = std::exp(-0.25 / a2);
+  const double br = sp * std::erf(0.5 / a) + (2.0 * a - 4.0 * a3) * ev - 3.0 * a + 4.0 * a3;
+  f = clampd(1.0 - (8.0 / 3.0) * a * br, 0.0, 1.0);
+  df = -(8.0 / 3.0) * (br + a * (-3.0 + 12.0 * a2 * (1.0 - ev)));
+}
+
+void cam_x_one(double r, double g, double& f, double& vr, double& vg) {
+  // xc.rs:910-944: ITYH attenuation with the B88-based Fermi wave vector, w = 0.35 + 0.46 F
+  f = vr = vg = 0.0;
+  if (r < kRhoCutoff) return;
+  double fs, vs, fb, vb, gb;
+  slater_one(r, fs, vs);
+  b88_one(r, g, fb, vb, gb);
+  const double fx = fs + fb, vrt = vs + vb;
+  const double kb = -fx / std::pow(r, 4.0 / 3.0);
+  const double kf = std::sqrt(9.0 * kPi / (2.0 * kb)) * std::cbrt(r);
+  const double a = 0.33 / (2.0 * kf);
+  double fa, dfa;
+  atten(a, fa, dfa);
+  const double w = 0.35 + 0.46 * fa, dw = 0.46 * dfa;
+  f = w * fx;
+  vr = w * vrt + dw * (a * (0.5 * vrt / fx - 1.0 / r)) * fx;
+  vg = w * gb + dw * (0.5 * a * gb / fx) * fx;
+}
+
+struct Wb97 { double omega, cx[5], css[5], cab[5]; };
+// xc.rs:1008-1017 (Chai & Head-Gordon 2008)
+const Wb97 kWb97xParams = {0.30, {0.842294, 0.726479, 1.04760, -5.70635, 13.2794},
+                     {1.0, -4.33879, 18.2308, -31.7430, 17.2901}, {1.0, 2.37031, -11.3995, 6.58405, -3.78132}};
+const Wb97 kWb97xdParams = {0.20, {0.777964, 0.661160, 0.574541, -5.25671, 11.6386},
+                      {1.0, -6.90539, 31.3343, -51.0533, 26.4423}, {1.0, 1.79413, -12.0477, 14.0847, -8.50809}};
+
+void b97_series(double gp, const double* c, double x2, double& gv, double& dg) {
+  // xc.rs:964-973
+  const double gx2 = gp * std::max(x2, 0.0), den = 1.0 + gx2, u = gx2 / den;
+  gv = c[0] + u * (c[1] + u * (c[2] + u * (c[3] + u * c[4])));
+  dg = (c[1] + u * (2.0 * c[2] + u * (3.0 * c[3] + 4.0 * u * c[4]))) * (gp / (den * den));
+}
+
+void pw92_lsda(double ra, double rb, double& f, double& va, double& vb) {
+  // xc.rs:975-1006
+  f = va = vb = 0.0;
+  const double rho = ra + rb;
+  if (rho < kRhoCutoff) return;
+  const double rs = std::cbrt(3.0 / (4.0 * kPi * rho)), drs = -rs / (3.0 * rho);
+  const double zeta = clampd((ra - rb) / rho, -1.0, 1.0);
+  double e0, de0, e1, de1, mac, dmac;
+  pw92_g(rs, kPwG0, e0, de0);
+  pw92_g(rs, kPwG1, e1, de1);
+  pw92_g(rs, kPwGA, mac, dmac);
+  const double ac = -mac, dac = -dmac;
+  double fz, dfz, fdd0;
+  spin_interp(zeta, fz, dfz, fdd0);
+  const double ifd = 1.0 / fdd0;
+  const double z2 = zeta * zeta, z3 = z2 * zeta, z4 = z2 * z2, om = 1.0 - z4;
+  const double ec = e0 + ac * fz * ifd * om + (e1 - e0) * fz * z4;
+  const double decr = de0 + dac * fz * ifd * om + (de1 - de0) * fz * z4;
+  const double decz = ac * ifd * (dfz * om - 4.0 * z3 * fz) + (e1 - e0) * (dfz * z4 + 4.0 * z3 * fz);
+  f = rho * ec;
+  va = ec + rho * decr * drs + (1.0 - zeta) * decz;
+  vb = ec + rho * decr * drs - (1.0 + zeta) * decz;
+}
+
+void wb97_x_one(double r, double g, const Wb97& P, double& f, double& vr, double& vg) {
+  // xc.rs:1020-1050
+  f = vr = vg = 0.0;
+  if (r < kRhoCutoff) return;
+  double fs, vs;
+  slater_one(r, fs, vs);
+  const double r43 = r * std::cbrt(r), r83 = r43 * r43;
+  const double a = P.omega / (2.0 * std::cbrt(6.0 * kPi * kPi * r));
+  double fa, dfa;
+  atten(a, fa, dfa);
+  const double fsr = fs * fa, vsr = vs * fa + fs * dfa * (-a / (3.0 * r));
+  const double x2 = std::max(g, 0.0) / r83;
+  double gx, dgx;
+  b97_series(0.004, P.cx, x2, gx, dgx);
+  f = fsr * gx;
+  vr = vsr * gx + fsr * dgx * (-(8.0 / 3.0) * x2 / r);
+  vg = fsr * dgx / r83;
+}
+
+XcOut wb97(double ra, double rb, double gaa, double gbb, const Wb97& P) {
+  // xc.rs:1052-1103
+  XcOut o;
+  double fxa, vxa, gxa, fxb, vxb, gxb;
+  wb97_x_one(ra, gaa, P, fxa, vxa, gxa);
+  wb97_x_one(rb, gbb, P, fxb, vxb, gxb);
+  double ft, vta, vtb, fpa, vpa, dm, fpb, vpb;
+  pw92_lsda(ra, rb, ft, vta, vtb);
+  pw92_lsda(ra, 0.0, fpa, vpa, dm);
+  pw92_lsda(0.0, rb, fpb, dm, vpb);
+  const double fpe = ft - fpa - fpb;
+  double xa2 = 0, dxar = 0, dxag = 0, xb2 = 0, dxbr = 0, dxbg = 0;
+  if (ra >= kRhoCutoff) {
+    const double r83 = std::pow(ra, 8.0 / 3.0);
+    xa2 = std::max(gaa, 0.0) / r83; dxar = -(8.0 / 3.0) * xa2 / ra; dxag = 1.0 / r83;
+  }
+  if (rb >= kRhoCutoff) {
+    const double r83 = std::pow(rb, 8.0 / 3.0);
+    xb2 = std::max(gbb, 0.0) / r83; dxbr = -(8.0 / 3.0) * xb2 / rb; dxbg = 1.0 / r83;
+  }
+  double gsa, dgsa, gsb, dgsb, gab, dgab;
+  b97_series(0.2, P.css, xa2, gsa, dgsa);
+  b97_series(0.2, P.css, xb2, gsb, dgsb);
+  b97_series(0.006, P.cab, 0.5 * (xa2 + xb2), gab, dgab);
+  o.f = fxa + fxb + fpa * gsa + fpb * gsb + fpe * gab;
+  o.vra = vxa + vpa * gsa + fpa * dgsa * dxar + (vta - vpa) * gab + fpe * dgab * 0.5 * dxar;
+  o.vrb = vxb + vpb * gsb + fpb * dgsb * dxbr + (vtb - vpb) * gab + fpe * dgab * 0.5 * dxbr;
+  o.vgaa = gxa + fpa * dgsa * dxag + fpe * dgab * 0.5 * dxag;
+  o.vgbb = gxb + fpb * dgsb * dxbg + fpe * dgab * 0.5 * dxbg;
+  return o;
+}
+
 // eval_xc_spin (xc.rs:159-223).  Codes follow the XcFunctional enum order (xc.rs:16-35).
-enum Xc { kSvwn5 = 0, kBlyp = 1, kPbe = 2, kB3lyp = 3, kB3lyp5 = 4, kPbe0 = 5 };
+enum Xc { kSvwn5 = 0, kBlyp = 1, kPbe = 2, kB3lyp = 3, kB3lyp5 = 4, kPbe0 = 5, kCamB3lyp = 6, kWb97x = 7, kWb97xd = 8 };
 
 XcOut eval_xc(int func, double rho_a, double rho_b, double gamma_aa, double gamma_ab, double gamma_bb) {
   XcOut o;
@@ -922,6 +1060,17 @@ XcOut eval_xc(int func, double rho_a, double rho_b, double gamma_aa, double gamm
       o.add(0.75, pbe_x(ra, rb, gaa, gbb));
       o.add(1.00, pbe_c(ra, rb, gaa, gamma_ab, gbb));
       break;
+    case kCamB3lyp: {  // xc.rs:214-219
+      double fa, va, ga, fb, vb, gb;
+      cam_x_one(ra, gaa, fa, va, ga);
+      cam_x_one(rb, gbb, fb, vb, gb);
+      o.f = fa + fb; o.vra = va; o.vrb = vb; o.vgaa = ga; o.vgbb = gb;
+      o.add(0.19, vwn_c(ra, rb, kVwn5));
+      o.add(0.81, lyp_c(ra, rb, gaa, gamma_ab, gbb));
+      break;
+    }
+    case kWb97x: o = wb97(ra, rb, gaa, gbb, kWb97xParams); break;
+    case kWb97xd: o = wb97(ra, rb, gaa, gbb, kWb97xdParams); break;
   }
   return o;
 }
@@ -1536,6 +1685,9 @@ void orc_ao_hess(void* bp, int npts, const double* xyz, double* out) {
   const Basis& b = *static_cast<Basis*>(bp);
   for (int g = 0; g < npts; ++g) eval_aos_hess_all(b, xyz + 3 * g, out + (size_t)g * 10 * b.n_ao);
 }
+
+// CAM-B3LYP attenuated exchange of one spin (xc.rs:910-944): out = (f, v_rho, v_gamma).
+void orc_cam_x_one(double rho, double gamma, double* out) { cam_x_one(rho, gamma, out[0], out[1], out[2]); }
 
 // eval_xc_spin for arrays of points: in[g][5] -> out[g][6]
 void orc_eval_xc(int func, int npts, const double* in, double* out) {

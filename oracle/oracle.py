@@ -49,7 +49,8 @@ _SIGS = {
     "orc_max_threads": (_I, []),
 }
 
-XC_CODES = {"svwn5": 0, "blyp": 1, "pbe": 2, "b3lyp": 3, "b3lyp5": 4, "pbe0": 5}
+XC_CODES = {"svwn5": 0, "blyp": 1, "pbe": 2, "b3lyp": 3, "b3lyp5": 4, "pbe0": 5, "camb3lyp": 6, "cam-b3lyp": 6,
+            "wb97x": 7, "wb97xd": 8, "wb97x-d": 8}
 LEVELS = {"coarse": 0, "medium": 1, "fine": 2, "ultrafine": 3}
 _BASIS_DIR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "calchem_gb300", "data",
                           "basis")
@@ -185,6 +186,13 @@ def eval_xc(func, inputs):
     x = np.ascontiguousarray(np.atleast_2d(inputs), np.float64)
     out = np.zeros((len(x), 6))
     lib().orc_eval_xc(xc_code(func), len(x), _p(x), _p(out))
+    return out
+
+
+def cam_x_one(rho, gamma):
+    """CAM-B3LYP attenuated exchange of one spin: (f, v_rho, v_gamma)."""
+    out = np.zeros(3)
+    lib().orc_cam_x_one(ctypes.c_double(rho), ctypes.c_double(gamma), _p(out))
     return out
 
 

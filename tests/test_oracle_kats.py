@@ -11,7 +11,7 @@ import pytest
 
 from tests.helpers import distorted_water, make_positive_density, oracle_basis
 
-FUNCS = ["svwn5", "blyp", "pbe", "b3lyp", "b3lyp5", "pbe0"]
+FUNCS = ["svwn5", "blyp", "pbe", "b3lyp", "b3lyp5", "pbe0", "camb3lyp", "wb97x", "wb97xd"]
 
 
 def _dfact(n):
@@ -271,3 +271,15 @@ def test_overlap_is_normalised_and_seeded_density_traces(oracle):
     assert np.max(np.abs(S - S.T)) < 1e-14
     D = workloads.seeded_density_rks(S, 5, 7)
     assert abs(np.trace(D @ S) - 10.0) < 1e-10
+
+
+def test_cam_exchange_matches_70_digit_ityh_reference(oracle):
+    """xc.rs:1110-1140: CAM-B3LYP attenuated exchange of one spin against independent high-precision
+    values (rho_s, gamma_ss) -> (f, v_rho, v_gamma)."""
+    for rho, gam, e, vr, vg in [(0.05, 0.001, -0.010533928866947627, -0.2932000891552038, -0.10900565576558356),
+                                (0.2, 0.1, -0.07507503986684043, -0.4990012926064571, -0.01800971179470531),
+                                (0.001, 0.3, -0.003471498357842851, -0.5447077074153023, -0.005110453550847137)]:
+        got = oracle.cam_x_one(rho, gam)
+        assert abs(got[0] - e) < 1e-12
+        assert abs(got[1] - vr) < 1e-10
+        assert abs(got[2] - vg) < 1e-10
