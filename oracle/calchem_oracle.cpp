@@ -1611,6 +1611,171 @@ int orc_lebedev(int n, double* xyzw) {
 double orc_bragg_slater_bohr(int z) { return bragg_slater_radius_bohr(z); }
 int orc_radial_shell_count(int z, int level) { return radial_shell_count(z, level); }
 
+// ============================================================================
+// XC nuclear gradient (vxc.rs:1769-1912) and the Becke weight derivative (grid.rs:423-584)
+// ============================================================================
+double becke_poly(double x) { return 1.5 * x - 0.5 * x * x * x; }
+double becke_poly_d(double x) { return 1.5 - 1.5 * x * x; }
+
+void becke_step_d(double nu, double& s, double& ds) {
+  // grid.rs:129-140
+  const double x = clampd(nu, -1.0, 1.0);
+  const double f1 = becke_poly(x), d1 = becke_poly_d(x);
+  const double f2 = becke_poly(f1), d2 = becke_poly_d(f1);
+  const double f3 = becke_poly(f2), d3 = becke_poly_d(f2);
+  s = 0.5 * (1.0 - f3);
+  ds = -0.5 * d3 * d2 * d1;
+}
+
+void becke_weight_gradient(int n, const int* z, const double* xyz, int host, const double r[3], double raw_w,
+                           double f_xc, double* grad) {
+  // grid.rs:423-584: derivative of the Becke partition weight P_host / sum_C P_C with respect to every
+  // nucleus except the host (whose term follows from translational invariance), times raw_w f_xc
+  if (n <= 1 || std::fabs(f_xc) < 1e-18 || raw_w == 0.0) return;
+  std::vector<double> dr(n), vr(3 * n), smat((size_t)n * n, 1.0), dsmu((size_t)n * n, 0.0), cell(n, 1.0);
+  for (int c = 0; c < n; ++c) {
+    for (int q = 0; q < 3; ++q) vr[3 * c + q] = r[q] - xyz[3 * c + q];
+    dr[c] = std::sqrt(vr[3 * c] * vr[3 * c] + vr[3 * c + 1] * vr[3 * c + 1] + vr[3 * c + 2] * vr[3 * c + 2]);
+  }
+  for (int c = 0; c < n; ++c)
+    for (int d = c + 1; d < n; ++d) {
+      const double dx = xyz[3 * c] - xyz[3 * d], dy = xyz[3 * c + 1] - xyz[3 * d + 1], dz = xyz[3 * c + 2] - xyz[3 * d + 2];
+      const double rcd = std::sqrt(dx * dx + dy * dy + dz * dz);
+      if (rcd < 1e-14) continue;
+      const double mu = clampd((dr[c] - dr[d]) / rcd, -1.0, 1.0);
+      const double a = becke_asymmetry(z[c], z[d]);
+      double scd, dsdnu;
+      becke_step_d(mu + a * (1.0 - mu * mu), scd, dsdnu);
+      const double dmu = dsdnu * (1.0 - 2.0 * a * mu);
+      smat[(size_t)c * n + d] = scd;
+      smat[(size_t)d * n + c] = 1.0 - scd;
+      dsmu[(size_t)c * n + d] = dmu;
+      dsmu[(size_t)d * n + c] = dmu;
+      cell[c] *= scd;
+      cell[d] *= 1.0 - scd;
+    }
+  double zs = 0.0;
+  for (double v : cell) zs += v;
+  if (zs <= 1e-30) return;
+  const double wn = cell[host] / zs, pref = raw_w * f_xc / zs;
+  auto prod_except = [&](int c, int skip) {
+    const double sv = smat[(size_t)c * n + skip];
+    if (sv > 1e-12) return cell[c] / sv;
+    double pr = 1.0;
+    for (int d = 0; d < n; ++d)
+      if (d != c && d != skip) pr *= smat[(size_t)c * n + d];
+    return pr;
+  };
+  double hacc[3] = {0, 0, 0};
+  for (int a = 0; a < n; ++a) {
+    if (a == host) continue;
+    const double ra = dr[a];
+    if (ra < 1e-14) continue;
+    const double dra[3] = {-vr[3 * a] / ra, -vr[3 * a + 1] / ra, -vr[3 * a + 2] / ra};
+    double dph[3] = {0, 0, 0}, dzs[3] = {0, 0, 0};
+    for (int b = 0; b < n; ++b) {
+      if (b == a) continue;
+      const double v[3] = {xyz[3 * a] - xyz[3 * b], xyz[3 * a + 1] - xyz[3 * b + 1], xyz[3 * a + 2] - xyz[3 * b + 2]};
+      const double rab = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      if (rab < 1e-14) continue;
+      const double mu = clampd((ra - dr[b]) / rab, -1.0, 1.0);
+      const double slope = dsmu[(size_t)a * n + b];
+      if (std::fabs(slope) < 1e-30) continue;
+      const double pa = prod_except(a, b), pb = prod_except(b, a);
+      for (int q = 0; q < 3; ++q) {
+        const double ds = slope * (dra[q] - mu * v[q] / rab) / rab;
+        dzs[q] += pa * ds - pb * ds;
+        if (b == host) dph[q] += -pb * ds;
+      }
+    }
+    for (int q = 0; q < 3; ++q) {
+      const double dw = pref * (dph[q] - wn * dzs[q]);
+      grad[3 * a + q] += dw;
+      hacc[q] -= dw;
+    }
+  }
+  for (int q = 0; q < 3; ++q) grad[3 * host + q] += hacc[q];
+}
+
+void xc_gradient(const Basis& bs, const std::vector<GridPoint>& pts, int n_atoms, const int* z, const double* xyz,
+                 const double* Pa, const double* Pb, int func, double* grad) {
+  // vxc.rs:1769-1900 (xc_nuclear_gradient_cpu), one pass over the points
+  const int n = bs.n_ao;
+  std::fill(grad, grad + 3 * n_atoms, 0.0);
+  if (n_atoms <= 1) return;
+  std::vector<int> atom_of(n);
+  for (const Shell& sh : bs.shells)
+    for (int c = 0; c < sh.ncomp(); ++c) atom_of[sh.ao_offset + c] = sh.atom;
+  std::vector<double> h(10 * (size_t)n), sa(n), sb(n), ga(3 * (size_t)n), gb(3 * (size_t)n);
+  for (const GridPoint& gp : pts) {
+    if (std::fabs(gp.raw_w) < 1e-24) continue;
+    const double r[3] = {gp.x, gp.y, gp.z};
+    eval_aos_hess_all(bs, r, h.data());
+    double ra = 0, rb = 0, gra[3] = {0, 0, 0}, grb[3] = {0, 0, 0};
+    for (int i = 0; i < n; ++i) {
+      double s1 = 0, s2 = 0, a3[3] = {0, 0, 0}, b3[3] = {0, 0, 0};
+      for (int j = 0; j < n; ++j) {
+        const double pa = Pa[(size_t)i * n + j], pb = Pb[(size_t)i * n + j];
+        s1 += pa * h[10 * j];
+        s2 += pb * h[10 * j];
+        for (int q = 0; q < 3; ++q) {
+          a3[q] += pa * h[10 * j + 1 + q];
+          b3[q] += pb * h[10 * j + 1 + q];
+        }
+      }
+      sa[i] = s1;
+      sb[i] = s2;
+      for (int q = 0; q < 3; ++q) {
+        ga[3 * i + q] = a3[q];
+        gb[3 * i + q] = b3[q];
+      }
+      ra += h[10 * i] * s1;
+      rb += h[10 * i] * s2;
+      for (int q = 0; q < 3; ++q) {
+        gra[q] += 2.0 * h[10 * i + 1 + q] * s1;
+        grb[q] += 2.0 * h[10 * i + 1 + q] * s2;
+      }
+    }
+    ra = std::max(ra, 0.0);
+    rb = std::max(rb, 0.0);
+    if (ra + rb < 1e-18) continue;
+    const double gaa = gra[0] * gra[0] + gra[1] * gra[1] + gra[2] * gra[2];
+    const double gab = gra[0] * grb[0] + gra[1] * grb[1] + gra[2] * grb[2];
+    const double gbb = grb[0] * grb[0] + grb[1] * grb[1] + grb[2] * grb[2];
+    const XcOut o = eval_xc(func, ra, rb, gaa, gab, gbb);
+    const double w = gp.w;
+    if (std::fabs(w) > 1e-24) {
+      double ua[3], ub[3];
+      for (int q = 0; q < 3; ++q) {
+        ua[q] = 2.0 * o.vgaa * gra[q] + o.vgab * grb[q];
+        ub[q] = 2.0 * o.vgbb * grb[q] + o.vgab * gra[q];
+      }
+      double sum[3] = {0, 0, 0};
+      static const int hidx[3][3] = {{4, 5, 6}, {5, 7, 8}, {6, 8, 9}};
+      for (int i = 0; i < n; ++i) {
+        const double* hi = h.data() + 10 * i;
+        if (hi[0] == 0 && hi[1] == 0 && hi[2] == 0 && hi[3] == 0 && hi[4] == 0 && hi[5] == 0 && hi[6] == 0 &&
+            hi[7] == 0 && hi[8] == 0 && hi[9] == 0)
+          continue;
+        const double uga = ua[0] * ga[3 * i] + ua[1] * ga[3 * i + 1] + ua[2] * ga[3 * i + 2];
+        const double ugb = ub[0] * gb[3 * i] + ub[1] * gb[3 * i + 1] + ub[2] * gb[3 * i + 2];
+        for (int q = 0; q < 3; ++q) {
+          const double dq = hi[1 + q];
+          const double uha = ua[0] * hi[hidx[q][0]] + ua[1] * hi[hidx[q][1]] + ua[2] * hi[hidx[q][2]];
+          const double uhb = ub[0] * hi[hidx[q][0]] + ub[1] * hi[hidx[q][1]] + ub[2] * hi[hidx[q][2]];
+          const double ta = o.vra * dq * sa[i] + uha * sa[i] + dq * uga;
+          const double tb = o.vrb * dq * sb[i] + uhb * sb[i] + dq * ugb;
+          const double f = -2.0 * w * (ta + tb);
+          grad[3 * atom_of[i] + q] += f;
+          sum[q] += f;
+        }
+      }
+      for (int q = 0; q < 3; ++q) grad[3 * gp.host + q] -= sum[q];
+    }
+    becke_weight_gradient(n_atoms, z, xyz, gp.host, r, gp.raw_w, o.f, grad);
+  }
+}
+
 struct OrcGrid { std::vector<GridPoint> pts; };
 
 void* orc_grid_build(int n_atoms, const int* z, const double* xyz_bohr, int level, int radial_min) {
@@ -1684,6 +1849,13 @@ void orc_ao_grad(void* bp, int npts, const double* xyz, double* out) {
 void orc_ao_hess(void* bp, int npts, const double* xyz, double* out) {
   const Basis& b = *static_cast<Basis*>(bp);
   for (int g = 0; g < npts; ++g) eval_aos_hess_all(b, xyz + 3 * g, out + (size_t)g * 10 * b.n_ao);
+}
+
+// XC nuclear gradient dExc/dR (Eh/Bohr, [n_atoms][3]) at fixed Pa, Pb, for a grid built by
+// orc_grid_build (raw weights and host atoms) of the molecule (z, xyz).
+void orc_xc_gradient(void* bp, void* gp, int n_atoms, const int* z, const double* xyz, const double* Pa,
+                     const double* Pb, int func, double* grad) {
+  xc_gradient(*static_cast<Basis*>(bp), static_cast<OrcGrid*>(gp)->pts, n_atoms, z, xyz, Pa, Pb, func, grad);
 }
 
 // CAM-B3LYP attenuated exchange of one spin (xc.rs:910-944): out = (f, v_rho, v_gamma).

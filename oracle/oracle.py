@@ -47,6 +47,8 @@ _SIGS = {
     "orc_rks_engine_free": (None, [_P]),
     "orc_overlap": (None, [_P, _P]),
     "orc_max_threads": (_I, []),
+    "orc_cam_x_one": (None, [_D, _D, _P]),
+    "orc_xc_gradient": (None, [_P, _P, _I, _P, _P, _P, _P, _I, _P]),
 }
 
 XC_CODES = {"svwn5": 0, "blyp": 1, "pbe": 2, "b3lyp": 3, "b3lyp5": 4, "pbe0": 5, "camb3lyp": 6, "cam-b3lyp": 6,
@@ -189,10 +191,20 @@ def eval_xc(func, inputs):
     return out
 
 
+def xc_gradient(basis, grid, z, xyz_bohr, Pa, Pb, func):
+    """dExc/dR_A at fixed densities, [n_atoms, 3] (xc_nuclear_gradient, vxc.rs:1903-1912)."""
+    z = np.ascontiguousarray(z, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz_bohr, dtype=np.float64)
+    out = np.zeros((len(z), 3))
+    lib().orc_xc_gradient(basis.h, grid.h, len(z), _p(z), _p(xyz), _p(np.ascontiguousarray(Pa, np.float64)),
+                          _p(np.ascontiguousarray(Pb, np.float64)), xc_code(func), _p(out))
+    return out
+
+
 def cam_x_one(rho, gamma):
     """CAM-B3LYP attenuated exchange of one spin: (f, v_rho, v_gamma)."""
     out = np.zeros(3)
-    lib().orc_cam_x_one(ctypes.c_double(rho), ctypes.c_double(gamma), _p(out))
+    lib().orc_cam_x_one(float(rho), float(gamma), _p(out))
     return out
 
 

@@ -283,3 +283,32 @@ def test_cam_exchange_matches_70_digit_ityh_reference(oracle):
         assert abs(got[0] - e) < 1e-12
         assert abs(got[1] - vr) < 1e-10
         assert abs(got[2] - vg) < 1e-10
+
+
+@pytest.mark.parametrize("func", ["svwn5", "pbe", "b3lyp"])
+def test_xc_gradient_matches_finite_differences_with_moving_grid(oracle, func):
+    """vxc.rs:2498-2548: the analytic XC nuclear gradient (AO and Becke-weight terms) equals the
+    central difference of Exc(R +- h) with the grid and basis moving with the atoms (h = 1e-5 Bohr,
+    |ana - fd| < 1e-8), and sums to zero over the atoms (translational invariance, < 1e-12)."""
+    from tests.helpers import distorted_water, make_positive_density
+    mol = distorted_water()
+    sym = [a.symbol for a in mol.atoms]
+    xyz = np.array(mol.coords_bohr)
+    basis = oracle.Basis.from_name("6-31g(d)", sym, xyz)
+    n = basis.n_ao
+    Pa, Pb = make_positive_density(n, 3), make_positive_density(n, 8)
+    grid = oracle.Grid.build(mol.z, xyz, "coarse")
+    ana = oracle.xc_gradient(basis, grid, mol.z, xyz, Pa, Pb, func)
+    assert np.max(np.abs(ana.sum(axis=0))) < 1e-12
+    h = 1e-5
+    for a in range(len(sym)):
+        for q in range(3):
+            e = []
+            for sgn in (1.0, -1.0):
+                x = xyz.copy()
+                x[a, q] += sgn * h
+                b = oracle.Basis.from_name("6-31g(d)", sym, x)
+                g = oracle.Grid.build(mol.z, x, "coarse")
+                e.append(oracle.vxc_uks_points(b, g, Pa, Pb, func)[0])
+            fd = (e[0] - e[1]) / (2 * h)
+            assert abs(ana[a, q] - fd) < 1e-8, (a, q, ana[a, q], fd)
