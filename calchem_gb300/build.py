@@ -27,6 +27,7 @@ CUDA_UNITS = {
     "noalloc.cu": [],
     "mlp.cu": [],
     "fxc.cu": [],
+    "xc_grad.cu": [],
 }
 CXX_UNITS = {"host_prep.cpp": [], "integrals.cpp": []}
 

@@ -83,6 +83,7 @@ struct Entry {
   double* d_fxc_m = nullptr;        // trial matrices / results of host-buffer contractions
   double* d_fxc_v = nullptr;
   int fxc_cap = 0;                  // trial matrices d_fxc_m and d_fxc_v hold
+  std::vector<int> h_host;          // host atom of every uploaded point (reference-layout uploads)
   std::vector<int> h_orig;          // caller's index of every uploaded point (empty: identity)
   int n_orig = 0;                   // points the caller passed (calchem_xc_upload_points*)
 
@@ -338,6 +339,8 @@ int upload_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_pri
     soa[3 * (size_t)n_pts + g] = h_w ? h_w[g] : 0.0;
   }
   e->has_w = h_w != nullptr;
+  e->h_host.resize(n_pts);
+  for (int g = 0; g < n_pts; ++g) e->h_host[g] = h_pts[g].host_atom;
   // float-pair copies of the basis constants: hi = float(x), lo = float(x - hi)
   std::vector<float4> pf(n_prims);
   for (int i = 0; i < n_prims; ++i) {
@@ -604,6 +607,102 @@ int grid_build_impl(int n_atoms, const int* z, const double* xyz_bohr, const std
   return 0;
 }
 
+// Device buffers of one gradient evaluation, freed on every return path.
+struct GradBufs {
+  double *pa = nullptr, *pb = nullptr, *wxc = nullptr, *raw = nullptr, *xyz = nullptr, *inv = nullptr,
+         *aij = nullptr, *part = nullptr, *slab = nullptr, *grad = nullptr;
+  int *host = nullptr, *ao_atom = nullptr, *counter = nullptr;
+  ~GradBufs() {
+    void* ptrs[] = {pa, pb, wxc, raw, xyz, inv, aij, part, slab, grad, host, ao_atom, counter};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+  }
+};
+
+// Runs the gradient kernel on an uploaded single-molecule grid.  xc >= 0: fused form (h_raw and
+// the atoms' z / xyz used); xc < 0: drop-in form with h_wxc.  host_up: host atom per uploaded
+// point.  Returns 0, -1 (arguments), -3 (memory limit), -4 (allocation) or -5 (CUDA).
+int gradient_run(Entry& e, int xc, bool closed, const double* h_pa, const double* h_pb, const double* h_wxc,
+                 const double* h_raw, const int* host_up, int n_atoms, const int* z, const double* xyz,
+                 double* h_grad, size_t mem_limit) {
+  const int n = e.n_ao;
+  std::vector<AoShellGpu> sh(e.n_shells);
+  if (cudaMemcpy(sh.data(), e.d_shells, sh.size() * sizeof(AoShellGpu), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -5;
+  std::vector<int> ao_atom(n, 0);
+  for (const AoShellGpu& a : sh) {
+    if (a.atom_index < 0 || a.atom_index >= n_atoms) return -1;
+    for (int c = 0; c < a.n_funcs; ++c) ao_atom[a.ao_offset + c] = a.atom_index;
+  }
+  for (int g = 0; g < e.n_pts; ++g)
+    if (host_up[g] < 0 || host_up[g] >= n_atoms) return -1;
+  std::vector<double> inv_r, a_ij;
+  if (xc >= 0) becke_tables(n_atoms, z, xyz, inv_r, a_ij);
+  const size_t nn = (size_t)n * n, na3 = 3 * (size_t)n_atoms;
+  const int n_ctas = std::max(1, std::min(e.n_batches, g_sm_count));
+  const size_t slab_stride = grad_slab_doubles(e.max_m, n_atoms);
+  size_t total = nn * sizeof(double) * (closed ? 1 : 2) + (size_t)e.n_pts * (xc < 0 ? 8 : 1) * sizeof(double) +
+                 (size_t)e.n_pts * sizeof(int) + (size_t)n * sizeof(int) + (inv_r.size() * 2 + na3) * sizeof(double) +
+                 ((size_t)e.n_batches + 1) * na3 * sizeof(double) + slab_stride * n_ctas * sizeof(double) + 64;
+  if (total > mem_limit) return -3;
+  GradBufs B;
+  bool ok = dalloc(&B.pa, nn) && (closed || dalloc(&B.pb, nn)) && dalloc(&B.host, e.n_pts) &&
+            dalloc(&B.ao_atom, n) && dalloc(&B.part, (size_t)e.n_batches * na3) && dalloc(&B.grad, na3) &&
+            dalloc(&B.slab, slab_stride * n_ctas) && dalloc(&B.counter, 1) &&
+            (xc < 0 ? dalloc(&B.wxc, (size_t)e.n_pts * 8)
+                    : dalloc(&B.raw, e.n_pts) && dalloc(&B.xyz, na3) && dalloc(&B.inv, inv_r.size()) &&
+                          dalloc(&B.aij, a_ij.size()));
+  if (!ok) {
+    cudaGetLastError();
+    return -4;
+  }
+  cudaStream_t st = e.stream;
+  ok = cudaMemcpyAsync(B.pa, h_pa, nn * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+       (closed || cudaMemcpyAsync(B.pb, h_pb, nn * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess) &&
+       cudaMemcpyAsync(B.host, host_up, (size_t)e.n_pts * sizeof(int), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+       cudaMemcpyAsync(B.ao_atom, ao_atom.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, st) ==
+           cudaSuccess &&
+       cudaMemsetAsync(B.counter, 0, sizeof(int), st) == cudaSuccess;
+  if (ok && xc < 0)
+    ok = cudaMemcpyAsync(B.wxc, h_wxc, (size_t)e.n_pts * 8 * sizeof(double), cudaMemcpyHostToDevice, st) ==
+         cudaSuccess;
+  if (ok && xc >= 0)
+    ok = cudaMemcpyAsync(B.raw, h_raw, (size_t)e.n_pts * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+         cudaMemcpyAsync(B.xyz, xyz, na3 * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+         cudaMemcpyAsync(B.inv, inv_r.data(), inv_r.size() * sizeof(double), cudaMemcpyHostToDevice, st) ==
+             cudaSuccess &&
+         cudaMemcpyAsync(B.aij, a_ij.data(), a_ij.size() * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess;
+  if (!ok) return -5;
+  GradArgs A{};
+  A.xc = xc;
+  A.closed = closed ? 1 : 0;
+  A.Pa = B.pa;
+  A.Pb = closed ? B.pa : B.pb;
+  A.wxc = B.wxc;
+  A.raw_w = B.raw;
+  A.host = B.host;
+  A.ao_atom = B.ao_atom;
+  A.xyz = B.xyz;
+  A.inv_r = B.inv;
+  A.a_ij = B.aij;
+  A.n_atoms = n_atoms;
+  A.max_m = e.max_m;
+  A.part = B.part;
+  A.counter = B.counter;
+  A.slab = B.slab;
+  A.slab_stride = slab_stride;
+  if (e.profiling) cudaEventRecord(e.ev0, st);
+  if (launch_xc_grad(dev_grid(e), A, n_ctas, st) != cudaSuccess ||
+      launch_grad_reduce(B.part, e.n_batches, n_atoms, B.grad, st) != cudaSuccess)
+    return -5;
+  if (e.profiling) cudaEventRecord(e.ev1, st);
+  e.last_launches = 2;
+  if (cudaMemcpyAsync(h_grad, B.grad, na3 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return -5;
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -664,6 +763,21 @@ int calchem_cuda_vxc_accum(uint64_t grid_id, const double* h_wv_in, double* h_vx
     return -5;
   std::memcpy(h_vxc_out, e->h_stage, nn * sizeof(double));
   return 0;
+}
+
+int calchem_cuda_vxc_grad_force(uint64_t grid_id, const double* h_pa, const double* h_pb, int is_rks,
+                                const double* h_wxc_in, double* h_grad_out, int n_pts, int n_ao, int n_atoms,
+                                size_t memory_limit_bytes) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (grid_id == 0 || !h_pa || (!is_rks && !h_pb) || !h_wxc_in || !h_grad_out || n_pts <= 0 || n_ao <= 0 ||
+      n_atoms <= 0 || n_atoms > grad_max_atoms())
+    return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e || e->n_mols != 1 || e->n_pts != n_pts || e->n_ao != n_ao || (int)e->h_host.size() != n_pts) return -2;
+  if (int rc0 = ensure_ws(*e)) return rc0;
+  return gradient_run(*e, -1, is_rks != 0, h_pa, h_pb, h_wxc_in, nullptr, e->h_host.data(), n_atoms, nullptr,
+                      nullptr, h_grad_out, memory_limit_bytes ? memory_limit_bytes : SIZE_MAX);
 }
 
 int calchem_cuda_vxc_release(uint64_t grid_id) {
@@ -1037,6 +1151,32 @@ int calchem_xc_fxc_contract(uint64_t grid_id, int triplet, const double* h_m, in
       cudaStreamSynchronize(e->stream) != cudaSuccess)
     return -5;
   return st != 0 ? -7 : 0;
+}
+
+int calchem_xc_nuclear_gradient(uint64_t grid_id, int xc_code, int n_atoms, const int* z, const double* xyz_bohr,
+                                const double* h_raw_w, const int* h_host_atom, int n_grid_pts, const double* h_pa,
+                                const double* h_pb, double* h_grad_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (grid_id == 0 || !z || !xyz_bohr || !h_raw_w || !h_host_atom || !h_pa || !h_grad_out || n_atoms <= 0 ||
+      n_atoms > grad_max_atoms() || !valid_xc(xc_code))
+    return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e || e->n_mols != 1 || !e->has_w) return -2;
+  const int n_caller = e->h_orig.empty() ? e->n_pts : e->n_orig;
+  if (n_grid_pts != n_caller) return -2;
+  std::fill(h_grad_out, h_grad_out + 3 * (size_t)n_atoms, 0.0);
+  if (n_atoms == 1) return 0;  // translational invariance: no gradient for one atom (vxc.rs:1922-1924)
+  if (int rc0 = ensure_ws(*e)) return rc0;
+  std::vector<double> raw(e->n_pts);
+  std::vector<int> host(e->n_pts);
+  for (int g = 0; g < e->n_pts; ++g) {
+    const int o = e->h_orig.empty() ? g : e->h_orig[g];
+    raw[g] = h_raw_w[o];
+    host[g] = h_host_atom[o];
+  }
+  return gradient_run(*e, xc_code, h_pb == nullptr, h_pa, h_pb, nullptr, raw.data(), host.data(), n_atoms, z,
+                      xyz_bohr, h_grad_out, SIZE_MAX);
 }
 
 int calchem_xc_group_create(const uint64_t* member_ids, int n_members, uint64_t group_id, size_t memory_limit_bytes) {

@@ -91,4 +91,29 @@ struct EvalArgs {
   const double* fxc_coef;
 };
 
+// XC nuclear gradient (xc_grad.cu).  xc >= 0: fused form (densities, functional, AO and Becke
+// terms); xc < 0: drop-in form, per-point coefficients wxc[8 g ..] = (w v_rho_a, w u_a, w v_rho_b,
+// w u_b) from the caller and the AO term only.
+constexpr int kMaxGradAtoms = 4096;
+
+struct GradArgs {
+  int xc;
+  int closed;              // beta density = alpha density (Pb unused)
+  const double* Pa;        // spin densities (n x n)
+  const double* Pb;
+  const double* wxc;       // drop-in form: 8 per point
+  const double* raw_w;     // per point: weight before the Becke partition (fused form)
+  const int* host;         // per point: host atom
+  const int* ao_atom;      // per AO: atom of its shell
+  const double* xyz;       // atoms, Bohr (3 n_atoms)
+  const double* inv_r;     // n_atoms^2 inverse distances (0: coincident)
+  const double* a_ij;      // n_atoms^2 Becke size adjustments
+  int n_atoms;
+  int max_m;
+  double* part;            // [batch][atom][3] partial sums
+  int* counter;            // work-queue head (zeroed by the caller)
+  double* slab;            // per-CTA scratch
+  size_t slab_stride;      // doubles per CTA
+};
+
 }  // namespace cxc

@@ -29,6 +29,13 @@ cudaError_t launch_mixed_prepare(const double* P, int n_total, const int* mol_n,
 // TD-DFT kernel coefficients per point (fxc.cu): rho_grad [n][4] of the total density -> out [n][11].
 cudaError_t launch_fxc_coef(const double* rho_grad, const double* w, int n_pts, int code, double* out,
                             cudaStream_t st);
+// XC nuclear gradient (xc_grad.cu): per-CTA scratch, shared memory, the persistent kernel and the
+// batch-ordered sum of its [batch][atom][3] partials into grad.
+size_t grad_slab_doubles(int max_m, int n_atoms);
+size_t grad_smem_bytes(int n_atoms);
+int grad_max_atoms();
+cudaError_t launch_xc_grad(const DevGrid& G, const GradArgs& A, int n_ctas, cudaStream_t st);
+cudaError_t launch_grad_reduce(const double* part, int n_batches, int n_atoms, double* grad, cudaStream_t st);
 // Dynamic shared-memory limits of the persistent kernels, set once per process (the launchers call
 // these; a graph capture calls them first so that no attribute is set while capturing).
 cudaError_t fp64_set_attributes();

@@ -101,6 +101,21 @@ class GpuVxcGrid:
             self.grid_id, _native.ptr(w), _native.ptr(out), self.n_pts, self.n_ao))
         return out
 
+    def eval_grad_force(self, pa, pb, is_rks, wxc, n_atoms, memory_limit=None) -> np.ndarray:
+        """AO part of the XC nuclear gradient for per-point coefficients wxc [n_pts][8] =
+        (w v_rho_a, w u_a, w v_rho_b, w u_b) (GpuVxcGrid::eval_grad_force, lib.rs:1308-1352);
+        returns [n_atoms][3]."""
+        lib = _native.load()
+        Pa = _as_matrix(pa, self.n_ao)
+        Pb = Pa if is_rks else _as_matrix(pb, self.n_ao)
+        w = np.ascontiguousarray(wxc, dtype=np.float64).reshape(self.n_pts, 8)
+        out = np.zeros((int(n_atoms), 3), dtype=np.float64)
+        lim = resolve_gpu_memory_limit() if memory_limit is None else int(memory_limit)
+        _native.check("calchem_cuda_vxc_grad_force", lib.calchem_cuda_vxc_grad_force(
+            self.grid_id, _native.ptr(Pa), _native.ptr(Pb), int(bool(is_rks)), _native.ptr(w), _native.ptr(out),
+            self.n_pts, self.n_ao, int(n_atoms), lim))
+        return out
+
     def release(self):
         if self.grid_id:
             _native.load().calchem_cuda_vxc_release(self.grid_id)
@@ -178,6 +193,24 @@ class _EngineBase:
     def last_launch_count(self) -> int:
         return int(_native.load().calchem_xc_last_launch_count(self.grid_id))
 
+    def nuclear_gradient(self, mol, grid, func, pa, pb=None) -> np.ndarray:
+        """dExc/dR [n_atoms][3] (Eh/Bohr) at fixed spin densities on this engine's grid, which must be
+        the grid it was built from (calchem_xc_nuclear_gradient).  pb = None: closed shell (beta =
+        alpha; pass P_total / 2)."""
+        lib = _native.load()
+        Pa = _as_matrix(pa, self.n_ao)
+        Pb = None if pb is None else _as_matrix(pb, self.n_ao)
+        z = np.ascontiguousarray(mol.z, dtype=np.int32)
+        xyz = np.ascontiguousarray(mol.coords_bohr, dtype=np.float64)
+        raw = np.ascontiguousarray(grid.raw_weight, dtype=np.float64)
+        host = np.ascontiguousarray(grid.host_atom, dtype=np.int32)
+        out = np.zeros((len(z), 3), dtype=np.float64)
+        _native.check("calchem_xc_nuclear_gradient", lib.calchem_xc_nuclear_gradient(
+            self.grid_id, _xc_code(func), len(z), _native.ptr(z), _native.ptr(xyz), _native.ptr(raw),
+            _native.ptr(host), len(raw), _native.ptr(Pa), None if Pb is None else _native.ptr(Pb), _native.ptr(out)))
+        self.gpu_kernel_invocations += self.last_launch_count()
+        return out
+
     def close(self):
         if self.grid_id:
             _native.load().calchem_cuda_vxc_release(self.grid_id)
@@ -244,6 +277,32 @@ def evaluate_vxc_uks(basis, grid, func, pa, pb, precision="fp64"):
         return eng.evaluate(basis, grid, func, pa, pb)
     finally:
         eng.close()
+
+
+def xc_nuclear_gradient_with_gpu(mol, basis, grid, func, pa, pb, use_gpu=True):
+    """xc_nuclear_gradient_with_gpu (vxc.rs:2030-2333): (grad [n_atoms][3], gpu_kernel_invocations,
+    gpu_fallback_invocations).  Equal pa and pb are treated as a closed shell, as the reference does
+    (is_rks = pa == pb).  There is no CPU path: use_gpu=False raises."""
+    if not use_gpu:
+        raise NotImplementedError("calchem_gb300 evaluates the XC gradient on the GPU only; there is no CPU path")
+    n_atoms = len(mol.z)
+    if n_atoms <= 1 or basis.n_ao == 0 or len(grid.xyzw) == 0:
+        return np.zeros((n_atoms, 3)), 0, 0
+    pa = _as_matrix(pa, basis.n_ao)
+    pb = _as_matrix(pb, basis.n_ao)
+    closed = pa is pb or np.array_equal(pa, pb)
+    eng = UksVxcEngine(basis, grid, True, "fp64")
+    try:
+        g = eng.nuclear_gradient(mol, grid, func, pa, None if closed else pb)
+        return g, eng.gpu_kernel_invocations, 0
+    finally:
+        eng.close()
+
+
+def xc_nuclear_gradient(mol, basis, grid, func, pa, pb):
+    """xc_nuclear_gradient (vxc.rs:1903-1912): dExc/dR_A at fixed spin densities pa, pb (closed
+    shell: pa = pb = P_total / 2), in Eh/Bohr, [n_atoms][3]."""
+    return xc_nuclear_gradient_with_gpu(mol, basis, grid, func, pa, pb, True)[0]
 
 
 class VxcGroup:

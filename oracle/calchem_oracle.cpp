@@ -1698,8 +1698,9 @@ void becke_weight_gradient(int n, const int* z, const double* xyz, int host, con
 }
 
 void xc_gradient(const Basis& bs, const std::vector<GridPoint>& pts, int n_atoms, const int* z, const double* xyz,
-                 const double* Pa, const double* Pb, int func, double* grad) {
-  // vxc.rs:1769-1900 (xc_nuclear_gradient_cpu), one pass over the points
+                 const double* Pa, const double* Pb, int func, int parts, double* grad) {
+  // vxc.rs:1769-1900 (xc_nuclear_gradient_cpu), one pass over the points; parts: 1 = AO terms
+  // (with the host-atom term), 2 = Becke weight term, 3 = both
   const int n = bs.n_ao;
   std::fill(grad, grad + 3 * n_atoms, 0.0);
   if (n_atoms <= 1) return;
@@ -1744,7 +1745,7 @@ void xc_gradient(const Basis& bs, const std::vector<GridPoint>& pts, int n_atoms
     const double gbb = grb[0] * grb[0] + grb[1] * grb[1] + grb[2] * grb[2];
     const XcOut o = eval_xc(func, ra, rb, gaa, gab, gbb);
     const double w = gp.w;
-    if (std::fabs(w) > 1e-24) {
+    if ((parts & 1) && std::fabs(w) > 1e-24) {
       double ua[3], ub[3];
       for (int q = 0; q < 3; ++q) {
         ua[q] = 2.0 * o.vgaa * gra[q] + o.vgab * grb[q];
@@ -1772,7 +1773,7 @@ void xc_gradient(const Basis& bs, const std::vector<GridPoint>& pts, int n_atoms
       }
       for (int q = 0; q < 3; ++q) grad[3 * gp.host + q] -= sum[q];
     }
-    becke_weight_gradient(n_atoms, z, xyz, gp.host, r, gp.raw_w, o.f, grad);
+    if (parts & 2) becke_weight_gradient(n_atoms, z, xyz, gp.host, r, gp.raw_w, o.f, grad);
   }
 }
 
@@ -1788,6 +1789,15 @@ void* orc_grid_from_points(int n, const double* xyzw, const int* host) {
   auto* g = new OrcGrid;
   g->pts.resize(n);
   for (int i = 0; i < n; ++i) g->pts[i] = {xyzw[4 * i], xyzw[4 * i + 1], xyzw[4 * i + 2], xyzw[4 * i + 3], 0.0, host[i]};
+  return g;
+}
+
+// As orc_grid_from_points with the weights before the Becke partition (for the gradient).
+void* orc_grid_from_points_raw(int n, const double* xyzw, const double* raw_w, const int* host) {
+  auto* g = new OrcGrid;
+  g->pts.resize(n);
+  for (int i = 0; i < n; ++i)
+    g->pts[i] = {xyzw[4 * i], xyzw[4 * i + 1], xyzw[4 * i + 2], xyzw[4 * i + 3], raw_w[i], host[i]};
   return g;
 }
 
@@ -1854,8 +1864,8 @@ void orc_ao_hess(void* bp, int npts, const double* xyz, double* out) {
 // XC nuclear gradient dExc/dR (Eh/Bohr, [n_atoms][3]) at fixed Pa, Pb, for a grid built by
 // orc_grid_build (raw weights and host atoms) of the molecule (z, xyz).
 void orc_xc_gradient(void* bp, void* gp, int n_atoms, const int* z, const double* xyz, const double* Pa,
-                     const double* Pb, int func, double* grad) {
-  xc_gradient(*static_cast<Basis*>(bp), static_cast<OrcGrid*>(gp)->pts, n_atoms, z, xyz, Pa, Pb, func, grad);
+                     const double* Pb, int func, int parts, double* grad) {
+  xc_gradient(*static_cast<Basis*>(bp), static_cast<OrcGrid*>(gp)->pts, n_atoms, z, xyz, Pa, Pb, func, parts, grad);
 }
 
 // CAM-B3LYP attenuated exchange of one spin (xc.rs:910-944): out = (f, v_rho, v_gamma).

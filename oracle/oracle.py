@@ -48,7 +48,8 @@ _SIGS = {
     "orc_overlap": (None, [_P, _P]),
     "orc_max_threads": (_I, []),
     "orc_cam_x_one": (None, [_D, _D, _P]),
-    "orc_xc_gradient": (None, [_P, _P, _I, _P, _P, _P, _P, _I, _P]),
+    "orc_xc_gradient": (None, [_P, _P, _I, _P, _P, _P, _P, _I, _I, _P]),
+    "orc_grid_from_points_raw": (_P, [_I, _P, _P, _P]),
 }
 
 XC_CODES = {"svwn5": 0, "blyp": 1, "pbe": 2, "b3lyp": 3, "b3lyp5": 4, "pbe0": 5, "camb3lyp": 6, "cam-b3lyp": 6,
@@ -103,10 +104,13 @@ class Grid:
         return cls(lib().orc_grid_build(len(z), _p(z), _p(xyz), lv, int(radial_min)))
 
     @classmethod
-    def from_points(cls, xyzw, host=None):
+    def from_points(cls, xyzw, host=None, raw_w=None):
         xyzw = np.ascontiguousarray(xyzw, dtype=np.float64).reshape(-1, 4)
         host = np.zeros(len(xyzw), np.int32) if host is None else np.ascontiguousarray(host, dtype=np.int32)
-        return cls(lib().orc_grid_from_points(len(xyzw), _p(xyzw), _p(host)))
+        if raw_w is None:
+            return cls(lib().orc_grid_from_points(len(xyzw), _p(xyzw), _p(host)))
+        raw_w = np.ascontiguousarray(raw_w, dtype=np.float64)
+        return cls(lib().orc_grid_from_points_raw(len(xyzw), _p(xyzw), _p(raw_w), _p(host)))
 
     def __len__(self):
         return lib().orc_grid_size(self.h)
@@ -191,13 +195,14 @@ def eval_xc(func, inputs):
     return out
 
 
-def xc_gradient(basis, grid, z, xyz_bohr, Pa, Pb, func):
-    """dExc/dR_A at fixed densities, [n_atoms, 3] (xc_nuclear_gradient, vxc.rs:1903-1912)."""
+def xc_gradient(basis, grid, z, xyz_bohr, Pa, Pb, func, parts=3):
+    """dExc/dR [n_atoms][3] at fixed spin densities (vxc.rs:1769-1912); parts 1 = AO terms only,
+    2 = Becke weight term only, 3 = both."""
     z = np.ascontiguousarray(z, dtype=np.int32)
     xyz = np.ascontiguousarray(xyz_bohr, dtype=np.float64)
     out = np.zeros((len(z), 3))
     lib().orc_xc_gradient(basis.h, grid.h, len(z), _p(z), _p(xyz), _p(np.ascontiguousarray(Pa, np.float64)),
-                          _p(np.ascontiguousarray(Pb, np.float64)), xc_code(func), _p(out))
+                          _p(np.ascontiguousarray(Pb, np.float64)), xc_code(func), int(parts), _p(out))
     return out
 
 

@@ -37,6 +37,7 @@ def reference_layout(basis, grid):
     centers = np.array([s["center"] for s in sh])
     rcut = np.sqrt(sh["r2_cutoff"])
     xyzw = grid.xyzw
+    hosts = getattr(grid, "host_atom", None)
     pts, ws, off, cs = [], [], [0], []
     bid = 0
     for s0 in range(0, len(xyzw), 128):
@@ -54,8 +55,9 @@ def reference_layout(basis, grid):
             continue
         cs.extend(int(i) for i in cand)
         off.append(len(cs))
-        for p in c:
-            pts.append((p[0], p[1], p[2], bid, 0))
+        for k in np.where(keep)[0]:
+            p = chunk[k]
+            pts.append((p[0], p[1], p[2], bid, 0 if hosts is None else int(hosts[s0 + k])))
             ws.append(p[3])
         bid += 1
     return (np.array(pts, dtype=_native.GRID_PT), np.array(ws), np.array(off, np.int32), np.array(cs, np.int32))
