@@ -56,9 +56,10 @@ def parse():
     ap.add_argument("--grid", default="learned", choices=["learned", "fine"],
                     help="learned: the MLP-pruned grid with the Fine-grid judge (headline workload only)")
     ap.add_argument("--workload", default="octane_b3lyp",
-                    choices=["octane_b3lyp", "c54h18_pbe0_uks", "water_clusters_pbe"],
+                    choices=["octane_b3lyp", "c54h18_pbe0_uks", "water_clusters_pbe", "octane_b3lyp_gradient"],
                     help="octane_b3lyp is the headline; the others report the same line for the UKS flake "
-                         "and the 64-cluster batched launch")
+                         "and the 64-cluster batched launch; octane_b3lyp_gradient times the XC nuclear "
+                         "gradient (its own metric) on the headline molecule")
     return ap.parse_args()
 
 
@@ -524,10 +525,98 @@ def run_ours(args):
     return 0
 
 
+GRADIENT_METRIC = "XC nuclear gradient dExc/dR ms on 1 GB300 (FP64, fixed density)"
+
+
+def cpu_gradient_sample(mol, basis, grid, Pa, func, n_sample=4000):
+    """The oracle's restatement of xc_nuclear_gradient_cpu (vxc.rs:1914-2024) on every k-th point of
+    the grid, scaled to the whole grid: (ms, sample description)."""
+    from oracle import oracle as O
+
+    stride = max(1, len(grid) // n_sample)
+    idx = np.arange(0, len(grid), stride)
+    og = O.Grid.from_points(grid.xyzw[idx], grid.host_atom[idx], grid.raw_weight[idx])
+    ob = O.Basis.from_name("6-31g(d,p)", [a.symbol for a in mol.atoms], mol.coords_bohr)
+    O.xc_gradient(ob, og, mol.z, mol.coords_bohr, Pa, Pa, func)  # warm-up (tables)
+    t0 = time.perf_counter()
+    O.xc_gradient(ob, og, mol.z, mol.coords_bohr, Pa, Pa, func)
+    t = time.perf_counter() - t0
+    ms = t * 1e3 * len(grid) / len(idx)
+    return ms, (f"oracle xc_gradient (per point: AO Hessians, P contractions, functional, Becke derivative; "
+                f"1 thread) on every {stride}-th point ({len(idx)} of {len(grid)}), scaled to the full grid")
+
+
+def run_gradient(args):
+    """One step = one XC nuclear gradient (calchem_xc_nuclear_gradient) of the headline workload on
+    its Fine grid at the seeded closed-shell density (P_alpha = D / 2)."""
+    import torch
+
+    from calchem_gb300 import GridLevel, MolecularGrid, RksVxcEngine
+
+    ws, rank, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    mol, basis, D = build_inputs()
+    grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
+    eng = RksVxcEngine(basis, grid)
+    eng.set_profiling(True)
+    Pa = 0.5 * D
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(max(3, args.warmup)):
+        g = eng.nuclear_gradient(mol, grid, "b3lyp", Pa)
+    n0 = eng.gpu_kernel_invocations
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    kern, wall = [], []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g = eng.nuclear_gradient(mol, grid, "b3lyp", Pa)
+        wall.append((time.perf_counter() - t0) * 1e3)
+        kern.append(eng.last_kernel_ms())
+    clk = clocks.stop()
+    launches = eng.gpu_kernel_invocations - n0
+    n_batches, sum_m2n, _, max_m = eng.plan_stats()
+    flops = 4.0 * sum_m2n  # T = P Phi and Y = P Psi, 2 m^2 n each (closed shell)
+    kms = statistics.mean(kern)
+    peak = fp64_peak_tflops(torch, dev)
+    achieved = flops / (kms * 1e-3) / 1e12
+    n = basis.n_ao
+    line = {
+        "metric": GRADIENT_METRIC, "value": round(kms, 4), "unit": "ms", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(kms, 4), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD + "; XC nuclear gradient at P_alpha = D / 2", "name": args.workload,
+                   "grid_points": len(grid), "batches": n_batches, "max_m": max_m, "atoms": len(mol.z),
+                   "l2": "flushed before every timed step (256 MiB write)"},
+        "roofline": {"bound": "fp64 pipe", "achieved": round(achieved, 4), "peak": round(peak, 3),
+                     "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "kernel": "xc_grad_kernel + grad_reduce_kernel", "kernel_ms": round(kms, 4),
+                     "work": f"4*sum(m^2 n) = {flops:.4e} flop of AO contractions per launch (Becke term not "
+                             f"counted)",
+                     "peak_source": "FP64 pipe: cuBLAS DGEMM 4096^3 measured in this run"},
+        "e2e": {"value": round(statistics.mean(wall), 4), "unit": "ms",
+                "h2d_bytes_per_step": n * n * 8 + len(grid) * 12, "d2h_bytes_per_step": len(mol.z) * 24},
+        "gpu_launches": launches, "clocks": clk,
+        "max_abs_grad": float(np.max(np.abs(g))), "sum_over_atoms": float(np.max(np.abs(g.sum(axis=0)))),
+    }
+    if not args.no_cpu_baseline:
+        cms, sample = cpu_gradient_sample(mol, basis, grid, Pa, "b3lyp")
+        line["cpu_baseline"] = {"value": round(cms, 2), "unit": "ms", "cores": 1, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "octane_b3lyp_gradient":
+        return run_gradient(args)
     return run_ours(args)
 
 
