@@ -28,6 +28,7 @@ CUDA_UNITS = {
     "mlp.cu": [],
     "fxc.cu": [],
     "xc_grad.cu": [],
+    "xc_grad_mixed.cu": [],
 }
 CXX_UNITS = {"host_prep.cpp": [], "integrals.cpp": []}
 

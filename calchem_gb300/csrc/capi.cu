@@ -612,8 +612,10 @@ struct GradBufs {
   double *pa = nullptr, *pb = nullptr, *wxc = nullptr, *raw = nullptr, *xyz = nullptr, *inv = nullptr,
          *aij = nullptr, *part = nullptr, *slab = nullptr, *grad = nullptr;
   int *host = nullptr, *ao_atom = nullptr, *counter = nullptr;
+  int2* pairs = nullptr;
+  float2* pair_df = nullptr;
   ~GradBufs() {
-    void* ptrs[] = {pa, pb, wxc, raw, xyz, inv, aij, part, slab, grad, host, ao_atom, counter};
+    void* ptrs[] = {pa, pb, wxc, raw, xyz, inv, aij, part, slab, grad, host, ao_atom, counter, pairs, pair_df};
     for (void* p : ptrs)
       if (p) cudaFree(p);
   }
@@ -622,10 +624,12 @@ struct GradBufs {
 // Runs the gradient kernel on an uploaded single-molecule grid.  xc >= 0: fused form (h_raw and
 // the atoms' z / xyz used); xc < 0: drop-in form with h_wxc.  host_up: host atom per uploaded
 // point.  Returns 0, -1 (arguments), -3 (memory limit), -4 (allocation) or -5 (CUDA).
-int gradient_run(Entry& e, int xc, bool closed, const double* h_pa, const double* h_pb, const double* h_wxc,
-                 const double* h_raw, const int* host_up, int n_atoms, const int* z, const double* xyz,
-                 double* h_grad, size_t mem_limit) {
+int gradient_run(Entry& e, int xc, int precision, bool closed, const double* h_pa, const double* h_pb,
+                 const double* h_wxc, const double* h_raw, const int* host_up, int n_atoms, const int* z,
+                 const double* xyz, double* h_grad, size_t mem_limit) {
   const int n = e.n_ao;
+  const bool mixed = precision == CALCHEM_XC_MIXED;
+  if (mixed && (xc < 0 || e.max_m > grad_mixed_max_m())) return -2;
   std::vector<AoShellGpu> sh(e.n_shells);
   if (cudaMemcpy(sh.data(), e.d_shells, sh.size() * sizeof(AoShellGpu), cudaMemcpyDeviceToHost) != cudaSuccess)
     return -5;
@@ -637,21 +641,49 @@ int gradient_run(Entry& e, int xc, bool closed, const double* h_pa, const double
   for (int g = 0; g < e.n_pts; ++g)
     if (host_up[g] < 0 || host_up[g] >= n_atoms) return -1;
   std::vector<double> inv_r, a_ij;
-  if (xc >= 0) becke_tables(n_atoms, z, xyz, inv_r, a_ij);
+  std::vector<int2> pairs;
+  std::vector<float2> pair_df;  // per ordered pair: 1 / R, a, (R_a - R_b) / R as float pairs
+  if (xc >= 0) {
+    becke_tables(n_atoms, z, xyz, inv_r, a_ij);
+    for (int c = 0; c < n_atoms; ++c)
+      for (int d = c + 1; d < n_atoms; ++d) pairs.push_back(make_int2(c, d));
+    auto fpair = [](double v) {
+      const float hi = (float)v;
+      return make_float2(hi, (float)(v - (double)hi));
+    };
+    pair_df.resize((size_t)n_atoms * n_atoms * 5);
+    for (int a = 0; a < n_atoms; ++a)
+      for (int b = 0; b < n_atoms; ++b) {
+        const size_t k = (size_t)a * n_atoms + b;
+        const double inv = inv_r[k];
+        pair_df[5 * k] = fpair(inv);
+        pair_df[5 * k + 1] = fpair(a_ij[k]);
+        for (int q = 0; q < 3; ++q) pair_df[5 * k + 2 + q] = fpair((xyz[3 * a + q] - xyz[3 * b + q]) * inv);
+      }
+  }
   const size_t nn = (size_t)n * n, na3 = 3 * (size_t)n_atoms;
-  const int n_ctas = std::max(1, std::min(e.n_batches, g_sm_count));
-  const size_t slab_stride = grad_slab_doubles(e.max_m, n_atoms);
+  const size_t slab_stride = mixed ? grad_mixed_slab_doubles(e.max_m, n_atoms) : grad_slab_doubles(e.max_m, n_atoms);
+  // persistent CTAs (one per SM for FP64, two for the tensor-core form), fewer when the per-CTA
+  // scratch (AO planes and the warps' atom-pair tables) would take more than half of the free memory
+  int n_ctas = std::max(1, std::min(e.n_batches, g_sm_count * (mixed ? 2 : 1)));
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+    const size_t fit = free_b / 2 / (slab_stride * sizeof(double));
+    n_ctas = (int)std::max<size_t>(1, std::min<size_t>(n_ctas, fit));
+  }
   size_t total = nn * sizeof(double) * (closed ? 1 : 2) + (size_t)e.n_pts * (xc < 0 ? 8 : 1) * sizeof(double) +
                  (size_t)e.n_pts * sizeof(int) + (size_t)n * sizeof(int) + (inv_r.size() * 2 + na3) * sizeof(double) +
-                 ((size_t)e.n_batches + 1) * na3 * sizeof(double) + slab_stride * n_ctas * sizeof(double) + 64;
+                 ((size_t)e.n_batches + 1) * na3 * sizeof(double) + slab_stride * n_ctas * sizeof(double) +
+                 pairs.size() * sizeof(int2) + pair_df.size() * sizeof(float2) + 64;
   if (total > mem_limit) return -3;
   GradBufs B;
   bool ok = dalloc(&B.pa, nn) && (closed || dalloc(&B.pb, nn)) && dalloc(&B.host, e.n_pts) &&
             dalloc(&B.ao_atom, n) && dalloc(&B.part, (size_t)e.n_batches * na3) && dalloc(&B.grad, na3) &&
-            dalloc(&B.slab, slab_stride * n_ctas) && dalloc(&B.counter, 1) &&
+            dalloc(&B.slab, slab_stride * n_ctas) && dalloc(&B.counter, 2) &&
             (xc < 0 ? dalloc(&B.wxc, (size_t)e.n_pts * 8)
                     : dalloc(&B.raw, e.n_pts) && dalloc(&B.xyz, na3) && dalloc(&B.inv, inv_r.size()) &&
-                          dalloc(&B.aij, a_ij.size()));
+                          dalloc(&B.aij, a_ij.size()) && dalloc(&B.pairs, pairs.size()) &&
+                          dalloc(&B.pair_df, pair_df.size()));
   if (!ok) {
     cudaGetLastError();
     return -4;
@@ -662,7 +694,8 @@ int gradient_run(Entry& e, int xc, bool closed, const double* h_pa, const double
        cudaMemcpyAsync(B.host, host_up, (size_t)e.n_pts * sizeof(int), cudaMemcpyHostToDevice, st) == cudaSuccess &&
        cudaMemcpyAsync(B.ao_atom, ao_atom.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, st) ==
            cudaSuccess &&
-       cudaMemsetAsync(B.counter, 0, sizeof(int), st) == cudaSuccess;
+       cudaMemsetAsync(B.counter, 0, 2 * sizeof(int), st) == cudaSuccess &&
+       (!mixed || cudaMemsetAsync(B.part, 0, (size_t)e.n_batches * na3 * sizeof(double), st) == cudaSuccess);
   if (ok && xc < 0)
     ok = cudaMemcpyAsync(B.wxc, h_wxc, (size_t)e.n_pts * 8 * sizeof(double), cudaMemcpyHostToDevice, st) ==
          cudaSuccess;
@@ -671,7 +704,12 @@ int gradient_run(Entry& e, int xc, bool closed, const double* h_pa, const double
          cudaMemcpyAsync(B.xyz, xyz, na3 * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess &&
          cudaMemcpyAsync(B.inv, inv_r.data(), inv_r.size() * sizeof(double), cudaMemcpyHostToDevice, st) ==
              cudaSuccess &&
-         cudaMemcpyAsync(B.aij, a_ij.data(), a_ij.size() * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess;
+         cudaMemcpyAsync(B.aij, a_ij.data(), a_ij.size() * sizeof(double), cudaMemcpyHostToDevice, st) ==
+             cudaSuccess &&
+         (pairs.empty() || cudaMemcpyAsync(B.pairs, pairs.data(), pairs.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                           st) == cudaSuccess) &&
+         cudaMemcpyAsync(B.pair_df, pair_df.data(), pair_df.size() * sizeof(float2), cudaMemcpyHostToDevice, st) ==
+             cudaSuccess;
   if (!ok) return -5;
   GradArgs A{};
   A.xc = xc;
@@ -685,22 +723,43 @@ int gradient_run(Entry& e, int xc, bool closed, const double* h_pa, const double
   A.xyz = B.xyz;
   A.inv_r = B.inv;
   A.a_ij = B.aij;
+  A.pairs = B.pairs;
+  A.n_pairs = (int)pairs.size();
+  A.pair_df = B.pair_df;
   A.n_atoms = n_atoms;
   A.max_m = e.max_m;
   A.part = B.part;
   A.counter = B.counter;
   A.slab = B.slab;
   A.slab_stride = slab_stride;
+  int launches = 0;
   if (e.profiling) cudaEventRecord(e.ev0, st);
-  if (launch_xc_grad(dev_grid(e), A, n_ctas, st) != cudaSuccess ||
-      launch_grad_reduce(B.part, e.n_batches, n_atoms, B.grad, st) != cudaSuccess)
+  if (mixed) {
+    // split copies of the spin densities for the tensor-core contractions (alpha, then beta)
+    uint2* pk = reinterpret_cast<uint2*>(e.d_mixed_ws);
+    int* fx = reinterpret_cast<int*>(pk + 2 * nn);
+    if (launch_mixed_prepare(B.pa, n, nullptr, nullptr, nullptr, 1, pk, fx, st) != cudaSuccess) return -5;
+    ++launches;
+    if (!closed) {
+      if (launch_mixed_prepare(B.pb, n, nullptr, nullptr, nullptr, 1, pk + nn, fx + n, st) != cudaSuccess) return -5;
+      ++launches;
+    }
+    A.Pa = reinterpret_cast<const double*>(e.d_mixed_ws);
+    A.Pb = nullptr;
+    if (launch_xc_grad_mixed(dev_grid(e), A, n_ctas, B.counter + 1, st) != cudaSuccess) return -5;
+  } else if (launch_xc_grad(dev_grid(e), A, n_ctas, st) != cudaSuccess) {
     return -5;
+  }
+  if (launch_grad_reduce(B.part, e.n_batches, n_atoms, B.grad, st) != cudaSuccess) return -5;
+  launches += 2;
   if (e.profiling) cudaEventRecord(e.ev1, st);
-  e.last_launches = 2;
+  e.last_launches = launches;
+  int status = 0;
   if (cudaMemcpyAsync(h_grad, B.grad, na3 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(&status, B.counter + 1, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return -5;
-  return 0;
+  return status ? -7 : 0;
 }
 
 }  // namespace
@@ -776,7 +835,8 @@ int calchem_cuda_vxc_grad_force(uint64_t grid_id, const double* h_pa, const doub
   Entry* e = find(grid_id);
   if (!e || e->n_mols != 1 || e->n_pts != n_pts || e->n_ao != n_ao || (int)e->h_host.size() != n_pts) return -2;
   if (int rc0 = ensure_ws(*e)) return rc0;
-  return gradient_run(*e, -1, is_rks != 0, h_pa, h_pb, h_wxc_in, nullptr, e->h_host.data(), n_atoms, nullptr,
+  return gradient_run(*e, -1, CALCHEM_XC_FP64, is_rks != 0, h_pa, h_pb, h_wxc_in, nullptr, e->h_host.data(), n_atoms,
+                      nullptr,
                       nullptr, h_grad_out, memory_limit_bytes ? memory_limit_bytes : SIZE_MAX);
 }
 
@@ -1153,12 +1213,13 @@ int calchem_xc_fxc_contract(uint64_t grid_id, int triplet, const double* h_m, in
   return st != 0 ? -7 : 0;
 }
 
-int calchem_xc_nuclear_gradient(uint64_t grid_id, int xc_code, int n_atoms, const int* z, const double* xyz_bohr,
-                                const double* h_raw_w, const int* h_host_atom, int n_grid_pts, const double* h_pa,
-                                const double* h_pb, double* h_grad_out) {
+int calchem_xc_nuclear_gradient(uint64_t grid_id, int xc_code, int precision, int n_atoms, const int* z,
+                                const double* xyz_bohr, const double* h_raw_w, const int* h_host_atom, int n_grid_pts,
+                                const double* h_pa, const double* h_pb, double* h_grad_out) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (grid_id == 0 || !z || !xyz_bohr || !h_raw_w || !h_host_atom || !h_pa || !h_grad_out || n_atoms <= 0 ||
-      n_atoms > grad_max_atoms() || !valid_xc(xc_code))
+      n_atoms > grad_max_atoms() || !valid_xc(xc_code) ||
+      (precision != CALCHEM_XC_FP64 && precision != CALCHEM_XC_MIXED))
     return -1;
   if (!device_ok()) return -3;
   Entry* e = find(grid_id);
@@ -1175,7 +1236,8 @@ int calchem_xc_nuclear_gradient(uint64_t grid_id, int xc_code, int n_atoms, cons
     raw[g] = h_raw_w[o];
     host[g] = h_host_atom[o];
   }
-  return gradient_run(*e, xc_code, h_pb == nullptr, h_pa, h_pb, nullptr, raw.data(), host.data(), n_atoms, z,
+  return gradient_run(*e, xc_code, precision, h_pb == nullptr, h_pa, h_pb, nullptr, raw.data(), host.data(), n_atoms,
+                      z,
                       xyz_bohr, h_grad_out, SIZE_MAX);
 }
 

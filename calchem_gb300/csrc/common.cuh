@@ -94,7 +94,7 @@ struct EvalArgs {
 // XC nuclear gradient (xc_grad.cu).  xc >= 0: fused form (densities, functional, AO and Becke
 // terms); xc < 0: drop-in form, per-point coefficients wxc[8 g ..] = (w v_rho_a, w u_a, w v_rho_b,
 // w u_b) from the caller and the AO term only.
-constexpr int kMaxGradAtoms = 4096;
+constexpr int kMaxGradAtoms = 1024;
 
 struct GradArgs {
   int xc;
@@ -108,6 +108,11 @@ struct GradArgs {
   const double* xyz;       // atoms, Bohr (3 n_atoms)
   const double* inv_r;     // n_atoms^2 inverse distances (0: coincident)
   const double* a_ij;      // n_atoms^2 Becke size adjustments
+  const int2* pairs;       // the atom pairs (c, d), c < d
+  int n_pairs;
+  // per ordered pair (a, b), 5 float pairs (hi, lo): 1 / R_ab, a_ab, (R_a - R_b) / R_ab (the
+  // double-float weight derivative of the tensor-core form)
+  const float2* pair_df;
   int n_atoms;
   int max_m;
   double* part;            // [batch][atom][3] partial sums

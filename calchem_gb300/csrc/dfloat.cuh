@@ -74,6 +74,14 @@ __device__ __forceinline__ df32 df_mul_f(df32 a, float b) {
   return fast_two_sum(p.hi, p.lo);
 }
 
+// a / b (b != 0): the FP32 quotient and one correction from the exact remainder (Dekker).
+__device__ __forceinline__ df32 df_div(df32 a, df32 b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const df32 p = two_prod(q1, b.hi);
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p.hi), p.lo), __fsub_rn(a.lo, __fmul_rn(q1, b.lo)));
+  return fast_two_sum(q1, __fdiv_rn(r, b.hi));
+}
+
 // Exact scaling by a power of two (as long as no underflow/overflow occurs).
 __device__ __forceinline__ df32 df_ldexp(df32 a, int e) { return df32{ldexpf(a.hi, e), ldexpf(a.lo, e)}; }
 

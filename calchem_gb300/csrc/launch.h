@@ -36,6 +36,11 @@ size_t grad_smem_bytes(int n_atoms);
 int grad_max_atoms();
 cudaError_t launch_xc_grad(const DevGrid& G, const GradArgs& A, int n_ctas, cudaStream_t st);
 cudaError_t launch_grad_reduce(const double* part, int n_batches, int n_atoms, double* grad, cudaStream_t st);
+// Tensor-core form of the gradient (xc_grad_mixed.cu): GradArgs.Pa points at the split densities of
+// launch_mixed_prepare (alpha, then beta); part must be zeroed; *status is set on a wait expiry.
+size_t grad_mixed_slab_doubles(int max_m, int n_atoms);
+int grad_mixed_max_m();
+cudaError_t launch_xc_grad_mixed(const DevGrid& G, const GradArgs& A, int n_ctas, int* status, cudaStream_t st);
 // Dynamic shared-memory limits of the persistent kernels, set once per process (the launchers call
 // these; a graph capture calls them first so that no attribute is set while capturing).
 cudaError_t fp64_set_attributes();

@@ -38,6 +38,7 @@
 
 #include "common.cuh"
 #include "dfloat.cuh"
+#include "mixed_ops.cuh"
 #include "tc_ptx.cuh"
 #include "xc_device.cuh"
 
@@ -45,12 +46,12 @@ namespace cxc {
 
 namespace {
 
-constexpr int kMT = 256;              // threads per CTA (two CTAs per SM)
+using namespace mix;
+constexpr int kMT = kThreads;         // threads per CTA (two CTAs per SM)
 constexpr int kGroups = kMT / 128;    // thread groups of 128 (one thread per point in each)
 constexpr int kMaxMixedM = 2048;      // AOs per batch held in shared memory
 constexpr uint32_t kWaitLimit = 1u << 26;
 constexpr uint32_t kTmemCols = 256;
-constexpr int kNc = 64;               // GEMM1 N chunk (AOs) per TMEM accumulator
 constexpr int kRing = 4;              // epilogue bulk-copy buffers in the stage
 constexpr int kRingBytes = 24576;     // one 8-row step: 4 x 4 KB FP32 + 4 x 2 KB BF16
 constexpr int kStageBytes = 98304;    // operand staging area: GEMM1 A 64 KB + B 32 KB; GEMM2 6 x 16 KB
@@ -67,57 +68,6 @@ constexpr int kOffDensInStage = 65536;
 static_assert(kRing * kRingBytes <= kStageBytes, "the epilogue ring lives in the stage");
 static_assert(20 + 8 * kRing + 4 <= 64, "misc area holds the barriers, the TMEM slot and the batch index");
 static_assert(2 * (kSmemBytes + 1024) <= 233472, "two CTAs must fit in one SM's shared memory");
-
-__device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
-  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
-}
-
-// x = hi + mid + lo, each an RN BF16 of the remaining residual; the residuals are exact in FP32.
-__device__ __forceinline__ void split3_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
-  hi = __float2bfloat16_rn(x);
-  const float r1 = x - __bfloat162float(hi);
-  mid = __float2bfloat16_rn(r1);
-  lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
-}
-
-__device__ __forceinline__ void pack8x3(const float* v, uint4& hi, uint4& mid, uint4& lo) {
-  __nv_bfloat16 h[8], m[8], l[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) split3_bf16(v[k], h[k], m[k], l[k]);
-  hi = make_uint4(pack_bf16x2(h[0], h[1]), pack_bf16x2(h[2], h[3]), pack_bf16x2(h[4], h[5]), pack_bf16x2(h[6], h[7]));
-  mid = make_uint4(pack_bf16x2(m[0], m[1]), pack_bf16x2(m[2], m[3]), pack_bf16x2(m[4], m[5]), pack_bf16x2(m[6], m[7]));
-  lo = make_uint4(pack_bf16x2(l[0], l[1]), pack_bf16x2(l[2], l[3]), pack_bf16x2(l[4], l[5]), pack_bf16x2(l[6], l[7]));
-}
-
-// Fixed-point split of |x| < 1 (a double-float hi + lo) into four pieces that are multiples of
-// 2^-7, 2^-15, 2^-23 and 2^-31 with at most 8 significant bits each (exact in BF16); the residual
-// x - (h + m + l + q) is below 2^-32.
-__device__ __forceinline__ void fixsplit4(float xh, float xl, __nv_bfloat16& hi, __nv_bfloat16& mid,
-                                          __nv_bfloat16& lo, __nv_bfloat16& q) {
-  const float h = rintf(xh * 128.f) * (1.f / 128.f);
-  const float r1 = __fadd_rn(__fsub_rn(xh, h), xl);
-  const float m = rintf(r1 * 32768.f) * (1.f / 32768.f);
-  const float r2 = __fsub_rn(r1, m);
-  const float l = rintf(r2 * 8388608.f) * (1.f / 8388608.f);
-  const float r3 = __fsub_rn(r2, l);
-  const float qq = rintf(r3 * 2147483648.f) * (1.f / 2147483648.f);
-  hi = __float2bfloat16_rn(h);
-  mid = __float2bfloat16_rn(m);
-  lo = __float2bfloat16_rn(l);
-  q = __float2bfloat16_rn(qq);
-}
-
-__device__ __forceinline__ uint4 pack8v(const __nv_bfloat16* v) {
-  return make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]), pack_bf16x2(v[6], v[7]));
-}
-
-// Byte offset of 16-byte chunk c (0..7) of row r in a 128-byte-swizzled K-major tile.
-__device__ __forceinline__ uint32_t sw128(int r, int c) { return (uint32_t)(r * 128 + ((c ^ (r & 7)) << 4)); }
-
-__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint4 v) {
-  asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
-               : "memory");
-}
 
 // (A) AO values and gradients in double-float.  Planes p = 0..3 (phi, d/dx, d/dy, d/dz) hold the
 // FP32 hi parts at planes + p * P and the lo parts, rounded to BF16 (lo <= ulp(hi) / 2, so hi + lo
@@ -230,57 +180,10 @@ __device__ void pack_a(unsigned char* __restrict__ apack, const float* __restric
   }
 }
 
-// GEMM1 B operand for K block kb and N chunk [nc, nc + 64): D[nu][mu] 2^-f_nu pieces hi / mid / lo
-// / lo2 at stage + 64 KB + q * 8 KB (64 rows x 64 K, 128-byte swizzle), gathered from the packed
-// fixed-point density (x = hi | mid << 16, y = lo | lo2 << 16).
-__device__ void gather_b(unsigned char* stage, const uint2* __restrict__ Dp, const int* s_ao, int n, int m, int kb,
-                         int nc) {
-  const uint32_t sbase = smem_addr(stage) + 65536;
-  for (int e = threadIdx.x; e < kNc * 8; e += kMT) {
-    const int c = e & 7, r = e >> 3;
-    const int nu = nc + r;
-    const int mu0 = kb * 64 + c * 8;
-    uint32_t hw[4] = {0, 0, 0, 0}, mw[4] = {0, 0, 0, 0}, lw[4] = {0, 0, 0, 0}, qw[4] = {0, 0, 0, 0};
-    if (nu < m) {
-      const uint2* row = Dp + (size_t)s_ao[nu] * n;
-#pragma unroll
-      for (int k = 0; k < 8; k += 2) {
-        const uint2 a = (mu0 + k < m) ? __ldg(row + s_ao[mu0 + k]) : make_uint2(0u, 0u);
-        const uint2 b = (mu0 + k + 1 < m) ? __ldg(row + s_ao[mu0 + k + 1]) : make_uint2(0u, 0u);
-        hw[k >> 1] = (a.x & 0xFFFFu) | (b.x << 16);
-        mw[k >> 1] = (a.x >> 16) | (b.x & 0xFFFF0000u);
-        lw[k >> 1] = (a.y & 0xFFFFu) | (b.y << 16);
-        qw[k >> 1] = (a.y >> 16) | (b.y & 0xFFFF0000u);
-      }
-    }
-    const uint32_t off = sw128(r, c);
-    st_shared_v4(sbase + off, make_uint4(hw[0], hw[1], hw[2], hw[3]));
-    st_shared_v4(sbase + 8192 + off, make_uint4(mw[0], mw[1], mw[2], mw[3]));
-    st_shared_v4(sbase + 16384 + off, make_uint4(lw[0], lw[1], lw[2], lw[3]));
-    st_shared_v4(sbase + 24576 + off, make_uint4(qw[0], qw[1], qw[2], qw[3]));
-  }
-}
-
 // Byte offset of GEMM2 image tile (piece p: 0..2 Phi^T, 3..5 Z^T; AO row block ib; point block kb2)
 // in the slab's image area; each tile is 128 AO rows x 64 points, 128-byte swizzle.
 __device__ __forceinline__ size_t img_tile(int p, int ib, int kb2, int n_ib) {
   return (((size_t)p * n_ib + ib) * 2 + kb2) * 16384;
-}
-
-// Compensated sum of double-float products: s collects the FP32 parts by TwoSum, c every rounding
-// and low-order term (Ogita-Rump-Oishi Sum2 applied to the TwoProd pieces).
-struct CompSum {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
-};
-
-__device__ __forceinline__ void acc_prod(CompSum& A, df32 x, df32 t) {
-  const float p = __fmul_rn(x.hi, t.hi);
-  float e = __fmaf_rn(x.hi, t.hi, -p);
-  e = __fmaf_rn(x.hi, t.lo, __fmaf_rn(x.lo, t.hi, e));
-  const df32 q = two_sum(A.s, p);
-  A.s = q.hi;
-  A.c = __fadd_rn(A.c, __fadd_rn(q.lo, e));
 }
 
 __device__ __forceinline__ double cta_sum(double v, double* red_row) {

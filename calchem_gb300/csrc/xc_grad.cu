@@ -26,6 +26,7 @@
 // (E): the per-point coefficients come from the caller, and only the AO term is returned.
 #include <cuda_runtime.h>
 
+#include "becke_grad.cuh"
 #include "common.cuh"
 #include "launch.h"
 #include "xc_device.cuh"
@@ -33,6 +34,10 @@
 namespace cxc {
 
 namespace {
+
+using becke::BeckeScratch;
+using becke::becke_point;
+using becke::becke_scratch_doubles;
 
 constexpr int kGT = 256;        // threads
 constexpr int kGRows = 64;      // AO rows per tile (32 per half)
@@ -261,124 +266,6 @@ __device__ void density_from_t(const BatchDesc& bd, const double* __restrict__ s
   __syncthreads();
 }
 
-// Becke step s(nu) and ds/dnu (grid.rs:129-140).
-__device__ __forceinline__ void step_d(double nu, double& s, double& ds) {
-  const double x = nu < -1.0 ? -1.0 : (nu > 1.0 ? 1.0 : nu);
-  const double f1 = 1.5 * x - 0.5 * x * x * x, d1 = 1.5 - 1.5 * x * x;
-  const double f2 = 1.5 * f1 - 0.5 * f1 * f1 * f1, d2 = 1.5 - 1.5 * f1 * f1;
-  const double f3 = 1.5 * f2 - 0.5 * f2 * f2 * f2, d3 = 1.5 - 1.5 * f2 * f2;
-  s = 0.5 * (1.0 - f3);
-  ds = -0.5 * d3 * d2 * d1;
-}
-
-__device__ __forceinline__ double clamp_unit(double v) { return v < -1.0 ? -1.0 : (v > 1.0 ? 1.0 : v); }
-
-// s_{c d} of the pair in the reference's orientation: computed for the lower index first, the
-// other orientation is 1 - s (grid.rs:456-476).  slope = ds_{lo hi}/dmu_{lo hi}.
-__device__ __forceinline__ double pair_s(int c, int d, const double* __restrict__ dist, const double* __restrict__ inv_r,
-                                         const double* __restrict__ a_ij, int n, double* slope) {
-  const int lo = c < d ? c : d, hi = c < d ? d : c;
-  const double mu = clamp_unit((dist[lo] - dist[hi]) * inv_r[(size_t)lo * n + hi]);
-  const double a = a_ij[(size_t)lo * n + hi];
-  double s, dsdnu;
-  step_d(mu + a * (1.0 - mu * mu), s, dsdnu);
-  if (slope) *slope = dsdnu * (1.0 - 2.0 * a * mu);
-  return c < d ? s : 1.0 - s;
-}
-
-// prod_{d != c, skip} s_{c d}: cell[c] / s_{c skip} when that factor exceeds 1e-12, else the
-// explicit product (grid.rs:500-515).
-__device__ __forceinline__ double prod_except(int c, int skip, double s_cskip, const double* __restrict__ cell,
-                                              const double* __restrict__ dist, const double* __restrict__ inv_r,
-                                              const double* __restrict__ a_ij, int n) {
-  if (s_cskip > 1e-12) return cell[c] / s_cskip;
-  double p = 1.0;
-  for (int d = 0; d < n; ++d) {
-    if (d == c || d == skip || inv_r[(size_t)c * n + d] == 0.0) continue;
-    p *= pair_s(c, d, dist, inv_r, a_ij, n, nullptr);
-  }
-  return p;
-}
-
-// (E) raw_w f dW/dR for one point, one warp; wacc[3a + q] owned by lane a % 32.
-__device__ void becke_point(int n, const double* __restrict__ xyz, const double* __restrict__ inv_r,
-                            const double* __restrict__ a_ij, int host, double x, double y, double z, double pref_in,
-                            double* __restrict__ dist, double* __restrict__ cell, double* __restrict__ wacc) {
-  const int lane = threadIdx.x & 31;
-  for (int c = lane; c < n; c += 32) {
-    const double dx = x - xyz[3 * c], dy = y - xyz[3 * c + 1], dz = z - xyz[3 * c + 2];
-    dist[c] = sqrt(dx * dx + dy * dy + dz * dz);
-  }
-  __syncwarp();
-  double zl = 0.0;
-  for (int c = lane; c < n; c += 32) {
-    double p = 1.0;
-    for (int d = 0; d < n; ++d) {
-      if (d == c || inv_r[(size_t)c * n + d] == 0.0) continue;
-      p *= pair_s(c, d, dist, inv_r, a_ij, n, nullptr);
-    }
-    cell[c] = p;
-    zl += p;
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) zl += __shfl_xor_sync(0xffffffffu, zl, o);
-  __syncwarp();
-  const double zs = zl;
-  if (zs <= 1e-30) return;
-  const double wn = cell[host] / zs, pref = pref_in / zs;
-  double h0 = 0, h1 = 0, h2 = 0;
-  for (int a = lane; a < n; a += 32) {
-    if (a == host) continue;
-    const double ra = dist[a];
-    if (ra < 1e-14) continue;
-    const double ax = xyz[3 * a], ay = xyz[3 * a + 1], az = xyz[3 * a + 2];
-    const double dr0 = -(x - ax) / ra, dr1 = -(y - ay) / ra, dr2 = -(z - az) / ra;
-    double ph0 = 0, ph1 = 0, ph2 = 0, zz0 = 0, zz1 = 0, zz2 = 0;
-    for (int b = 0; b < n; ++b) {
-      if (b == a) continue;
-      const double inv = inv_r[(size_t)a * n + b];
-      if (inv == 0.0) continue;
-      double slope;
-      const double s_ab = pair_s(a, b, dist, inv_r, a_ij, n, &slope);
-      if (fabs(slope) < 1e-30) continue;
-      const double mu = clamp_unit((ra - dist[b]) * inv);
-      const double v0 = ax - xyz[3 * b], v1 = ay - xyz[3 * b + 1], v2 = az - xyz[3 * b + 2];
-      const double pa = prod_except(a, b, s_ab, cell, dist, inv_r, a_ij, n);
-      const double pb = prod_except(b, a, 1.0 - s_ab, cell, dist, inv_r, a_ij, n);
-      const double k = slope * inv;
-      const double ds0 = k * (dr0 - mu * v0 * inv), ds1 = k * (dr1 - mu * v1 * inv), ds2 = k * (dr2 - mu * v2 * inv);
-      zz0 += pa * ds0 - pb * ds0;
-      zz1 += pa * ds1 - pb * ds1;
-      zz2 += pa * ds2 - pb * ds2;
-      if (b == host) {
-        ph0 -= pb * ds0;
-        ph1 -= pb * ds1;
-        ph2 -= pb * ds2;
-      }
-    }
-    const double w0 = pref * (ph0 - wn * zz0), w1 = pref * (ph1 - wn * zz1), w2 = pref * (ph2 - wn * zz2);
-    wacc[3 * a] += w0;
-    wacc[3 * a + 1] += w1;
-    wacc[3 * a + 2] += w2;
-    h0 -= w0;
-    h1 -= w1;
-    h2 -= w2;
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    h0 += __shfl_xor_sync(0xffffffffu, h0, o);
-    h1 += __shfl_xor_sync(0xffffffffu, h1, o);
-    h2 += __shfl_xor_sync(0xffffffffu, h2, o);
-  }
-  __syncwarp();
-  if (lane == 0) {
-    wacc[3 * host] += h0;
-    wacc[3 * host + 1] += h1;
-    wacc[3 * host + 2] += h2;
-  }
-  __syncwarp();
-}
-
 __global__ void __launch_bounds__(kGT, 1) xc_grad_kernel(DevGrid G, GradArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   GradSmem& S = *reinterpret_cast<GradSmem*>(smem_raw);
@@ -391,16 +278,21 @@ __global__ void __launch_bounds__(kGT, 1) xc_grad_kernel(DevGrid G, GradArgs A) 
   const int m_pad = (A.max_m + kGRows - 1) / kGRows * kGRows;
   const size_t plane = (size_t)m_pad * kBlockPts;
   double* slab = A.slab + (size_t)blockIdx.x * A.slab_stride;
-  // Becke scratch of each warp behind the planes: dist[n], cell[n], wacc[3n]
+  // Becke scratch of each warp behind the planes: dist[n], cell[n], wacc[3n], s, e, l [n x n]
   double* wscr = slab + (size_t)kGradPlanes * plane;
   const int n_at = A.n_atoms;
-  double* my_dist = wscr + (size_t)warp * 5 * n_at;
-  double* my_cell = my_dist + n_at;
-  double* my_wacc = my_cell + n_at;
+  const size_t per_warp = becke_scratch_doubles(n_at);
+  BeckeScratch W;
+  W.dist = wscr + (size_t)warp * per_warp;
+  W.cell = W.dist + n_at;
+  W.wacc = W.cell + n_at;
+  W.s = W.wacc + 3 * n_at;
+  W.e = W.s + (size_t)n_at * n_at;
+  W.l = W.e + (size_t)n_at * n_at;
   const bool fused = A.xc >= 0;
   for (int k = tid; k < na3; k += kGT) acc[k] = 0.0;
   if (fused)
-    for (size_t k = tid; k < (size_t)kGWarps * 5 * n_at; k += kGT) wscr[k] = 0.0;
+    for (size_t k = tid; k < (size_t)kGWarps * per_warp; k += kGT) wscr[k] = 0.0;
   __syncthreads();
 
   while (true) {
@@ -518,8 +410,8 @@ __global__ void __launch_bounds__(kGT, 1) xc_grad_kernel(DevGrid G, GradArgs A) 
         const size_t p = (size_t)bd.pt_start + gg;
         const double rw = A.raw_w[p];
         if (fabs(f) < 1e-18 || rw == 0.0) continue;
-        becke_point(n_at, A.xyz, A.inv_r, A.a_ij, S.host[gg], G.px[p], G.py[p], G.pz[p], rw * f, my_dist, my_cell,
-                    my_wacc);
+        becke_point(n_at, A.xyz, A.inv_r, A.a_ij, A.pairs, A.n_pairs, S.host[gg], G.px[p], G.py[p], G.pz[p], rw * f,
+                    W);
       }
     }
     __syncthreads();
@@ -530,7 +422,7 @@ __global__ void __launch_bounds__(kGT, 1) xc_grad_kernel(DevGrid G, GradArgs A) 
       acc[k] = 0.0;
       if (fused) {
         for (int w = 0; w < kGWarps; ++w) {
-          double* wa = wscr + (size_t)w * 5 * n_at + 2 * n_at;
+          double* wa = wscr + (size_t)w * per_warp + 2 * n_at;
           v += wa[k];
           wa[k] = 0.0;
         }
@@ -564,7 +456,7 @@ size_t grad_smem_bytes(int n_atoms) { return sizeof(GradSmem) + (size_t)3 * n_at
 
 size_t grad_slab_doubles(int max_m, int n_atoms) {
   const size_t m_pad = (size_t)(max_m + kGRows - 1) / kGRows * kGRows;
-  return (size_t)kGradPlanes * m_pad * kBlockPts + (size_t)kGWarps * 5 * n_atoms;
+  return (size_t)kGradPlanes * m_pad * kBlockPts + (size_t)kGWarps * becke_scratch_doubles(n_atoms);
 }
 
 int grad_max_atoms() { return kMaxGradAtoms; }

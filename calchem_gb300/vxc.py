@@ -193,10 +193,10 @@ class _EngineBase:
     def last_launch_count(self) -> int:
         return int(_native.load().calchem_xc_last_launch_count(self.grid_id))
 
-    def nuclear_gradient(self, mol, grid, func, pa, pb=None) -> np.ndarray:
+    def nuclear_gradient(self, mol, grid, func, pa, pb=None, precision=None) -> np.ndarray:
         """dExc/dR [n_atoms][3] (Eh/Bohr) at fixed spin densities on this engine's grid, which must be
         the grid it was built from (calchem_xc_nuclear_gradient).  pb = None: closed shell (beta =
-        alpha; pass P_total / 2)."""
+        alpha; pass P_total / 2).  precision: "fp64" or "mixed" (default: the engine's)."""
         lib = _native.load()
         Pa = _as_matrix(pa, self.n_ao)
         Pb = None if pb is None else _as_matrix(pb, self.n_ao)
@@ -205,8 +205,9 @@ class _EngineBase:
         raw = np.ascontiguousarray(grid.raw_weight, dtype=np.float64)
         host = np.ascontiguousarray(grid.host_atom, dtype=np.int32)
         out = np.zeros((len(z), 3), dtype=np.float64)
+        prec = self.precision if precision is None else _PRECISION[precision]
         _native.check("calchem_xc_nuclear_gradient", lib.calchem_xc_nuclear_gradient(
-            self.grid_id, _xc_code(func), len(z), _native.ptr(z), _native.ptr(xyz), _native.ptr(raw),
+            self.grid_id, _xc_code(func), prec, len(z), _native.ptr(z), _native.ptr(xyz), _native.ptr(raw),
             _native.ptr(host), len(raw), _native.ptr(Pa), None if Pb is None else _native.ptr(Pb), _native.ptr(out)))
         self.gpu_kernel_invocations += self.last_launch_count()
         return out
@@ -279,7 +280,7 @@ def evaluate_vxc_uks(basis, grid, func, pa, pb, precision="fp64"):
         eng.close()
 
 
-def xc_nuclear_gradient_with_gpu(mol, basis, grid, func, pa, pb, use_gpu=True):
+def xc_nuclear_gradient_with_gpu(mol, basis, grid, func, pa, pb, use_gpu=True, precision="fp64"):
     """xc_nuclear_gradient_with_gpu (vxc.rs:2030-2333): (grad [n_atoms][3], gpu_kernel_invocations,
     gpu_fallback_invocations).  Equal pa and pb are treated as a closed shell, as the reference does
     (is_rks = pa == pb).  There is no CPU path: use_gpu=False raises."""
@@ -291,7 +292,7 @@ def xc_nuclear_gradient_with_gpu(mol, basis, grid, func, pa, pb, use_gpu=True):
     pa = _as_matrix(pa, basis.n_ao)
     pb = _as_matrix(pb, basis.n_ao)
     closed = pa is pb or np.array_equal(pa, pb)
-    eng = UksVxcEngine(basis, grid, True, "fp64")
+    eng = UksVxcEngine(basis, grid, True, precision)
     try:
         g = eng.nuclear_gradient(mol, grid, func, pa, None if closed else pb)
         return g, eng.gpu_kernel_invocations, 0
@@ -299,10 +300,11 @@ def xc_nuclear_gradient_with_gpu(mol, basis, grid, func, pa, pb, use_gpu=True):
         eng.close()
 
 
-def xc_nuclear_gradient(mol, basis, grid, func, pa, pb):
+def xc_nuclear_gradient(mol, basis, grid, func, pa, pb, precision="fp64"):
     """xc_nuclear_gradient (vxc.rs:1903-1912): dExc/dR_A at fixed spin densities pa, pb (closed
-    shell: pa = pb = P_total / 2), in Eh/Bohr, [n_atoms][3]."""
-    return xc_nuclear_gradient_with_gpu(mol, basis, grid, func, pa, pb, True)[0]
+    shell: pa = pb = P_total / 2), in Eh/Bohr, [n_atoms][3]; precision "mixed" runs the density
+    contractions on the tensor cores."""
+    return xc_nuclear_gradient_with_gpu(mol, basis, grid, func, pa, pb, True, precision)[0]
 
 
 class VxcGroup:

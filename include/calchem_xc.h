@@ -113,7 +113,7 @@ int calchem_cuda_vxc_accum(uint64_t grid_id, const double* h_wv_in, double* h_vx
  * overwritten) = -2 sum over points and spins of the AO force terms of the atoms' AOs, with every
  * point's total subtracted at its host atom (GridPtGpu.host_atom of the upload).  The Becke weight
  * term is the caller's, as in the reference.  memory_limit_bytes = 0: no limit.  Returns -1 (bad
- * arguments, host or shell atom outside [0, n_atoms), n_atoms > 4096), -2 (unknown grid or size
+ * arguments, host or shell atom outside [0, n_atoms), n_atoms > 1024), -2 (unknown grid or size
  * mismatch), -3 (memory limit), -4 (allocation), -5 (CUDA). */
 int calchem_cuda_vxc_grad_force(uint64_t grid_id, const double* h_pa, const double* h_pb, int is_rks,
                                 const double* h_wxc_in, double* h_grad_out, int n_pts, int n_ao, int n_atoms,
@@ -231,19 +231,23 @@ int calchem_xc_fxc_contract_device(uint64_t grid_id, int triplet, const double* 
                                    void* stream);
 
 /* XC nuclear gradient dExc/dR at fixed densities (xc_nuclear_gradient, vxc.rs:1903-1912 and the
- * Becke weight derivative grid.rs:423-584), entirely on the device, in FP64: densities, functional,
- * AO force terms with the host-atom term, and the weight derivative.  grid_id is a single grid
+ * Becke weight derivative grid.rs:423-584), entirely on the device: densities, functional, AO force
+ * terms with the host-atom term, and the weight derivative.  precision CALCHEM_XC_FP64: all FP64;
+ * CALCHEM_XC_MIXED: the contractions P Phi and P Psi on the tensor cores (exact fixed-point split),
+ * AO values, derivatives and the force terms in double-float, functional and weight derivative in
+ * FP64; batches of more than 2048 AOs return -2 for it.  grid_id is a single grid
  * uploaded with its weights (calchem_xc_upload_points*); h_raw_w (weights before the Becke
  * partition) and h_host_atom hold the n_grid_pts points the caller uploaded, in its order (as
  * calchem_xc_grid_fetch returns them); the atoms (z, xyz_bohr) are the molecule the grid was built
  * for.  h_pa / h_pb are the spin densities; h_pb = NULL means a closed shell (beta = alpha, so an
  * RKS caller passes P_total / 2).  h_grad_out[3 A + q] = dExc/dR_Aq in Eh/Bohr.  Points that were
  * not uploaded (|w| < 1e-24) are left out.  One atom: zeros.  Returns -1 (bad arguments, host or
- * shell atom outside [0, n_atoms), n_atoms > 4096), -2 (unknown grid, a group, no weights, or
- * n_grid_pts not the uploaded count), -4 / -5 on allocation / CUDA failure. */
-int calchem_xc_nuclear_gradient(uint64_t grid_id, int xc_code, int n_atoms, const int* z, const double* xyz_bohr,
-                                const double* h_raw_w, const int* h_host_atom, int n_grid_pts, const double* h_pa,
-                                const double* h_pb, double* h_grad_out);
+ * shell atom outside [0, n_atoms), n_atoms > 1024), -2 (unknown grid, a group, no weights, or
+ * n_grid_pts not the uploaded count), -4 / -5 on allocation / CUDA failure, -7 when a device-side
+ * wait of the tensor-core form expired. */
+int calchem_xc_nuclear_gradient(uint64_t grid_id, int xc_code, int precision, int n_atoms, const int* z,
+                                const double* xyz_bohr, const double* h_raw_w, const int* h_host_atom, int n_grid_pts,
+                                const double* h_pa, const double* h_pb, double* h_grad_out);
 
 /* ======================================================================================
  * (3b) Many molecules in one launch, and CUDA-graph replay.  No counterpart in the reference.

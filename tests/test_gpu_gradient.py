@@ -137,12 +137,44 @@ def test_gradient_error_codes(setup, native_lib):
     P = make_positive_density(basis.n_ao, 1)
     out = np.zeros((len(z), 3))
     from calchem_gb300 import _native
-    rc = native_lib.calchem_xc_nuclear_gradient(eng.grid_id, 1, len(z), _native.ptr(z), _native.ptr(xyz),
+    rc = native_lib.calchem_xc_nuclear_gradient(eng.grid_id, 1, 0, len(z), _native.ptr(z), _native.ptr(xyz),
                                                 _native.ptr(grid.raw_weight), _native.ptr(bad), len(bad),
                                                 _native.ptr(P), None, _native.ptr(out))
     assert rc == -1
-    rc = native_lib.calchem_xc_nuclear_gradient(eng.grid_id, 1, len(z), _native.ptr(z), _native.ptr(xyz),
+    rc = native_lib.calchem_xc_nuclear_gradient(eng.grid_id, 1, 0, len(z), _native.ptr(z), _native.ptr(xyz),
                                                 _native.ptr(grid.raw_weight), _native.ptr(grid.host_atom),
                                                 len(bad) - 1, _native.ptr(P), None, _native.ptr(out))
     assert rc == -2
     eng.close()
+
+
+MIXED_TOL = 1e-9  # tensor-core form vs the oracle, Eh/Bohr per component (measured ~7e-11 on water)
+
+
+@pytest.mark.parametrize("func", ["svwn5", "pbe", "b3lyp", "camb3lyp"])
+def test_mixed_gradient_matches_oracle(setup, oracle, func):
+    mol, basis, grid, ob, og = setup
+    P = make_positive_density(basis.n_ao, 3)
+    Pa, Pb = make_positive_density(basis.n_ao, 3), make_positive_density(basis.n_ao, 8)
+    for pa, pb in ((0.5 * P, 0.5 * P), (Pa, Pb)):
+        g = xc_nuclear_gradient(mol, basis, grid, func, pa, pb, precision="mixed")
+        ref = oracle.xc_gradient(ob, og, mol.z, mol.coords_bohr, pa, pb, func)
+        assert np.max(np.abs(g - ref)) < MIXED_TOL, np.abs(g - ref).max()
+        assert np.max(np.abs(g.sum(axis=0))) < 1e-12
+
+
+def test_mixed_gradient_octane_matches_fp64():
+    """C8H18 B3LYP on the Medium grid: the tensor-core gradient within 5e-9 Eh/Bohr of the FP64 one
+    (measured 5.4e-10 on the Fine grid), deterministic on repeat."""
+    from calchem_gb300 import BasisSet as BS, RksVxcEngine, workloads
+    mol = workloads.octane()
+    basis = BS.from_name("6-31g(d,p)", mol)
+    grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.MEDIUM)
+    D = workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, 7)
+    eng = RksVxcEngine(basis, grid)
+    g64 = eng.nuclear_gradient(mol, grid, "b3lyp", 0.5 * D)
+    gm = eng.nuclear_gradient(mol, grid, "b3lyp", 0.5 * D, precision="mixed")
+    gm2 = eng.nuclear_gradient(mol, grid, "b3lyp", 0.5 * D, precision="mixed")
+    eng.close()
+    assert np.max(np.abs(gm - g64)) < 5e-9, np.abs(gm - g64).max()
+    assert np.array_equal(gm, gm2)
