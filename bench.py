@@ -525,7 +525,7 @@ def run_ours(args):
     return 0
 
 
-GRADIENT_METRIC = "XC nuclear gradient dExc/dR ms on 1 GB300 (FP64, fixed density)"
+GRADIENT_METRIC = "XC nuclear gradient dExc/dR ms on 1 GB300: tensor-core form vs FP64 plain (fixed density)"
 
 
 def cpu_gradient_sample(mol, basis, grid, Pa, func, n_sample=4000):
@@ -548,7 +548,8 @@ def cpu_gradient_sample(mol, basis, grid, Pa, func, n_sample=4000):
 
 def run_gradient(args):
     """One step = one XC nuclear gradient (calchem_xc_nuclear_gradient) of the headline workload on
-    its Fine grid at the seeded closed-shell density (P_alpha = D / 2)."""
+    its Fine grid at the seeded closed-shell density (P_alpha = D / 2); the tensor-core form unless
+    --precision fp64, with the FP64 form timed beside it."""
     import torch
 
     from calchem_gb300 import GridLevel, MolecularGrid, RksVxcEngine
@@ -556,50 +557,66 @@ def run_gradient(args):
     ws, rank, local = dist_env()
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    prec = "fp64" if args.precision == "fp64" else "mixed"
     mol, basis, D = build_inputs()
     grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
     eng = RksVxcEngine(basis, grid)
     eng.set_profiling(True)
     Pa = 0.5 * D
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    for _ in range(max(3, args.warmup)):
-        g = eng.nuclear_gradient(mol, grid, "b3lyp", Pa)
+
+    def timed(precision, steps):
+        kern, wall, g = [], [], None
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            g = eng.nuclear_gradient(mol, grid, "b3lyp", Pa, precision=precision)
+            wall.append((time.perf_counter() - t0) * 1e3)
+            kern.append(eng.last_kernel_ms())
+        return kern, wall, g
+
+    timed(prec, max(3, args.warmup))
     n0 = eng.gpu_kernel_invocations
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    kern, wall = [], []
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        g = eng.nuclear_gradient(mol, grid, "b3lyp", Pa)
-        wall.append((time.perf_counter() - t0) * 1e3)
-        kern.append(eng.last_kernel_ms())
+    kern, wall, g = timed(prec, args.steps)
     clk = clocks.stop()
     launches = eng.gpu_kernel_invocations - n0
+    k64, _, g64 = timed("fp64", 2)
     n_batches, sum_m2n, _, max_m = eng.plan_stats()
     flops = 4.0 * sum_m2n  # T = P Phi and Y = P Psi, 2 m^2 n each (closed shell)
     kms = statistics.mean(kern)
-    peak = fp64_peak_tflops(torch, dev)
+    if prec == "mixed":
+        pk, pk_kind = peaks()
+        peak, bound, unit = pk.get("bf16_tflops", 1900.0), "tensor", "TFLOP/s"
+        peak_note = f"dense bf16 burst, {pk_kind}"
+    else:
+        peak, bound, unit = fp64_peak_tflops(torch, dev), "fp64 pipe", "TFLOP/s"
+        peak_note = "FP64 pipe: cuBLAS DGEMM 4096^3 measured in this run"
     achieved = flops / (kms * 1e-3) / 1e12
     n = basis.n_ao
     line = {
         "metric": GRADIENT_METRIC, "value": round(kms, 4), "unit": "ms", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(kms, 4), "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None,
+        "dtype": "f64" if prec == "fp64" else "bf16x4 fixed-point split contractions, df32 AO/forces/weights, f64 functional",
+        "data": "synthetic",
         "config": {"workload": WORKLOAD + "; XC nuclear gradient at P_alpha = D / 2", "name": args.workload,
-                   "grid_points": len(grid), "batches": n_batches, "max_m": max_m, "atoms": len(mol.z),
-                   "l2": "flushed before every timed step (256 MiB write)"},
-        "roofline": {"bound": "fp64 pipe", "achieved": round(achieved, 4), "peak": round(peak, 3),
-                     "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": None,
-                     "kernel": "xc_grad_kernel + grad_reduce_kernel", "kernel_ms": round(kms, 4),
+                   "precision": prec, "grid_points": len(grid), "batches": n_batches, "max_m": max_m,
+                   "atoms": len(mol.z), "l2": "flushed before every timed step (256 MiB write)"},
+        "roofline": {"bound": bound, "achieved": round(achieved, 4), "peak": round(peak, 3), "unit": unit,
+                     "frac": round(achieved / peak, 5), "traffic": None,
+                     "kernel": "gradient kernel + split + reduce", "kernel_ms": round(kms, 4),
                      "work": f"4*sum(m^2 n) = {flops:.4e} flop of AO contractions per launch (Becke term not "
-                             f"counted)",
-                     "peak_source": "FP64 pipe: cuBLAS DGEMM 4096^3 measured in this run"},
+                             f"counted)", "peak_source": peak_note},
         "e2e": {"value": round(statistics.mean(wall), 4), "unit": "ms",
                 "h2d_bytes_per_step": n * n * 8 + len(grid) * 12, "d2h_bytes_per_step": len(mol.z) * 24},
         "gpu_launches": launches, "clocks": clk,
+        "fp64_plain_ms": round(statistics.mean(k64), 4),
+        "speedup_vs_fp64_plain": round(statistics.mean(k64) / kms, 3),
+        "max_abs_dgrad_vs_fp64": float(np.max(np.abs(g - g64))),
         "max_abs_grad": float(np.max(np.abs(g))), "sum_over_atoms": float(np.max(np.abs(g.sum(axis=0)))),
     }
     if not args.no_cpu_baseline:

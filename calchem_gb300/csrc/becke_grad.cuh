@@ -312,8 +312,11 @@ static __device__ void becke_point_df(int n, const double* __restrict__ xyz, con
 //   cnt[n] (int); su, scu, lu [n (n - 1) / 2] (double-float): s_cd, 1 - s_cd and ds_cd/dmu_cd, c < d.
 // The "product but one" E_ab = prod_{d != a, b} s_ad comes from the row's product of its factors
 // above 1e-30 (pp) and the count of the others (cnt): pp / s_ab when none is below, pp when s_ab
-// is the only one, and 0 otherwise (then E_ab < 1e-30).  The pass-2 sums over b are reduced by xor
-// shuffles inside fixed lane groups, so results are deterministic.
+// is the only one, and 0 otherwise (then E_ab < 1e-30).  Pairs whose terms are below 1e-18
+// (|E_ab - E_ba| |slope| / R_ab, and E_ba |slope| / R_ab for b = host; first tested on FP32 estimates)
+// are skipped: with every E, slope and R^-1 of order one at most, the dropped sum over a grid stays
+// below ~1e-12 Eh/Bohr.  The pass-2 sums over b are reduced by xor shuffles inside fixed lane groups,
+// so results are deterministic.
 
 __host__ __device__ constexpr size_t becke_cta_bytes(int n) {
   return (8 * (8 * (size_t)n + 4) + 8 * (size_t)n + 4 * (size_t)(n + (n & 1)) + 12 * (size_t)n * (size_t)(n - 1) + 15) /
@@ -430,7 +433,10 @@ static __device__ void becke_point_team(int n, const double* __restrict__ xyz, c
   const int iters = (n + groups - 1) / groups;
   for (int it = 0; it < iters; ++it) {
     const int a = tid / L + it * groups;
-    df32 zz0 = {0.f, 0.f}, zz1 = zz0, zz2 = zz0, ph0 = zz0, ph1 = zz0, ph2 = zz0;
+    // dZ/dR_a = sum_b (E_ab - E_ba) k_ab (dr_a - mu_ab e_ab) with k = slope / R_ab, accumulated as
+    // dr_a C - W with C = sum c_b, W = sum c_b mu_ab e_ab, c_b = (E_ab - E_ba) k_ab
+    df32 cs = {0.f, 0.f}, w0 = cs, w1 = cs, w2 = cs, ph0 = cs, ph1 = cs, ph2 = cs;
+    df32 dr0 = cs, dr1 = cs, dr2 = cs;
     bool act = false;
     if (a < n && a != host) {
       const df32 dra = T.dist[a];
@@ -438,8 +444,9 @@ static __device__ void becke_point_team(int n, const double* __restrict__ xyz, c
       act = ra >= 1e-14;
       if (act) {
         const double ir = 1.0 / ra;
-        const df32 dr0 = df_from_double(-(x - xyz[3 * a]) * ir), dr1 = df_from_double(-(y - xyz[3 * a + 1]) * ir),
-                   dr2 = df_from_double(-(z - xyz[3 * a + 2]) * ir);
+        dr0 = df_from_double(-(x - xyz[3 * a]) * ir);
+        dr1 = df_from_double(-(y - xyz[3 * a + 1]) * ir);
+        dr2 = df_from_double(-(z - xyz[3 * a + 2]) * ir);
         for (int b = sub; b < n; b += L) {
           const df32* t = pdf + 5 * ((size_t)a * n + b);
           const df32 inv = t[0];
@@ -451,34 +458,36 @@ static __device__ void becke_point_team(int n, const double* __restrict__ xyz, c
           const float scl = fabsf(sl.hi) * inv.hi;
           // both products but one from FP32 estimates: skip the pair when even their sum is below
           // the threshold (half of it, for the estimates' error), before any double-float work
-          if (est_but_one(T, a, s_ab.hi) * scl < 5e-21f && est_but_one(T, b, s_ba.hi) * scl < 5e-21f) continue;
+          if (est_but_one(T, a, s_ab.hi) * scl < 5e-19f && est_but_one(T, b, s_ba.hi) * scl < 5e-19f) continue;
           const df32 ea = prod_but_one(T, a, s_ab), eb = prod_but_one(T, b, s_ba);
           const df32 diff = df_sub(ea, eb);
-          if (fabsf(diff.hi) * scl < 1e-20f && (b != host || fabsf(eb.hi) * scl < 1e-20f)) continue;
+          if (fabsf(diff.hi) * scl < 1e-18f && (b != host || fabsf(eb.hi) * scl < 1e-18f)) continue;
           const df32 mu = df_clamp_unit(df_mul(df_sub(dra, T.dist[b]), inv));
           const df32 k = df_mul(sl, inv);
-          const df32 ds0 = df_mul(k, df_sub(dr0, df_mul(mu, t[2])));
-          const df32 ds1 = df_mul(k, df_sub(dr1, df_mul(mu, t[3])));
-          const df32 ds2 = df_mul(k, df_sub(dr2, df_mul(mu, t[4])));
-          zz0 = df_add(zz0, df_mul(diff, ds0));
-          zz1 = df_add(zz1, df_mul(diff, ds1));
-          zz2 = df_add(zz2, df_mul(diff, ds2));
-          if (b == host) {
-            ph0 = df_sub(ph0, df_mul(eb, ds0));
-            ph1 = df_sub(ph1, df_mul(eb, ds1));
-            ph2 = df_sub(ph2, df_mul(eb, ds2));
+          const df32 c = df_mul(diff, k), cm = df_mul(c, mu);
+          cs = df_add(cs, c);
+          w0 = df_add(w0, df_mul(cm, t[2]));
+          w1 = df_add(w1, df_mul(cm, t[3]));
+          w2 = df_add(w2, df_mul(cm, t[4]));
+          if (b == host) {  // d P_host / dR_a = -E_ba k (dr_a - mu e)
+            const df32 kb = df_mul(eb, k);
+            ph0 = df_mul(kb, df_sub(df_mul(mu, t[2]), dr0));
+            ph1 = df_mul(kb, df_sub(df_mul(mu, t[3]), dr1));
+            ph2 = df_mul(kb, df_sub(df_mul(mu, t[4]), dr2));
           }
         }
       }
     }
     for (int o = L / 2; o > 0; o >>= 1) {
-      zz0 = df_add(zz0, df32{__shfl_xor_sync(0xffffffffu, zz0.hi, o), __shfl_xor_sync(0xffffffffu, zz0.lo, o)});
-      zz1 = df_add(zz1, df32{__shfl_xor_sync(0xffffffffu, zz1.hi, o), __shfl_xor_sync(0xffffffffu, zz1.lo, o)});
-      zz2 = df_add(zz2, df32{__shfl_xor_sync(0xffffffffu, zz2.hi, o), __shfl_xor_sync(0xffffffffu, zz2.lo, o)});
+      cs = df_add(cs, df32{__shfl_xor_sync(0xffffffffu, cs.hi, o), __shfl_xor_sync(0xffffffffu, cs.lo, o)});
+      w0 = df_add(w0, df32{__shfl_xor_sync(0xffffffffu, w0.hi, o), __shfl_xor_sync(0xffffffffu, w0.lo, o)});
+      w1 = df_add(w1, df32{__shfl_xor_sync(0xffffffffu, w1.hi, o), __shfl_xor_sync(0xffffffffu, w1.lo, o)});
+      w2 = df_add(w2, df32{__shfl_xor_sync(0xffffffffu, w2.hi, o), __shfl_xor_sync(0xffffffffu, w2.lo, o)});
       ph0 = df_add(ph0, df32{__shfl_xor_sync(0xffffffffu, ph0.hi, o), __shfl_xor_sync(0xffffffffu, ph0.lo, o)});
       ph1 = df_add(ph1, df32{__shfl_xor_sync(0xffffffffu, ph1.hi, o), __shfl_xor_sync(0xffffffffu, ph1.lo, o)});
       ph2 = df_add(ph2, df32{__shfl_xor_sync(0xffffffffu, ph2.hi, o), __shfl_xor_sync(0xffffffffu, ph2.lo, o)});
     }
+    const df32 zz0 = df_sub(df_mul(dr0, cs), w0), zz1 = df_sub(df_mul(dr1, cs), w1), zz2 = df_sub(df_mul(dr2, cs), w2);
     if (sub == 0 && a < n) {
       T.tmp[3 * a] = act ? pref * (df_to_double(ph0) - wn * df_to_double(zz0)) : 0.0;
       T.tmp[3 * a + 1] = act ? pref * (df_to_double(ph1) - wn * df_to_double(zz1)) : 0.0;

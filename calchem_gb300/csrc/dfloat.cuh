@@ -74,12 +74,13 @@ __device__ __forceinline__ df32 df_mul_f(df32 a, float b) {
   return fast_two_sum(p.hi, p.lo);
 }
 
-// a / b (b != 0): the FP32 quotient and one correction from the exact remainder (Dekker).
+// a / b for 2^-126 < |b| < 2^126: an approximate FP32 quotient (a few ulp) and one correction from
+// the exact remainder (Dekker); the correction's own error is ~1e-7 of a term ~1e-7 of the result.
 __device__ __forceinline__ df32 df_div(df32 a, df32 b) {
-  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const float q1 = __fdividef(a.hi, b.hi);
   const df32 p = two_prod(q1, b.hi);
   const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p.hi), p.lo), __fsub_rn(a.lo, __fmul_rn(q1, b.lo)));
-  return fast_two_sum(q1, __fdiv_rn(r, b.hi));
+  return two_sum(q1, __fdividef(r, b.hi));
 }
 
 // Exact scaling by a power of two (as long as no underflow/overflow occurs).

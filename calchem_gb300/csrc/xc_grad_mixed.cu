@@ -16,12 +16,12 @@
 //       scaled by 2^-e_g, D rows by 2^-f_nu, four BF16 pieces each, ten products, hh products summed
 //       exactly); the epilogue keeps T as a double-float plane and forms rho_s, grad rho_s by
 //       compensated sums;
-//   (C) the FP64 spin functional per point: (w v_rho_s, w u_s) and f;
+//   (C) the FP64 functional per point (the one-spin form for a closed shell): (w v_rho_s, w u_s), f;
 //   (D) per spin, Psi_s = (w u_s) . grad Phi in double-float, split the same way (scale 2^-e'_g) and
 //       Y_s = Psi_s P_s on tcgen05; the epilogue forms each row's force from T, Y, grad phi and the
-//       Hessian in double-float, reduces it over the points with warp shuffles and adds it, row by
-//       row in a fixed order, to the batch's row of per-atom sums; every point's total goes to its
-//       host atom with the opposite sign;
+//       Hessian in double-float, sums consecutive rows of one atom per point, reduces those sums
+//       over the points with warp shuffles and adds them, in a fixed order, to the batch's row of
+//       per-atom sums; every point's total goes to its host atom with the opposite sign;
 //   (E) the Becke weight derivative in double-float (becke_grad.cuh): teams of 1-8 warps, one point
 //       per team, with the pair tables in the idle operand stage (up to 87 atoms), else one warp
 //       per point with the tables in the scratch slab;
@@ -66,7 +66,7 @@ constexpr int kOffMiscG = kOffHostG + 512;       // mbarriers, TMEM slot, batch 
 constexpr int kSmemG = kOffMiscG + 32 + 1024;    // + alignment slack
 // stage-resident scratch while no operands are in flight
 constexpr int kOffDensS = 65536;                 // double [2][4][128]
-constexpr int kOffRedS = 0;                      // double [8][32][3]: warp sums of the row forces
+constexpr int kOffRedS = 0;                      // per-warp runs of the row forces (7.2 KB)
 constexpr int kOffHsumS = 8192;                  // double [2][3][128]: per-point host sums
 static_assert(2 * (kSmemG + 1024) <= 233472, "two CTAs must fit in one SM's shared memory");
 constexpr int kPlanesG = 10;                     // phi, grad (3), Hessian (xx xy xz yy yz zz)
@@ -234,7 +234,10 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffMiscG + 16);
   int* s_batch = reinterpret_cast<int*>(base + kOffMiscG + 20);
   double(*dens)[4][128] = reinterpret_cast<double(*)[4][128]>(stage + kOffDensS);
-  double(*red)[32][3] = reinterpret_cast<double(*)[32][3]>(stage + kOffRedS);
+  double(*run_v)[32][3] = reinterpret_cast<double(*)[32][3]>(stage + kOffRedS);  // per warp: run sums
+  int(*run_at)[32] = reinterpret_cast<int(*)[32]>(stage + kOffRedS + 6144);        // per warp: run atoms
+  int* run_n = reinterpret_cast<int*>(stage + kOffRedS + 7168);                     // per warp: runs
+
   double(*hsum)[3][128] = reinterpret_cast<double(*)[3][128]>(stage + kOffHsumS);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -462,7 +465,19 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
       const double rb = spin_rho[sb1][0];
       const double gbx = 2.0 * spin_rho[sb1][1], gby = 2.0 * spin_rho[sb1][2], gbz = 2.0 * spin_rho[sb1][3];
       const double rpa = fmax(ra, 0.0), rpb = fmax(rb, 0.0);
-      if (live && !(rpa + rpb < 1e-18)) {
+      if (live && A.closed && !(rpa + rpb < 1e-18)) {
+        // closed shell: the one-spin form (u_a = (2 v_gamma_aa + v_gamma_ab) grad rho_a = 2 v_g grad rho_a)
+        const XcCs o = xc_eval_cs(A.xc, rpa, gax * gax + gay * gay + gaz * gaz);
+        const double w = G.pw[pt];
+        if (fabs(w) > 1e-24) {
+          const double us = 2.0 * w * o.vg;
+          cf[0] = cf[4] = w * o.vr;
+          cf[1] = cf[5] = us * gax;
+          cf[2] = cf[6] = us * gay;
+          cf[3] = cf[7] = us * gaz;
+        }
+        cf[8] = o.f;
+      } else if (live && !(rpa + rpb < 1e-18)) {
         const double gaa = gax * gax + gay * gay + gaz * gaz;
         const double gab = gax * gbx + gay * gby + gaz * gbz;
         const double gbb = gbx * gbx + gby * gby + gbz * gbz;
@@ -486,7 +501,7 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
     __syncthreads();
 
     // (D) per spin: Psi_s, Y_s = Psi_s P_s, and the row forces
-    double hs0 = 0, hs1 = 0, hs2 = 0;
+    df32 hs0 = {0.f, 0.f}, hs1 = hs0, hs2 = hs0;  // this thread's point: sum of its row terms
     for (int s = 0; s < nspin && !failed; ++s) {
       const uint2* Dhl = s ? Dhl_b0 : Dhl_a0;
       const int* fexp = s ? fexp_b0 : fexp_a0;
@@ -516,6 +531,25 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
       for (int nc = 0; nc < m && !failed; nc += kNc) {
         if (tid < kNc) s_fx[tid] = nc + tid < m ? fexp[s_ao[nc + tid]] : 0;
         chunk(nc, m, nkb, n, Dhl, [&](bool first_group) {
+          // the group's 32 columns in runs of one atom: each thread sums its point's terms per run,
+          // and a finished run's sum over the warp's 32 points goes to the warp's run list
+          df32 r0 = {0.f, 0.f}, r1 = r0, r2 = r0;
+          int cur = -1, nrun = 0;
+          auto flush = [&]() {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+              r0 = df_add(r0, df32{__shfl_xor_sync(0xffffffffu, r0.hi, off), __shfl_xor_sync(0xffffffffu, r0.lo, off)});
+              r1 = df_add(r1, df32{__shfl_xor_sync(0xffffffffu, r1.hi, off), __shfl_xor_sync(0xffffffffu, r1.lo, off)});
+              r2 = df_add(r2, df32{__shfl_xor_sync(0xffffffffu, r2.hi, off), __shfl_xor_sync(0xffffffffu, r2.lo, off)});
+            }
+            if (lane == 0) {
+              run_v[warp][nrun][0] = df_to_double(r0);
+              run_v[warp][nrun][1] = df_to_double(r1);
+              run_v[warp][nrun][2] = df_to_double(r2);
+              run_at[warp][nrun] = cur;
+            }
+            ++nrun;
+          };
           for (int c0c = h * (kNc / 2); c0c < (h + 1) * (kNc / 2); c0c += 4) {
             df32 y[4];
             load4(c0c, first_group, y);
@@ -523,8 +557,13 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
             for (int j = 0; j < 4; ++j) {
               const int col = c0c + j;
               const int i = nc + col;
-              double v0 = 0.0, v1 = 0.0, v2 = 0.0;
-              if (i < m && live && A.ao_atom[s_ao[i]] != hg) {
+              const int at = i < m ? A.ao_atom[s_ao[i]] : -1;  // the same for the whole warp
+              if (at != cur) {
+                if (cur >= 0) flush();
+                cur = at;
+                r0 = r1 = r2 = df32{0.f, 0.f};
+              }
+              if (i < m && live && at != hg) {
                 const df32 yv = df_ldexp(y[j], ep + s_fx[col]);
                 const size_t o = (size_t)i * 128 + g;
                 const df32 t = df32{th[o], tl[o]};
@@ -536,54 +575,40 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
                 const df32 a0 = df_add(df_add(df_mul(c0, d0), df_mul(ux, hxx)), df_add(df_mul(uy, hxy), df_mul(uz, hxz)));
                 const df32 a1 = df_add(df_add(df_mul(c0, d1), df_mul(ux, hxy)), df_add(df_mul(uy, hyy), df_mul(uz, hyz)));
                 const df32 a2 = df_add(df_add(df_mul(c0, d2), df_mul(ux, hxz)), df_add(df_mul(uy, hyz), df_mul(uz, hzz)));
-                v0 = scale * df_to_double(df_add(df_mul(a0, t), df_mul(d0, yv)));
-                v1 = scale * df_to_double(df_add(df_mul(a1, t), df_mul(d1, yv)));
-                v2 = scale * df_to_double(df_add(df_mul(a2, t), df_mul(d2, yv)));
-                hs0 += v0;
-                hs1 += v1;
-                hs2 += v2;
-              }
-#pragma unroll
-              for (int off = 16; off > 0; off >>= 1) {
-                v0 += __shfl_xor_sync(0xffffffffu, v0, off);
-                v1 += __shfl_xor_sync(0xffffffffu, v1, off);
-                v2 += __shfl_xor_sync(0xffffffffu, v2, off);
-              }
-              if (lane == 0) {
-                red[warp][col & 31][0] = v0;
-                red[warp][col & 31][1] = v1;
-                red[warp][col & 31][2] = v2;
+                const df32 v0 = df_add(df_mul(a0, t), df_mul(d0, yv));
+                const df32 v1 = df_add(df_mul(a1, t), df_mul(d1, yv));
+                const df32 v2 = df_add(df_mul(a2, t), df_mul(d2, yv));
+                r0 = df_add(r0, v0);
+                r1 = df_add(r1, v1);
+                r2 = df_add(r2, v2);
+                hs0 = df_add(hs0, v0);
+                hs1 = df_add(hs1, v1);
+                hs2 = df_add(hs2, v2);
               }
             }
           }
+          if (cur >= 0) flush();
+          if (lane == 0) run_n[warp] = nrun;
         });
         if (failed) break;
-        // the chunk's row sums, in column order, into the batch's per-atom row (runs of one atom
-        // are summed first)
+        // the runs' sums, group by group in column order, into the batch's per-atom row
         if (tid < 3) {
-          double run = 0.0;
-          int cur = -1;
-          for (int col = 0; col < kNc && nc + col < m; ++col) {
-            const int at = A.ao_atom[s_ao[nc + col]];
-            const int w0 = 4 * (col >> 5), cc = col & 31;
-            const double v = red[w0][cc][tid] + red[w0 + 1][cc][tid] + red[w0 + 2][cc][tid] + red[w0 + 3][cc][tid];
-            if (at != cur) {
-              if (cur >= 0) out[3 * cur + tid] += run;
-              cur = at;
-              run = 0.0;
+          for (int grp = 0; grp < 2; ++grp) {
+            const int w0 = 4 * grp;
+            for (int r = 0; r < run_n[w0]; ++r) {
+              const double v = run_v[w0][r][tid] + run_v[w0 + 1][r][tid] + run_v[w0 + 2][r][tid] + run_v[w0 + 3][r][tid];
+              out[3 * run_at[w0][r] + tid] += scale * v;
             }
-            run += v;
           }
-          if (cur >= 0) out[3 * cur + tid] += run;
         }
         __syncthreads();
       }
     }
     if (failed) break;
     // host-atom term: minus every point's total
-    hsum[h][0][g] = hs0;
-    hsum[h][1][g] = hs1;
-    hsum[h][2][g] = hs2;
+    hsum[h][0][g] = df_to_double(hs0);
+    hsum[h][1][g] = df_to_double(hs1);
+    hsum[h][2][g] = df_to_double(hs2);
     __syncthreads();
     if (tid < 3) {
       double run = 0.0;
@@ -591,13 +616,13 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
       for (int gg = 0; gg < bd.n_pts; ++gg) {
         const int at = s_host[gg];
         if (at != cur) {
-          if (cur >= 0) out[3 * cur + tid] -= run;
+          if (cur >= 0) out[3 * cur + tid] -= scale * run;
           cur = at;
           run = 0.0;
         }
         run += hsum[0][tid][gg] + hsum[1][tid][gg];
       }
-      if (cur >= 0) out[3 * cur + tid] -= run;
+      if (cur >= 0) out[3 * cur + tid] -= scale * run;
     }
     // (E) Becke weight derivative: teams of 1-8 warps per point with the pair tables in the (idle)
     // stage when one team's tables fit, else one warp per point with tables in the scratch slab
