@@ -107,30 +107,79 @@ __device__ void ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restr
         on = !(fabsf(r0.hi) < 1e-18f && fabsf(r1.hi) < 1e-18f);
       }
     }
+    // per shell: r1 * (dx, dy, dz), and the squares for d shells
+    df32 r1x = {0.f, 0.f}, r1y = r1x, r1z = r1x, x2 = r1x, y2 = r1x, z2 = r1x;
+    if (on) {
+      r1x = df_mul(r1, dx);
+      r1y = df_mul(r1, dy);
+      r1z = df_mul(r1, dz);
+      if (sh.n_funcs == 6) {
+        x2 = df_mul(dx, dx);
+        y2 = df_mul(dy, dy);
+        z2 = df_mul(dz, dz);
+      }
+    }
     for (int c = 0; c < sh.n_funcs; ++c) {
       df32 v = {0.f, 0.f}, gx = {0.f, 0.f}, gy = {0.f, 0.f}, gz = {0.f, 0.f};
       if (on) {
         const AoCompGpu cp = G.comps[sh.comp_start + c];
         const float2 sc = G.comp_f[sh.comp_start + c];
         const df32 s = {sc.x, sc.y};
-        // x^l and its derivative l x^(l-1)
-        df32 px = {1.f, 0.f}, dpx = {0.f, 0.f}, py = {1.f, 0.f}, dpy = {0.f, 0.f}, pz = {1.f, 0.f}, dpz = {0.f, 0.f};
-        if (cp.lx >= 1) { dpx = px; px = dx; }
-        if (cp.lx >= 2) { dpx = df_mul_f(dx, 2.f); px = df_mul(dx, dx); }
-        if (cp.lx >= 3) { dpx = df_mul_f(px, 3.f); px = df_mul(px, dx); }
-        if (cp.ly >= 1) { dpy = py; py = dy; }
-        if (cp.ly >= 2) { dpy = df_mul_f(dy, 2.f); py = df_mul(dy, dy); }
-        if (cp.ly >= 3) { dpy = df_mul_f(py, 3.f); py = df_mul(py, dy); }
-        if (cp.lz >= 1) { dpz = pz; pz = dz; }
-        if (cp.lz >= 2) { dpz = df_mul_f(dz, 2.f); pz = df_mul(dz, dz); }
-        if (cp.lz >= 3) { dpz = df_mul_f(pz, 3.f); pz = df_mul(pz, dz); }
-        const df32 yz = df_mul(py, pz), xz = df_mul(px, pz), xy = df_mul(px, py);
-        const df32 mm = df_mul(px, yz);
-        const df32 mr1 = df_mul(mm, r1);
-        v = df_mul(s, df_mul(mm, r0));
-        gx = df_mul(s, df_add(df_mul(df_mul(dpx, yz), r0), df_mul(mr1, dx)));
-        gy = df_mul(s, df_add(df_mul(df_mul(dpy, xz), r0), df_mul(mr1, dy)));
-        gz = df_mul(s, df_add(df_mul(df_mul(dpz, xy), r0), df_mul(mr1, dz)));
+        const int lsum = cp.lx + cp.ly + cp.lz;
+        if (lsum <= 2) {
+          // monomial mm = x^lx y^ly z^lz and its derivatives m_q (uniform branches: one component
+          // per thread group); phi = s mm r0, d/dq phi = s (m_q r0 + mm r1 q)
+          df32 mm = {1.f, 0.f};
+          df32 mqx = {0.f, 0.f}, mqy = mqx, mqz = mqx;
+          if (lsum == 1) {
+            mm = cp.lx ? dx : (cp.ly ? dy : dz);
+          } else if (lsum == 2) {
+            if (cp.lx == 2) { mm = x2; mqx = df_mul_f(dx, 2.f); }
+            else if (cp.ly == 2) { mm = y2; mqy = df_mul_f(dy, 2.f); }
+            else if (cp.lz == 2) { mm = z2; mqz = df_mul_f(dz, 2.f); }
+            else if (cp.lz == 0) { mm = df_mul(dx, dy); mqx = dy; mqy = dx; }
+            else if (cp.ly == 0) { mm = df_mul(dx, dz); mqx = dz; mqz = dx; }
+            else { mm = df_mul(dy, dz); mqy = dz; mqz = dy; }
+          }
+          v = df_mul(mm, r0);
+          gx = df_mul(mm, r1x);
+          gy = df_mul(mm, r1y);
+          gz = df_mul(mm, r1z);
+          if (lsum == 1) {  // m_q = 1 on the component's axis
+            if (cp.lx) gx = df_add(gx, r0);
+            else if (cp.ly) gy = df_add(gy, r0);
+            else gz = df_add(gz, r0);
+          } else if (lsum == 2) {
+            if (cp.lx) gx = df_add(gx, df_mul(mqx, r0));
+            if (cp.ly) gy = df_add(gy, df_mul(mqy, r0));
+            if (cp.lz) gz = df_add(gz, df_mul(mqz, r0));
+          }
+          if (!(sc.x == 1.f && sc.y == 0.f)) {
+            v = df_mul(s, v);
+            gx = df_mul(s, gx);
+            gy = df_mul(s, gy);
+            gz = df_mul(s, gz);
+          }
+        } else {
+          // x^l and its derivative l x^(l-1)
+          df32 px = {1.f, 0.f}, dpx = {0.f, 0.f}, py = {1.f, 0.f}, dpy = {0.f, 0.f}, pz = {1.f, 0.f}, dpz = {0.f, 0.f};
+          if (cp.lx >= 1) { dpx = px; px = dx; }
+          if (cp.lx >= 2) { dpx = df_mul_f(dx, 2.f); px = df_mul(dx, dx); }
+          if (cp.lx >= 3) { dpx = df_mul_f(px, 3.f); px = df_mul(px, dx); }
+          if (cp.ly >= 1) { dpy = py; py = dy; }
+          if (cp.ly >= 2) { dpy = df_mul_f(dy, 2.f); py = df_mul(dy, dy); }
+          if (cp.ly >= 3) { dpy = df_mul_f(py, 3.f); py = df_mul(py, dy); }
+          if (cp.lz >= 1) { dpz = pz; pz = dz; }
+          if (cp.lz >= 2) { dpz = df_mul_f(dz, 2.f); pz = df_mul(dz, dz); }
+          if (cp.lz >= 3) { dpz = df_mul_f(pz, 3.f); pz = df_mul(pz, dz); }
+          const df32 yz = df_mul(py, pz), xz = df_mul(px, pz), xy = df_mul(px, py);
+          const df32 mm = df_mul(px, yz);
+          const df32 mr1 = df_mul(mm, r1);
+          v = df_mul(s, df_mul(mm, r0));
+          gx = df_mul(s, df_add(df_mul(df_mul(dpx, yz), r0), df_mul(mr1, dx)));
+          gy = df_mul(s, df_add(df_mul(df_mul(dpy, xz), r0), df_mul(mr1, dy)));
+          gz = df_mul(s, df_add(df_mul(df_mul(dpz, xy), r0), df_mul(mr1, dz)));
+        }
         if (!(fabsf(v.hi) > 1e-16f || fabsf(gx.hi) > 1e-16f || fabsf(gy.hi) > 1e-16f || fabsf(gz.hi) > 1e-16f))
           v = gx = gy = gz = df32{0.f, 0.f};
       }

@@ -51,6 +51,29 @@ def test_no_device_means_error_codes_not_fallback(native_lib):
     n = np.zeros(1, np.int32)
     assert native_lib.calchem_xc_grid_build(1, _native.ptr(z), _native.ptr(xyz), 2, 0, 5, _native.ptr(n)) == -3
     assert native_lib.calchem_xc_grid_build(1, _native.ptr(z), _native.ptr(xyz), 9, 0, 5, _native.ptr(n)) == -1
+    # the XC gradient entry points: argument checks first, then "no device"
+    g = np.zeros((1, 3))
+    raw = np.ones(8)
+    host = np.zeros(8, np.int32)
+    assert native_lib.calchem_xc_nuclear_gradient(1, 3, 0, 1, _native.ptr(z), _native.ptr(xyz), _native.ptr(raw),
+                                                  _native.ptr(host), 8, _native.ptr(P), None, _native.ptr(g)) == -3
+    assert native_lib.calchem_xc_nuclear_gradient(1, 3, 2, 1, _native.ptr(z), _native.ptr(xyz), _native.ptr(raw),
+                                                  _native.ptr(host), 8, _native.ptr(P), None, _native.ptr(g)) == -1
+    assert native_lib.calchem_xc_nuclear_gradient(1, 99, 0, 1, _native.ptr(z), _native.ptr(xyz), _native.ptr(raw),
+                                                  _native.ptr(host), 8, _native.ptr(P), None, _native.ptr(g)) == -1
+    wxc = np.zeros((8, 8))
+    assert native_lib.calchem_cuda_vxc_grad_force(1, _native.ptr(P), None, 1, _native.ptr(wxc), _native.ptr(g), 8, 4,
+                                                  1, 0) == -3
+    assert native_lib.calchem_cuda_vxc_grad_force(1, _native.ptr(P), None, 0, _native.ptr(wxc), _native.ptr(g), 8, 4,
+                                                  1, 0) == -1
+
+
+def test_gradient_has_no_cpu_path():
+    from calchem_gb300 import xc_nuclear_gradient_with_gpu
+    from tests.helpers import distorted_water
+    mol = distorted_water()
+    with pytest.raises(NotImplementedError):
+        xc_nuclear_gradient_with_gpu(mol, None, None, "pbe", np.eye(2), np.eye(2), use_gpu=False)
 
 
 def test_version_string(native_lib):
