@@ -72,8 +72,10 @@ static_assert(2 * (kSmemBytes + 1024) <= 233472, "two CTAs must fit in one SM's 
 // (A) AO values and gradients in double-float.  Planes p = 0..3 (phi, d/dx, d/dy, d/dz) hold the
 // FP32 hi parts at planes + p * P and the lo parts, rounded to BF16 (lo <= ulp(hi) / 2, so hi + lo
 // keeps ~32 significant bits), at lo_planes + p * P; row = local AO, column = point.
-__device__ void ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restrict__ planes,
-                           __nv_bfloat16* __restrict__ lo_planes, size_t P, int m_pad, const df32* tab) {
+// Returns the largest |phi| hi part this thread wrote (the point's row scale needs the maximum).
+__device__ float ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restrict__ planes,
+                            __nv_bfloat16* __restrict__ lo_planes, size_t P, int m_pad, const df32* tab) {
+  float vmax = 0.f;
   const int tid = threadIdx.x;
   const int g = tid & 127;
   const bool live = g < bd.n_pts;
@@ -184,6 +186,7 @@ __device__ void ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restr
           v = gx = gy = gz = df32{0.f, 0.f};
       }
       const size_t o = (size_t)(loc + c) * 128 + g;
+      vmax = fmaxf(vmax, fabsf(v.hi));
       planes[o] = v.hi;
       planes[P + o] = gx.hi;
       planes[2 * P + o] = gy.hi;
@@ -204,6 +207,7 @@ __device__ void ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restr
       lo_planes[p * P + o] = __float2bfloat16_rn(0.f);
     }
   }
+  return vmax;
 }
 
 // (B) the GEMM1 A operand of the whole batch: for K block kb, tile q (q = 0..3: pieces of weight
@@ -341,12 +345,9 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
     const int m_pad = (m + 127) / 128 * 128;
     const int nkb = (m + 63) / 64;
     for (int i = tid; i < m; i += kMT) s_ao[i] = G.batch_ao[bd.ao_start + i];
-    ao_eval_df(G, bd, planes, lo_planes, P, m_pad, s_tab);
-    __syncthreads();
+    const float vmax = ao_eval_df(G, bd, planes, lo_planes, P, m_pad, s_tab);
     {  // e_g: power-of-two exponent with max_mu |Phi[g][mu]| 2^-e_g < 1
-      float mx = 0.f;
-      for (int i = h; i < m; i += kGroups) mx = fmaxf(mx, fabsf(planes[(size_t)i * 128 + g]));
-      dens[0][0][g + 128 * h] = (double)mx;  // scratch
+      dens[0][0][g + 128 * h] = (double)vmax;  // scratch: the stage is idle
       __syncthreads();
       if (h == 0) {
         float t = 0.f;
