@@ -79,8 +79,10 @@ __device__ __forceinline__ df32 ld_df(const float* hi, const __nv_bfloat16* lo, 
 __device__ __forceinline__ df32 df_fma(df32 a, df32 b, df32 c) { return df_add(df_mul(a, b), c); }
 
 // (A) values, gradients and Hessians of the batch's AOs in double-float (rows [m, m_pad) zeroed).
-__device__ void ao_eval_df_hess(const DevGrid& G, const BatchDesc& bd, float* __restrict__ hi,
-                                __nv_bfloat16* __restrict__ lo, size_t P, int m_pad, const df32* tab) {
+// Returns the largest |phi| hi part this thread wrote.
+__device__ float ao_eval_df_hess(const DevGrid& G, const BatchDesc& bd, float* __restrict__ hi,
+                                 __nv_bfloat16* __restrict__ lo, size_t P, int m_pad, const df32* tab) {
+  float vmax = 0.f;
   const int tid = threadIdx.x;
   const int g = tid & 127;
   const bool live = g < bd.n_pts;
@@ -162,6 +164,7 @@ __device__ void ao_eval_df_hess(const DevGrid& G, const BatchDesc& bd, float* __
                                 df_mul(mr2, df_mul(dz, dz))));
       }
       const size_t off = (size_t)(loc + c) * 128 + g;
+      vmax = fmaxf(vmax, fabsf(o[0].hi));
 #pragma unroll
       for (int k = 0; k < kPlanesG; ++k) {
         hi[k * P + off] = o[k].hi;
@@ -178,6 +181,7 @@ __device__ void ao_eval_df_hess(const DevGrid& G, const BatchDesc& bd, float* __
       lo[k * P + o] = __float2bfloat16_rn(0.f);
     }
   }
+  return vmax;
 }
 
 // Psi = u . grad phi at row mu, point g (double-float).
@@ -188,25 +192,20 @@ __device__ __forceinline__ df32 psi_at(const float* __restrict__ hi, const __nv_
 }
 
 // GEMM1 A operand of the batch, tile (kb, piece q) at apack + (4 kb + q) * 16 KB: the rows of the
-// source (Phi, or Psi for psi != 0) scaled by 2^-e_g and cut into four fixed-point pieces.
+// source (the Phi planes, or the double-float Psi plane psi_hi / psi_lo when given) scaled by 2^-e_g
+// and cut into four fixed-point pieces.
 __device__ void pack_rows(unsigned char* __restrict__ apack, const float* __restrict__ hi,
-                          const __nv_bfloat16* __restrict__ lo, size_t P, const int* s_e, int nkb, bool psi,
-                          const double* __restrict__ coef_u) {
+                          const __nv_bfloat16* __restrict__ lo, const int* s_e, int nkb,
+                          const float* __restrict__ psi_hi, const float* __restrict__ psi_lo) {
   for (int e = threadIdx.x; e < nkb * 128 * 8; e += kGM) {
     const int kb = e >> 10, g = e & 127, c = (e >> 7) & 7;
     const int mu0 = kb * 64 + c * 8;
     const int eg = s_e[g];
-    df32 ux = {0.f, 0.f}, uy = ux, uz = ux;
-    if (psi) {
-      ux = df_from_double(coef_u[g]);
-      uy = df_from_double(coef_u[128 + g]);
-      uz = df_from_double(coef_u[256 + g]);
-    }
     __nv_bfloat16 h[8], md[8], l[8], q[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       const size_t o = (size_t)(mu0 + k) * 128 + g;
-      const df32 v = psi ? psi_at(hi, lo, P, o, ux, uy, uz) : ld_df(hi, lo, o);
+      const df32 v = psi_hi ? df32{psi_hi[o], psi_lo[o]} : ld_df(hi, lo, o);
       fixsplit4(ldexpf(v.hi, -eg), ldexpf(v.lo, -eg), h[k], md[k], l[k], q[k]);
     }
     unsigned char* t = apack + (size_t)kb * 65536 + sw128(g, c);
@@ -271,7 +270,9 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
   __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(hi + kPlanesG * P);
   float* t_hi = reinterpret_cast<float*>(lo + kPlanesG * P);  // [2][P]
   float* t_lo = t_hi + 2 * P;                                 // [2][P]
-  unsigned char* apack = reinterpret_cast<unsigned char*>(t_lo + 2 * P);  // m_pad_all / 64 x 64 KB
+  float* p_hi = t_lo + 2 * P;                                  // Psi of the current spin
+  float* p_lo = p_hi + P;
+  unsigned char* apack = reinterpret_cast<unsigned char*>(p_lo + P);  // m_pad_all / 64 x 64 KB
   double* coef = reinterpret_cast<double*>(apack + (size_t)m_pad_all * 1024);  // [9][128]
   double* bscr = coef + 9 * 128;
   const size_t per_warp = becke_scratch_doubles(A.n_atoms);
@@ -397,12 +398,9 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
     double* out = A.part + (size_t)b * na3;
     for (int i = tid; i < m; i += kGM) s_ao[i] = G.batch_ao[bd.ao_start + i];
     if (tid < 128) s_host[g] = live ? A.host[pt] : -1;
-    ao_eval_df_hess(G, bd, hi, lo, P, m_pad, s_tab);
-    __syncthreads();
+    const float vmax = ao_eval_df_hess(G, bd, hi, lo, P, m_pad, s_tab);
     {  // e_g: power-of-two exponent with max_mu |Phi[g][mu]| 2^-e_g < 1
-      float mx = 0.f;
-      for (int i = h; i < m; i += 2) mx = fmaxf(mx, fabsf(hi[(size_t)i * 128 + g]));
-      dens[0][0][g + 128 * h] = (double)mx;
+      dens[0][0][g + 128 * h] = (double)vmax;  // scratch: the stage is idle
       __syncthreads();
       if (h == 0) {
         int ex = 0;
@@ -411,7 +409,7 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
       }
       __syncthreads();
     }
-    pack_rows(apack, hi, lo, P, s_eg, nkb, false, nullptr);
+    pack_rows(apack, hi, lo, s_eg, nkb, nullptr, nullptr);
     fence_proxy_async_global();  // the packed tiles are read by bulk copies
     __syncthreads();
 
@@ -511,9 +509,15 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
       const df32 ux = df_from_double(coef[(4 * s + 1) * 128 + g]);
       const df32 uy = df_from_double(coef[(4 * s + 2) * 128 + g]);
       const df32 uz = df_from_double(coef[(4 * s + 3) * 128 + g]);
-      {  // e'_g for Psi
+      {  // Psi into its plane (rows up to m_pad: the padding rows give zeros), and e'_g
         float mx = 0.f;
-        for (int i = h; i < m; i += 2) mx = fmaxf(mx, fabsf(psi_at(hi, lo, P, (size_t)i * 128 + g, ux, uy, uz).hi));
+        for (int i = h; i < m_pad; i += 2) {
+          const size_t o = (size_t)i * 128 + g;
+          const df32 ps = psi_at(hi, lo, P, o, ux, uy, uz);
+          p_hi[o] = ps.hi;
+          p_lo[o] = ps.lo;
+          mx = fmaxf(mx, fabsf(ps.hi));
+        }
         dens[0][0][g + 128 * h] = (double)mx;
         __syncthreads();
         if (h == 0) {
@@ -523,7 +527,7 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
         }
         __syncthreads();
       }
-      pack_rows(apack, hi, lo, P, s_ep, nkb, true, coef + (4 * s + 1) * 128);
+      pack_rows(apack, hi, lo, s_ep, nkb, p_hi, p_lo);
       fence_proxy_async_global();
       __syncthreads();
       const int ep = s_ep[g];
@@ -695,8 +699,8 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
 
 size_t grad_mixed_slab_doubles(int max_m, int n_atoms) {
   const size_t m_pad = (size_t)(max_m + 127) / 128 * 128, P = m_pad * 128;
-  // planes: 10 FP32 + 10 BF16; T planes: 2 spins x (FP32 hi + FP32 lo); packed A operand (8 B)
-  const size_t bytes = P * (kPlanesG * 4 + kPlanesG * 2 + 16 + 8) + 9 * 128 * sizeof(double) +
+  // planes: 10 FP32 + 10 BF16; T planes: 2 spins x (FP32 hi + FP32 lo); Psi (FP32 hi + lo); packed A
+  const size_t bytes = P * (kPlanesG * 4 + kPlanesG * 2 + 16 + 8 + 8) + 9 * 128 * sizeof(double) +
                        (size_t)kGWarpsM * becke_scratch_doubles(n_atoms) * sizeof(double);
   return (bytes / sizeof(double) + 127) / 128 * 128;  // 1 KB multiples keep every CTA's slab aligned
 }
