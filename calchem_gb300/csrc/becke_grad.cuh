@@ -324,18 +324,17 @@ __host__ __device__ constexpr size_t becke_cta_bytes(int n) {
 }
 
 struct BeckeCta {
-  df32* dist;
-  double *cell, *tmp, *wacc, *hq;
+  df32 *dist, *cell, *tmp, *wacc, *hq;
   df32* pp;
   int* cnt;
   df32 *su, *scu, *lu;
   __device__ void carve(unsigned char* base, int n) {
     dist = reinterpret_cast<df32*>(base);
-    cell = reinterpret_cast<double*>(dist + n);
+    cell = dist + n;
     tmp = cell + n;
     wacc = tmp + 3 * n;
     hq = wacc + 3 * n;
-    pp = reinterpret_cast<df32*>(hq + 4);
+    pp = hq + 4;
     cnt = reinterpret_cast<int*>(pp + n);
     su = reinterpret_cast<df32*>(cnt + n + (n & 1));  // 8-byte aligned
     const size_t np = (size_t)n * (n - 1) / 2;
@@ -374,12 +373,13 @@ __device__ __forceinline__ void team_sync(int nt, int team) {
 // Called by every thread of a team (threads tid = 0..nt-1 of the team, team index `team`) for one
 // point (uniform arguments within the team).  T.wacc collects the weight-derivative sums of the
 // team's points and must be zeroed by the caller.
-static __device__ void becke_point_team(int n, const double* __restrict__ xyz, const df32* __restrict__ pdf, int host,
-                                        double x, double y, double z, double pref_in, const BeckeCta& T, int tid,
-                                        int nth, int team) {
+static __device__ void becke_point_team(int n, const df32* __restrict__ xyz_df, const df32* __restrict__ pdf, int host,
+                                        df32 x, df32 y, df32 z, df32 pref_in, const BeckeCta& T, int tid, int nth,
+                                        int team) {
+  // everything below is double-float arithmetic on the FP32 pipe (GB300's FP64 rate is 1/64 of it)
   for (int c = tid; c < n; c += nth) {
-    const double dx = x - xyz[3 * c], dy = y - xyz[3 * c + 1], dz = z - xyz[3 * c + 2];
-    T.dist[c] = df_from_double(sqrt(dx * dx + dy * dy + dz * dz));
+    const df32 dx = df_sub(x, xyz_df[3 * c]), dy = df_sub(y, xyz_df[3 * c + 1]), dz = df_sub(z, xyz_df[3 * c + 2]);
+    T.dist[c] = df_sqrt(df_add(df_add(df_mul(dx, dx), df_mul(dy, dy)), df_mul(dz, dz)));
   }
   team_sync(nth, team);
   const int np = n * (n - 1) / 2;
@@ -415,18 +415,18 @@ static __device__ void becke_point_team(int n, const double* __restrict__ xyz, c
     }
     T.pp[c] = pr;
     T.cnt[c] = k;
-    T.cell[c] = k == 0 ? df_to_double(pr) : 0.0;
+    T.cell[c] = k == 0 ? pr : df32{0.f, 0.f};
   }
   team_sync(nth, team);
   if (tid == 0) {
-    double zs = 0.0;
-    for (int c = 0; c < n; ++c) zs += T.cell[c];
+    df32 zs = {0.f, 0.f};
+    for (int c = 0; c < n; ++c) zs = df_add(zs, T.cell[c]);
     T.hq[3] = zs;
   }
   team_sync(nth, team);
-  const double zs = T.hq[3];
-  if (zs <= 1e-30) return;  // uniform: every thread read the same value
-  const double wn = T.cell[host] / zs, pref = pref_in / zs;
+  const df32 zs = T.hq[3];
+  if (zs.hi <= 1e-30f) return;  // uniform: every thread read the same value
+  const df32 wn = df_div(T.cell[host], zs), pref = df_div(pref_in, zs);
   int L = 1;
   while (L < 32 && 2 * L * n <= nth) L *= 2;
   const int groups = nth / L, sub = tid % L;
@@ -440,13 +440,12 @@ static __device__ void becke_point_team(int n, const double* __restrict__ xyz, c
     bool act = false;
     if (a < n && a != host) {
       const df32 dra = T.dist[a];
-      const double ra = df_to_double(dra);
-      act = ra >= 1e-14;
+      act = dra.hi >= 1e-14f;
       if (act) {
-        const double ir = 1.0 / ra;
-        dr0 = df_from_double(-(x - xyz[3 * a]) * ir);
-        dr1 = df_from_double(-(y - xyz[3 * a + 1]) * ir);
-        dr2 = df_from_double(-(z - xyz[3 * a + 2]) * ir);
+        const df32 ir = df_div(df32{1.f, 0.f}, dra);
+        dr0 = df_mul(df_sub(xyz_df[3 * a], x), ir);
+        dr1 = df_mul(df_sub(xyz_df[3 * a + 1], y), ir);
+        dr2 = df_mul(df_sub(xyz_df[3 * a + 2], z), ir);
         for (int b = sub; b < n; b += L) {
           const df32* t = pdf + 5 * ((size_t)a * n + b);
           const df32 inv = t[0];
@@ -487,22 +486,23 @@ static __device__ void becke_point_team(int n, const double* __restrict__ xyz, c
       ph1 = df_add(ph1, df32{__shfl_xor_sync(0xffffffffu, ph1.hi, o), __shfl_xor_sync(0xffffffffu, ph1.lo, o)});
       ph2 = df_add(ph2, df32{__shfl_xor_sync(0xffffffffu, ph2.hi, o), __shfl_xor_sync(0xffffffffu, ph2.lo, o)});
     }
-    const df32 zz0 = df_sub(df_mul(dr0, cs), w0), zz1 = df_sub(df_mul(dr1, cs), w1), zz2 = df_sub(df_mul(dr2, cs), w2);
     if (sub == 0 && a < n) {
-      T.tmp[3 * a] = act ? pref * (df_to_double(ph0) - wn * df_to_double(zz0)) : 0.0;
-      T.tmp[3 * a + 1] = act ? pref * (df_to_double(ph1) - wn * df_to_double(zz1)) : 0.0;
-      T.tmp[3 * a + 2] = act ? pref * (df_to_double(ph2) - wn * df_to_double(zz2)) : 0.0;
+      const df32 zz0 = df_sub(df_mul(dr0, cs), w0), zz1 = df_sub(df_mul(dr1, cs), w1), zz2 = df_sub(df_mul(dr2, cs), w2);
+      const df32 zero = {0.f, 0.f};
+      T.tmp[3 * a] = act ? df_mul(pref, df_sub(ph0, df_mul(wn, zz0))) : zero;
+      T.tmp[3 * a + 1] = act ? df_mul(pref, df_sub(ph1, df_mul(wn, zz1))) : zero;
+      T.tmp[3 * a + 2] = act ? df_mul(pref, df_sub(ph2, df_mul(wn, zz2))) : zero;
     }
   }
   team_sync(nth, team);
   if (tid < 3) {
-    double h = 0.0;
+    df32 h = {0.f, 0.f};
     for (int a = 0; a < n; ++a)
-      if (a != host) h -= T.tmp[3 * a + tid];
+      if (a != host) h = df_sub(h, T.tmp[3 * a + tid]);
     T.hq[tid] = h;
   }
   team_sync(nth, team);
-  for (int k = tid; k < 3 * n; k += nth) T.wacc[k] += (k / 3 == host) ? T.hq[k % 3] : T.tmp[k];
+  for (int k = tid; k < 3 * n; k += nth) T.wacc[k] = df_add(T.wacc[k], (k / 3 == host) ? T.hq[k % 3] : T.tmp[k]);
   team_sync(nth, team);
 }
 

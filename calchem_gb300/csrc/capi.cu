@@ -614,8 +614,10 @@ struct GradBufs {
   int *host = nullptr, *ao_atom = nullptr, *counter = nullptr;
   int2* pairs = nullptr;
   float2* pair_df = nullptr;
+  double *fx = nullptr, *part2 = nullptr;  // tensor-core form: per-point f, weight-derivative rows
   ~GradBufs() {
-    void* ptrs[] = {pa, pb, wxc, raw, xyz, inv, aij, part, slab, grad, host, ao_atom, counter, pairs, pair_df};
+    void* ptrs[] = {pa, pb, wxc, raw, xyz, inv, aij, part, slab, grad, host, ao_atom, counter, pairs, pair_df,
+                    fx, part2};
     for (void* p : ptrs)
       if (p) cudaFree(p);
   }
@@ -684,6 +686,10 @@ int gradient_run(Entry& e, int xc, int precision, bool closed, const double* h_p
                     : dalloc(&B.raw, e.n_pts) && dalloc(&B.xyz, na3) && dalloc(&B.inv, inv_r.size()) &&
                           dalloc(&B.aij, a_ij.size()) && dalloc(&B.pairs, pairs.size()) &&
                           dalloc(&B.pair_df, pair_df.size()));
+  // the tensor-core form runs the weight derivative as its own kernel when its tables fit
+  const bool becke_apart = mixed && xc >= 0 && becke_kernel_fits(n_atoms);
+  const int n_bk = becke_apart ? becke_kernel_ctas(e.n_pts) : 0;
+  if (ok && becke_apart) ok = dalloc(&B.fx, e.n_pts) && dalloc(&B.part2, (size_t)n_bk * na3);
   if (!ok) {
     cudaGetLastError();
     return -4;
@@ -695,7 +701,8 @@ int gradient_run(Entry& e, int xc, int precision, bool closed, const double* h_p
        cudaMemcpyAsync(B.ao_atom, ao_atom.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, st) ==
            cudaSuccess &&
        cudaMemsetAsync(B.counter, 0, 2 * sizeof(int), st) == cudaSuccess &&
-       (!mixed || cudaMemsetAsync(B.part, 0, (size_t)e.n_batches * na3 * sizeof(double), st) == cudaSuccess);
+       (!mixed || cudaMemsetAsync(B.part, 0, (size_t)e.n_batches * na3 * sizeof(double), st) == cudaSuccess) &&
+       (!becke_apart || cudaMemsetAsync(B.fx, 0, (size_t)e.n_pts * sizeof(double), st) == cudaSuccess);
   if (ok && xc < 0)
     ok = cudaMemcpyAsync(B.wxc, h_wxc, (size_t)e.n_pts * 8 * sizeof(double), cudaMemcpyHostToDevice, st) ==
          cudaSuccess;
@@ -726,6 +733,7 @@ int gradient_run(Entry& e, int xc, int precision, bool closed, const double* h_p
   A.pairs = B.pairs;
   A.n_pairs = (int)pairs.size();
   A.pair_df = B.pair_df;
+  A.fx_out = B.fx;
   A.n_atoms = n_atoms;
   A.max_m = e.max_m;
   A.part = B.part;
@@ -747,11 +755,19 @@ int gradient_run(Entry& e, int xc, int precision, bool closed, const double* h_p
     A.Pa = reinterpret_cast<const double*>(e.d_mixed_ws);
     A.Pb = nullptr;
     if (launch_xc_grad_mixed(dev_grid(e), A, n_ctas, B.counter + 1, st) != cudaSuccess) return -5;
+    if (becke_apart) {
+      if (launch_becke_mixed(dev_grid(e), A, B.fx, B.part2, st) != cudaSuccess) return -5;
+      ++launches;
+    }
   } else if (launch_xc_grad(dev_grid(e), A, n_ctas, st) != cudaSuccess) {
     return -5;
   }
   if (launch_grad_reduce(B.part, e.n_batches, n_atoms, B.grad, st) != cudaSuccess) return -5;
   launches += 2;
+  if (becke_apart) {
+    if (launch_grad_accumulate(B.part2, n_bk, n_atoms, B.grad, st) != cudaSuccess) return -5;
+    ++launches;
+  }
   if (e.profiling) cudaEventRecord(e.ev1, st);
   e.last_launches = launches;
   int status = 0;

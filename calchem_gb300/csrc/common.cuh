@@ -113,6 +113,9 @@ struct GradArgs {
   // per ordered pair (a, b), 5 float pairs (hi, lo): 1 / R_ab, a_ab, (R_a - R_b) / R_ab (the
   // double-float weight derivative of the tensor-core form)
   const float2* pair_df;
+  // tensor-core form: when set, the quadrature kernel writes each point's energy density f here and
+  // leaves the weight derivative to a separate kernel (becke_mixed_kernel)
+  double* fx_out;
   int n_atoms;
   int max_m;
   double* part;            // [batch][atom][3] partial sums

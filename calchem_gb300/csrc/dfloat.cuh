@@ -83,6 +83,16 @@ __device__ __forceinline__ df32 df_div(df32 a, df32 b) {
   return two_sum(q1, __fdividef(r, b.hi));
 }
 
+// sqrt(a) for a >= 0: the FP32 root and one Newton correction from the exact residual a - s^2
+// (Karp and Markstein's form of the correction).
+__device__ __forceinline__ df32 df_sqrt(df32 a) {
+  if (!(a.hi > 0.f)) return df32{0.f, 0.f};
+  const float s0 = sqrtf(a.hi);
+  const df32 p = two_prod(s0, s0);
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p.hi), p.lo), a.lo);
+  return two_sum(s0, __fdividef(r, __fmul_rn(2.f, s0)));
+}
+
 // Exact scaling by a power of two (as long as no underflow/overflow occurs).
 __device__ __forceinline__ df32 df_ldexp(df32 a, int e) { return df32{ldexpf(a.hi, e), ldexpf(a.lo, e)}; }
 

@@ -41,6 +41,13 @@ cudaError_t launch_grad_reduce(const double* part, int n_batches, int n_atoms, d
 size_t grad_mixed_slab_doubles(int max_m, int n_atoms);
 int grad_mixed_max_m();
 cudaError_t launch_xc_grad_mixed(const DevGrid& G, const GradArgs& A, int n_ctas, int* status, cudaStream_t st);
+// The weight derivative of the tensor-core form as its own kernel (GradArgs.fx_out given to the
+// quadrature kernel): per-CTA rows of per-atom sums in part [becke_kernel_ctas(n_pts)][3 n_atoms].
+bool becke_kernel_fits(int n_atoms);
+int becke_kernel_ctas(int n_pts);
+cudaError_t launch_becke_mixed(const DevGrid& G, const GradArgs& A, const double* fx, double* part, cudaStream_t st);
+// grad[k] += sum over rows r (in order) of part[r][k]
+cudaError_t launch_grad_accumulate(const double* part, int n_rows, int n_atoms, double* grad, cudaStream_t st);
 // Dynamic shared-memory limits of the persistent kernels, set once per process (the launchers call
 // these; a graph capture calls them first so that no attribute is set while capturing).
 cudaError_t fp64_set_attributes();

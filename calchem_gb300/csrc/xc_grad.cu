@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(kGT, 1) xc_grad_kernel(DevGrid G, GradArgs A) 
 
 // grad[k] = sum over batches b (in order) of part[b][k]; one CTA per entry k.
 __global__ void __launch_bounds__(256) grad_reduce_kernel(const double* __restrict__ part, int n_batches, int na3,
-                                                          double* __restrict__ grad) {
+                                                          double* __restrict__ grad, int accumulate) {
   __shared__ double s[256];
   const int k = blockIdx.x, t = threadIdx.x;
   double v = 0.0;
@@ -447,7 +447,7 @@ __global__ void __launch_bounds__(256) grad_reduce_kernel(const double* __restri
     if (t < o) s[t] += s[t + o];
     __syncthreads();
   }
-  if (t == 0) grad[k] = s[0];
+  if (t == 0) grad[k] = accumulate ? grad[k] + s[0] : s[0];
 }
 
 }  // namespace
@@ -470,7 +470,12 @@ cudaError_t launch_xc_grad(const DevGrid& G, const GradArgs& A, int n_ctas, cuda
 }
 
 cudaError_t launch_grad_reduce(const double* part, int n_batches, int n_atoms, double* grad, cudaStream_t st) {
-  grad_reduce_kernel<<<3 * n_atoms, 256, 0, st>>>(part, n_batches, 3 * n_atoms, grad);
+  grad_reduce_kernel<<<3 * n_atoms, 256, 0, st>>>(part, n_batches, 3 * n_atoms, grad, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grad_accumulate(const double* part, int n_rows, int n_atoms, double* grad, cudaStream_t st) {
+  grad_reduce_kernel<<<3 * n_atoms, 256, 0, st>>>(part, n_rows, 3 * n_atoms, grad, 1);
   return cudaGetLastError();
 }
 

@@ -495,6 +495,7 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
       }
 #pragma unroll
       for (int k = 0; k < 9; ++k) coef[k * 128 + g] = cf[k];
+      if (A.fx_out && live) A.fx_out[pt] = cf[8];
     }
     __syncthreads();
 
@@ -632,22 +633,28 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
     // stage when one team's tables fit, else one warp per point with tables in the scratch slab
     __syncthreads();
     const size_t team_bytes = becke::becke_cta_bytes(A.n_atoms);
-    const bool cta_becke = team_bytes <= (size_t)kStageG;
-    if (A.n_atoms > 1 && cta_becke) {
+    const bool cta_becke = team_bytes + (size_t)24 * A.n_atoms <= (size_t)kStageG;
+    if (A.fx_out) {
+      // the weight derivative runs as becke_mixed_kernel
+    } else if (A.n_atoms > 1 && cta_becke) {
       int n_teams = 1;
-      while (n_teams < kGWarpsM && (size_t)(2 * n_teams) * team_bytes <= (size_t)kStageG) n_teams *= 2;
+      while (n_teams < kGWarpsM && (size_t)(2 * n_teams) * team_bytes + (size_t)24 * A.n_atoms <= (size_t)kStageG)
+        n_teams *= 2;
       const int nt = kGM / n_teams, team = tid / nt, tt = tid % nt;
+      df32* xyz_df = reinterpret_cast<df32*>(stage + (size_t)n_teams * team_bytes);
+      for (int k = tid; k < 3 * A.n_atoms; k += kGM) xyz_df[k] = df_from_double(A.xyz[k]);
       becke::BeckeCta T;
       T.carve(stage + (size_t)team * team_bytes, A.n_atoms);
-      for (int k = tt; k < na3; k += nt) T.wacc[k] = 0.0;
-      becke::team_sync(nt, team);
+      for (int k = tt; k < na3; k += nt) T.wacc[k] = df32{0.f, 0.f};
+      __syncthreads();
       for (int gg = team; gg < bd.n_pts; gg += n_teams) {
         const double f = coef[8 * 128 + gg];
         const size_t p = (size_t)bd.pt_start + gg;
         const double rw = A.raw_w[p];
         if (fabs(f) < 1e-18 || rw == 0.0) continue;
-        becke::becke_point_team(A.n_atoms, A.xyz, reinterpret_cast<const df32*>(A.pair_df), s_host[gg], G.px[p],
-                                G.py[p], G.pz[p], rw * f, T, tt, nt, team);
+        becke::becke_point_team(A.n_atoms, xyz_df, reinterpret_cast<const df32*>(A.pair_df), s_host[gg],
+                                df_from_double(G.px[p]), df_from_double(G.py[p]), df_from_double(G.pz[p]),
+                                df_from_double(rw * f), T, tt, nt, team);
       }
       __syncthreads();
       for (int k = tid; k < na3; k += kGM) {
@@ -655,7 +662,7 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
         for (int t = 0; t < n_teams; ++t) {
           becke::BeckeCta Tt;
           Tt.carve(stage + (size_t)t * team_bytes, A.n_atoms);
-          v += Tt.wacc[k];
+          v += df_to_double(Tt.wacc[k]);
         }
         out[k] += v;
       }
@@ -672,7 +679,7 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
       }
     }
     __syncthreads();
-    if (A.n_atoms > 1 && !cta_becke) {
+    if (!A.fx_out && A.n_atoms > 1 && !cta_becke) {
       for (int k = tid; k < na3; k += kGM) {
         double v = 0.0;
         for (int w = 0; w < kGWarpsM; ++w) {
@@ -695,6 +702,56 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
   __syncthreads();
   tc_fence_after();
   if (warp == 0) tmem_dealloc(tmem, kTmemColsG);
+}
+
+// The Becke weight derivative as its own kernel (atoms whose pair tables fit in shared memory):
+// one team of nt threads per CTA (a warp for up to 40 atoms, else the whole 256-thread CTA), the
+// team's tables in dynamic shared memory, kBeckePts consecutive points per CTA, and one row of
+// per-atom sums per CTA (part[cta][3 n_atoms]).  Separate from the quadrature kernel so that many
+// more teams are resident per SM than its two CTAs of eight warps allow.
+constexpr int kBeckePts = 16;
+
+__global__ void becke_mixed_kernel(DevGrid G, GradArgs A, const double* __restrict__ fx, double* __restrict__ part) {
+  extern __shared__ __align__(16) unsigned char bsm[];
+  const int na = A.n_atoms, na3 = 3 * na;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  becke::BeckeCta T;
+  T.carve(bsm, na);
+  // the nuclei as double-floats behind the team's tables
+  df32* xyz_df = reinterpret_cast<df32*>(bsm + becke::becke_cta_bytes(na));
+  for (int k = tid; k < 3 * na; k += nt) xyz_df[k] = df_from_double(A.xyz[k]);
+  for (int k = tid; k < na3; k += nt) T.wacc[k] = df32{0.f, 0.f};
+  becke::team_sync(nt, 0);
+  const int p0 = blockIdx.x * kBeckePts;
+  for (int k = 0; k < kBeckePts; ++k) {
+    const int p = p0 + k;
+    if (p >= G.n_pts) break;
+    const double f = fx[p], rw = A.raw_w[p];
+    if (fabs(f) < 1e-18 || rw == 0.0) continue;
+    becke::becke_point_team(na, xyz_df, reinterpret_cast<const df32*>(A.pair_df), A.host[p], df_from_double(G.px[p]),
+                            df_from_double(G.py[p]), df_from_double(G.pz[p]), df_from_double(rw * f), T, tid, nt, 0);
+  }
+  becke::team_sync(nt, 0);
+  double* out = part + (size_t)blockIdx.x * na3;
+  for (int k = tid; k < na3; k += nt) out[k] = df_to_double(T.wacc[k]);
+}
+
+// Whether the separate weight-derivative kernel applies (its team's tables fit in shared memory),
+// its launch shape, and the number of CTAs (rows of its partial sums).
+int becke_kernel_threads(int n_atoms) { return n_atoms <= 40 ? 32 : 256; }
+size_t becke_kernel_smem(int n_atoms) { return becke::becke_cta_bytes(n_atoms) + (size_t)24 * n_atoms; }
+bool becke_kernel_fits(int n_atoms) {
+  return n_atoms > 1 && becke::becke_cta_bytes(n_atoms) + (size_t)24 * n_atoms <= (size_t)kStageG;
+}
+int becke_kernel_ctas(int n_pts) { return (n_pts + kBeckePts - 1) / kBeckePts; }
+
+cudaError_t launch_becke_mixed(const DevGrid& G, const GradArgs& A, const double* fx, double* part, cudaStream_t st) {
+  const int nt = becke_kernel_threads(A.n_atoms);
+  const size_t smem = becke_kernel_smem(A.n_atoms);
+  const cudaError_t e = cudaFuncSetAttribute(becke_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  becke_mixed_kernel<<<becke_kernel_ctas(G.n_pts), nt, smem, st>>>(G, A, fx, part);
+  return cudaGetLastError();
 }
 
 size_t grad_mixed_slab_doubles(int max_m, int n_atoms) {
