@@ -318,28 +318,31 @@ static __device__ void becke_point_df(int n, const double* __restrict__ xyz, con
 // below ~1e-12 Eh/Bohr.  The pass-2 sums over b are reduced by xor shuffles inside fixed lane groups,
 // so results are deterministic.
 
+// dist, cell, tmp[3], wacc[3], ph[4] (n each), hq[4], pp (n); cnt (n ints); su, scu, lu, cres (n(n-1)/2)
 __host__ __device__ constexpr size_t becke_cta_bytes(int n) {
-  return (8 * (8 * (size_t)n + 4) + 8 * (size_t)n + 4 * (size_t)(n + (n & 1)) + 12 * (size_t)n * (size_t)(n - 1) + 15) /
+  return (8 * (13 * (size_t)n + 4) + 8 * (size_t)n + 4 * (size_t)(n + (n & 1)) + 16 * (size_t)n * (size_t)(n - 1) + 15) /
          16 * 16;
 }
 
 struct BeckeCta {
-  df32 *dist, *cell, *tmp, *wacc, *hq;
+  df32 *dist, *cell, *tmp, *wacc, *ph, *hq;
   df32* pp;
   int* cnt;
-  df32 *su, *scu, *lu;
+  df32 *su, *scu, *lu, *cres;
   __device__ void carve(unsigned char* base, int n) {
     dist = reinterpret_cast<df32*>(base);
     cell = dist + n;
     tmp = cell + n;
     wacc = tmp + 3 * n;
-    hq = wacc + 3 * n;
+    ph = wacc + 3 * n;  // per atom a: E_{host a} slope / R and mu e of the pair (a, host)
+    hq = ph + 4 * n;
     pp = hq + 4;
     cnt = reinterpret_cast<int*>(pp + n);
     su = reinterpret_cast<df32*>(cnt + n + (n & 1));  // 8-byte aligned
     const size_t np = (size_t)n * (n - 1) / 2;
     scu = su + np;
     lu = scu + np;
+    cres = lu + np;
   }
 };
 
@@ -427,72 +430,102 @@ static __device__ void becke_point_team(int n, const df32* __restrict__ xyz_df, 
   const df32 zs = T.hq[3];
   if (zs.hi <= 1e-30f) return;  // uniform: every thread read the same value
   const df32 wn = df_div(T.cell[host], zs), pref = df_div(pref_in, zs);
-  int L = 1;
-  while (L < 32 && 2 * L * n <= nth) L *= 2;
-  const int groups = nth / L, sub = tid % L;
-  const int iters = (n + groups - 1) / groups;
-  for (int it = 0; it < iters; ++it) {
-    const int a = tid / L + it * groups;
-    // dZ/dR_a = sum_b (E_ab - E_ba) k_ab (dr_a - mu_ab e_ab) with k = slope / R_ab, accumulated as
-    // dr_a C - W with C = sum c_b, W = sum c_b mu_ab e_ab, c_b = (E_ab - E_ba) k_ab
-    df32 cs = {0.f, 0.f}, w0 = cs, w1 = cs, w2 = cs, ph0 = cs, ph1 = cs, ph2 = cs;
-    df32 dr0 = cs, dr1 = cs, dr2 = cs;
-    bool act = false;
-    if (a < n && a != host) {
-      const df32 dra = T.dist[a];
-      act = dra.hi >= 1e-14f;
-      if (act) {
-        const df32 ir = df_div(df32{1.f, 0.f}, dra);
-        dr0 = df_mul(df_sub(xyz_df[3 * a], x), ir);
-        dr1 = df_mul(df_sub(xyz_df[3 * a + 1], y), ir);
-        dr2 = df_mul(df_sub(xyz_df[3 * a + 2], z), ir);
-        for (int b = sub; b < n; b += L) {
-          const df32* t = pdf + 5 * ((size_t)a * n + b);
-          const df32 inv = t[0];
-          if (b == a || inv.hi == 0.f) continue;
-          const int pid = a < b ? pair_id(a, b, n) : pair_id(b, a, n);
-          const df32 sl = T.lu[pid];
-          const df32 s_ab = a < b ? T.su[pid] : T.scu[pid];
-          const df32 s_ba = a < b ? T.scu[pid] : T.su[pid];
-          const float scl = fabsf(sl.hi) * inv.hi;
-          // both products but one from FP32 estimates: skip the pair when even their sum is below
-          // the threshold (half of it, for the estimates' error), before any double-float work
-          if (est_but_one(T, a, s_ab.hi) * scl < 5e-19f && est_but_one(T, b, s_ba.hi) * scl < 5e-19f) continue;
-          const df32 ea = prod_but_one(T, a, s_ab), eb = prod_but_one(T, b, s_ba);
-          const df32 diff = df_sub(ea, eb);
-          if (fabsf(diff.hi) * scl < 1e-18f && (b != host || fabsf(eb.hi) * scl < 1e-18f)) continue;
-          const df32 mu = df_clamp_unit(df_mul(df_sub(dra, T.dist[b]), inv));
-          const df32 k = df_mul(sl, inv);
-          const df32 c = df_mul(diff, k), cm = df_mul(c, mu);
-          cs = df_add(cs, c);
-          w0 = df_add(w0, df_mul(cm, t[2]));
-          w1 = df_add(w1, df_mul(cm, t[3]));
-          w2 = df_add(w2, df_mul(cm, t[4]));
-          if (b == host) {  // d P_host / dR_a = -E_ba k (dr_a - mu e)
-            const df32 kb = df_mul(eb, k);
-            ph0 = df_mul(kb, df_sub(df_mul(mu, t[2]), dr0));
-            ph1 = df_mul(kb, df_sub(df_mul(mu, t[3]), dr1));
-            ph2 = df_mul(kb, df_sub(df_mul(mu, t[4]), dr2));
+  // dZ/dR_a = sum_b (E_ab - E_ba) k_ab (dr_a - mu_ab e_ab) with k = slope / R_ab.  Each unordered
+  // pair (c < d) is evaluated once, lanes over pairs: c_cd = (E_cd - E_dc) k and c_cd mu_cd e_cd
+  // go to atom c with a plus sign and to atom d with a minus sign (mu, e and the difference of E
+  // change sign with the orientation).  The results overwrite the pair's s, 1 - s and slope slots
+  // (only this lane reads them) plus cres; the pair with the host also leaves E_{host a} k and
+  // mu e for the host term of atom a.
+  for (int k = tid; k < 4 * n; k += nth) T.ph[k] = df32{0.f, 0.f};
+  team_sync(nth, team);
+  {
+    int c = 0, rem = tid;
+    while (c < n - 1 && rem >= n - 1 - c) { rem -= n - 1 - c; ++c; }
+    for (int p = tid; p < np; p += nth) {
+      const int d = c + 1 + rem;
+      const df32* t = pdf + 5 * ((size_t)c * n + d);
+      const df32 inv = t[0];
+      const df32 zero = {0.f, 0.f};
+      df32 cc = zero, w0 = zero, w1 = zero, w2 = zero;
+      if (inv.hi != 0.f) {
+        const df32 sl = T.lu[p], s_cd = T.su[p], s_dc = T.scu[p];
+        const float scl = fabsf(sl.hi) * inv.hi;
+        const bool host_pair = c == host || d == host;
+        // FP32 estimates first: skip when both products but one are below the threshold
+        if (!(est_but_one(T, c, s_cd.hi) * scl < 5e-19f && est_but_one(T, d, s_dc.hi) * scl < 5e-19f)) {
+          const df32 ec = prod_but_one(T, c, s_cd), ed = prod_but_one(T, d, s_dc);
+          const df32 diff = df_sub(ec, ed);
+          const bool use_diff = !(fabsf(diff.hi) * scl < 1e-18f);
+          const df32 eh = c == host ? ec : ed;  // E_{host a}
+          const bool use_host = host_pair && !(fabsf(eh.hi) * scl < 1e-18f);
+          if (use_diff || use_host) {
+            const df32 mu = df_clamp_unit(df_mul(df_sub(T.dist[c], T.dist[d]), inv));  // mu_cd
+            const df32 k = df_mul(sl, inv);
+            if (use_diff) {
+              cc = df_mul(diff, k);
+              const df32 cm = df_mul(cc, mu);
+              w0 = df_mul(cm, t[2]);
+              w1 = df_mul(cm, t[3]);
+              w2 = df_mul(cm, t[4]);
+            }
+            if (use_host) {
+              // atom a = the other one; mu_{a host} e_{a host} = mu_cd e_cd in either orientation
+              const int a = c == host ? d : c;
+              T.ph[4 * a] = df_mul(eh, k);
+              T.ph[4 * a + 1] = df_mul(mu, t[2]);
+              T.ph[4 * a + 2] = df_mul(mu, t[3]);
+              T.ph[4 * a + 3] = df_mul(mu, t[4]);
+            }
           }
         }
       }
+      T.su[p] = cc;
+      T.scu[p] = w0;
+      T.lu[p] = w1;
+      T.cres[p] = w2;
+      rem += nth;
+      while (c < n - 1 && rem >= n - 1 - c) { rem -= n - 1 - c; ++c; }
     }
-    for (int o = L / 2; o > 0; o >>= 1) {
-      cs = df_add(cs, df32{__shfl_xor_sync(0xffffffffu, cs.hi, o), __shfl_xor_sync(0xffffffffu, cs.lo, o)});
-      w0 = df_add(w0, df32{__shfl_xor_sync(0xffffffffu, w0.hi, o), __shfl_xor_sync(0xffffffffu, w0.lo, o)});
-      w1 = df_add(w1, df32{__shfl_xor_sync(0xffffffffu, w1.hi, o), __shfl_xor_sync(0xffffffffu, w1.lo, o)});
-      w2 = df_add(w2, df32{__shfl_xor_sync(0xffffffffu, w2.hi, o), __shfl_xor_sync(0xffffffffu, w2.lo, o)});
-      ph0 = df_add(ph0, df32{__shfl_xor_sync(0xffffffffu, ph0.hi, o), __shfl_xor_sync(0xffffffffu, ph0.lo, o)});
-      ph1 = df_add(ph1, df32{__shfl_xor_sync(0xffffffffu, ph1.hi, o), __shfl_xor_sync(0xffffffffu, ph1.lo, o)});
-      ph2 = df_add(ph2, df32{__shfl_xor_sync(0xffffffffu, ph2.hi, o), __shfl_xor_sync(0xffffffffu, ph2.lo, o)});
-    }
-    if (sub == 0 && a < n) {
+  }
+  team_sync(nth, team);
+  for (int a = tid; a < n; a += nth) {
+    const df32 zero = {0.f, 0.f};
+    df32 tq0 = zero, tq1 = zero, tq2 = zero;
+    const df32 dra = T.dist[a];
+    if (a != host && dra.hi >= 1e-14f) {
+      df32 cs = zero, w0 = zero, w1 = zero, w2 = zero;
+      for (int b = 0; b < n; ++b) {
+        if (b == a) continue;
+        const int p = a < b ? pair_id(a, b, n) : pair_id(b, a, n);
+        if (a < b) {
+          cs = df_add(cs, T.su[p]);
+          w0 = df_add(w0, T.scu[p]);
+          w1 = df_add(w1, T.lu[p]);
+          w2 = df_add(w2, T.cres[p]);
+        } else {
+          cs = df_sub(cs, T.su[p]);
+          w0 = df_sub(w0, T.scu[p]);
+          w1 = df_sub(w1, T.lu[p]);
+          w2 = df_sub(w2, T.cres[p]);
+        }
+      }
+      const df32 ir = df_div(df32{1.f, 0.f}, dra);
+      const df32 dr0 = df_mul(df_sub(xyz_df[3 * a], x), ir);
+      const df32 dr1 = df_mul(df_sub(xyz_df[3 * a + 1], y), ir);
+      const df32 dr2 = df_mul(df_sub(xyz_df[3 * a + 2], z), ir);
       const df32 zz0 = df_sub(df_mul(dr0, cs), w0), zz1 = df_sub(df_mul(dr1, cs), w1), zz2 = df_sub(df_mul(dr2, cs), w2);
-      const df32 zero = {0.f, 0.f};
-      T.tmp[3 * a] = act ? df_mul(pref, df_sub(ph0, df_mul(wn, zz0))) : zero;
-      T.tmp[3 * a + 1] = act ? df_mul(pref, df_sub(ph1, df_mul(wn, zz1))) : zero;
-      T.tmp[3 * a + 2] = act ? df_mul(pref, df_sub(ph2, df_mul(wn, zz2))) : zero;
+      // d P_host / dR_a = -E_{host a} k (dr_a - mu e): mu e was stored for the pair's (lower, higher)
+      // orientation, and both factors change sign with it, so it is also the (a, host) value
+      const df32 kb = T.ph[4 * a];
+      const df32 ph0 = df_mul(kb, df_sub(T.ph[4 * a + 1], dr0)), ph1 = df_mul(kb, df_sub(T.ph[4 * a + 2], dr1)),
+                 ph2 = df_mul(kb, df_sub(T.ph[4 * a + 3], dr2));
+      tq0 = df_mul(pref, df_sub(ph0, df_mul(wn, zz0)));
+      tq1 = df_mul(pref, df_sub(ph1, df_mul(wn, zz1)));
+      tq2 = df_mul(pref, df_sub(ph2, df_mul(wn, zz2)));
     }
+    T.tmp[3 * a] = tq0;
+    T.tmp[3 * a + 1] = tq1;
+    T.tmp[3 * a + 2] = tq2;
   }
   team_sync(nth, team);
   if (tid < 3) {
