@@ -312,3 +312,18 @@ def test_xc_gradient_matches_finite_differences_with_moving_grid(oracle, func):
                 e.append(oracle.vxc_uks_points(b, g, Pa, Pb, func)[0])
             fd = (e[0] - e[1]) / (2 * h)
             assert abs(ana[a, q] - fd) < 1e-8, (a, q, ana[a, q], fd)
+
+
+def test_xc_gradient_parts_add_up(oracle):
+    """The AO term (parts=1) and the Becke weight term (parts=2) sum to the full gradient."""
+    from tests.helpers import distorted_water, make_positive_density
+    mol = distorted_water()
+    xyz = np.array(mol.coords_bohr)
+    basis = oracle.Basis.from_name("6-31g(d)", [a.symbol for a in mol.atoms], xyz)
+    grid = oracle.Grid.build(mol.z, xyz, "coarse")
+    Pa, Pb = make_positive_density(basis.n_ao, 3), make_positive_density(basis.n_ao, 8)
+    full = oracle.xc_gradient(basis, grid, mol.z, xyz, Pa, Pb, "pbe")
+    ao = oracle.xc_gradient(basis, grid, mol.z, xyz, Pa, Pb, "pbe", parts=1)
+    wt = oracle.xc_gradient(basis, grid, mol.z, xyz, Pa, Pb, "pbe", parts=2)
+    assert np.max(np.abs(ao + wt - full)) < 1e-13
+    assert np.max(np.abs(wt)) > 1e-4 and np.max(np.abs(ao)) > 1e-3
