@@ -155,6 +155,27 @@ def fp64_peak_tflops(torch, dev):
     return 2 * 4096 ** 3 / (best * 1e-3) / 1e12
 
 
+def roofline(flops, bytes_alg, kms, tc_peak, tc_unit_note, traffic, kernel, work):
+    """Roofline of one launch after the definition used for this path: the contractions' flops at the
+    tensor (or FP64) peak and the algorithmic HBM bytes at the measured copy bandwidth; the larger of
+    the two times is the bound, and achieved / peak are given in that resource's unit."""
+    pk, pk_kind = peaks()
+    hbm = pk.get("hbm_gbs", 6800.0)
+    t_c = flops / (tc_peak * 1e12)
+    t_m = bytes_alg / (hbm * 1e9)
+    if t_m >= t_c:
+        bound, achieved, peak, unit = "hbm", bytes_alg / (kms * 1e-3) / 1e9, hbm, "GB/s"
+        note = f"measured copy bandwidth, {pk_kind}"
+    else:
+        bound, achieved, peak, unit = "tensor", flops / (kms * 1e-3) / 1e12, tc_peak, "TFLOP/s"
+        note = tc_unit_note
+    return {"bound": bound, "achieved": round(achieved, 4), "peak": round(peak, 3), "unit": unit,
+            "frac": round(achieved / peak, 5), "traffic": traffic, "kernel": kernel, "kernel_ms": round(kms, 4),
+            "work": work, "algorithmic_bytes": float(bytes_alg), "algorithmic_flop": float(flops),
+            "roofline_ms": {"contractions": round(t_c * 1e3, 5), "hbm": round(t_m * 1e3, 5)},
+            "peak_source": note}
+
+
 def cpu_reference_run(basis, mol, D, steps, warmup, budget_s=150.0):
     """Times the oracle's restatement of CalChem's RksVxcEngine CPU path (all host threads)."""
     from oracle import oracle as O
@@ -272,7 +293,7 @@ class _Work:
                                 f"replayed as a CUDA graph")
         else:
             raise ValueError(name)
-        self.n_batches, self.sum_m2n, _, self.max_m = self.obj.plan_stats()
+        self.n_batches, self.sum_m2n, self.sum_m2, self.max_m = self.obj.plan_stats()
         self.flops = (8.0 if self.kind == "uks" else 4.0) * self.sum_m2n
         # packed device buffers
         if self.kind == "group":
@@ -479,14 +500,15 @@ def run_ours(args):
             ref_fp64["dExc_vs_fp64_is"] = "largest |dExc| over the molecules"
     pk, pk_kind = peaks()
     if W.prec == 1:
-        peak, bound, unit = pk.get("bf16_tflops", 1900.0), "tensor", "TFLOP/s"
-        peak_note = f"dense bf16 burst, {pk_kind}"
+        tc_peak, peak_note = pk.get("bf16_tflops", 1900.0), f"dense bf16 burst, {pk_kind}"
     else:
-        peak = fp64_peak_tflops(torch, dev)
-        bound, unit = "tensor", "TFLOP/s"
+        tc_peak = fp64_peak_tflops(torch, dev)
         peak_note = "FP64 pipe: cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in the measured peaks)"
-    achieved = W.flops / (kms * 1e-3) / 1e12
     traffic = NCU_TRAFFIC_BYTES.get(prec_name) if W.name == "octane_b3lyp" else None
+    nspin = 2 if W.kind == "uks" else 1
+    # algorithmic bytes per build: D_sub gathered and V_sub scattered per batch and spin (8 B each per
+    # AO pair), the points (x, y, z, w), and D in and V out once
+    bytes_alg = nspin * 16.0 * W.sum_m2 + 32.0 * W.n_points + nspin * 16.0 * W.nn
     h2d, d2h = W.io_bytes()
     line = {
         "metric": METRIC, "value": round(ms, 4), "unit": "ms", "n_gpus": ws, "steps": args.steps,
@@ -501,11 +523,9 @@ def run_ours(args):
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "grid_points_per_s": round(W.n_points / (ms * 1e-3), 1),
         "exc": float(res_dev[0]), "nelec": float(res_dev[1]),
-        "roofline": {"bound": bound, "achieved": round(achieved, 4), "peak": round(peak, 2), "unit": unit,
-                     "frac": round(achieved / peak, 5), "traffic": traffic,
-                     "kernel": "vxc quadrature kernel", "kernel_ms": round(kms, 4),
-                     "work": f"{'8' if W.kind == 'uks' else '4'}*sum(m^2 n) = {W.flops:.4e} flop per launch",
-                     "peak_source": peak_note},
+        "roofline": roofline(W.flops, bytes_alg, kms, tc_peak, peak_note, traffic, "vxc quadrature kernel",
+                             f"{'8' if W.kind == 'uks' else '4'}*sum(m^2 n) = {W.flops:.4e} flop; "
+                             f"{16 * nspin}*sum(m^2) + 32 N + {16 * nspin} n^2 = {bytes_alg:.4e} B per launch"),
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "wall_s_timed": round(t_wall, 3),
@@ -590,12 +610,12 @@ def run_gradient(args):
     kms = statistics.mean(kern)
     if prec == "mixed":
         pk, pk_kind = peaks()
-        peak, bound, unit = pk.get("bf16_tflops", 1900.0), "tensor", "TFLOP/s"
-        peak_note = f"dense bf16 burst, {pk_kind}"
+        tc_peak, peak_note = pk.get("bf16_tflops", 1900.0), f"dense bf16 burst, {pk_kind}"
     else:
-        peak, bound, unit = fp64_peak_tflops(torch, dev), "fp64 pipe", "TFLOP/s"
-        peak_note = "FP64 pipe: cuBLAS DGEMM 4096^3 measured in this run"
-    achieved = flops / (kms * 1e-3) / 1e12
+        tc_peak, peak_note = fp64_peak_tflops(torch, dev), "FP64 pipe: cuBLAS DGEMM 4096^3 measured in this run"
+    sum_m2 = eng.plan_stats()[2]
+    # D_sub gathered for T and for Y per batch, the points (x, y, z, w, raw w, host), D in
+    bytes_alg = 16.0 * sum_m2 + 44.0 * len(grid) + 8.0 * basis.n_ao ** 2
     n = basis.n_ao
     line = {
         "metric": GRADIENT_METRIC, "value": round(kms, 4), "unit": "ms", "n_gpus": 1, "steps": args.steps,
@@ -606,11 +626,9 @@ def run_gradient(args):
         "config": {"workload": WORKLOAD + "; XC nuclear gradient at P_alpha = D / 2", "name": args.workload,
                    "precision": prec, "grid_points": len(grid), "batches": n_batches, "max_m": max_m,
                    "atoms": len(mol.z), "l2": "flushed before every timed step (256 MiB write)"},
-        "roofline": {"bound": bound, "achieved": round(achieved, 4), "peak": round(peak, 3), "unit": unit,
-                     "frac": round(achieved / peak, 5), "traffic": None,
-                     "kernel": "gradient kernel + split + reduce", "kernel_ms": round(kms, 4),
-                     "work": f"4*sum(m^2 n) = {flops:.4e} flop of AO contractions per launch (Becke term not "
-                             f"counted)", "peak_source": peak_note},
+        "roofline": roofline(flops, bytes_alg, kms, tc_peak, peak_note, None, "gradient kernels + split + reduce",
+                             f"4*sum(m^2 n) = {flops:.4e} flop of AO contractions (weight derivative not counted); "
+                             f"16*sum(m^2) + 44 N + 8 n^2 = {bytes_alg:.4e} B per gradient"),
         "e2e": {"value": round(statistics.mean(wall), 4), "unit": "ms",
                 "h2d_bytes_per_step": n * n * 8 + len(grid) * 12, "d2h_bytes_per_step": len(mol.z) * 24},
         "gpu_launches": launches, "clocks": clk,
