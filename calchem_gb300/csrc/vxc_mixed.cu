@@ -312,6 +312,9 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
   const int* fexp_a0 = reinterpret_cast<const int*>(Dhl_a0 + 2 * G.nn_total);
   const int* fexp_b0 = fexp_a0 + G.n_total;
   const uint32_t sb = smem_addr(stage);
+  // L2 policies: the packed A operand and the GEMM2 image tiles are read again (per N chunk, per
+  // tile pair); the BF16 low planes are read for the last time by the GEMM1 epilogue
+  const uint64_t pol_keep = l2_policy_evict_last(), pol_last_use = l2_policy_evict_first();
 
   // one MMA round: wait for the commit of the round just issued
   auto wait_mma = [&]() -> bool {
@@ -377,7 +380,8 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
           if (tid == 0) {  // A operand of this K block: four 16 KB tiles
             mbar_arrive_expect_tx(tbar, 65536);
 #pragma unroll
-            for (int t = 0; t < 4; ++t) bulk_g2s(sb + t * 16384, apack + (size_t)kb * 65536 + t * 16384, 16384, tbar);
+            for (int t = 0; t < 4; ++t)
+              bulk_g2s_hint(sb + t * 16384, apack + (size_t)kb * 65536 + t * 16384, 16384, tbar, pol_keep);
             tma_busy = true;
           }
           gather_b(stage, Dhl, s_ao, n, m, kb, nc);
@@ -437,7 +441,8 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
 #pragma unroll
               for (int pl = 0; pl < 4; ++pl) {
                 bulk_g2s(sb + r * kRingBytes + pl * 4096, planes + pl * P + row0, 4096, ring + r);
-                bulk_g2s(sb + r * kRingBytes + 16384 + pl * 2048, lo_planes + pl * P + row0, 2048, ring + r);
+                bulk_g2s_hint(sb + r * kRingBytes + 16384 + pl * 2048, lo_planes + pl * P + row0, 2048, ring + r,
+                              pol_last_use);
               }
               ring_busy[r] = true;
             };
@@ -567,14 +572,15 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
         const int mu = e >> 4, c16 = e & 15;
         const size_t o = (size_t)mu * 128 + c16 * 8;
         float ph[8], zz[8];
-        const float4 p0 = *reinterpret_cast<const float4*>(planes + o);
-        const float4 p1 = *reinterpret_cast<const float4*>(planes + o + 4);
-        const float4 x0 = *reinterpret_cast<const float4*>(planes + P + o);
-        const float4 x1 = *reinterpret_cast<const float4*>(planes + P + o + 4);
-        const float4 y0 = *reinterpret_cast<const float4*>(planes + 2 * P + o);
-        const float4 y1 = *reinterpret_cast<const float4*>(planes + 2 * P + o + 4);
-        const float4 z0 = *reinterpret_cast<const float4*>(planes + 3 * P + o);
-        const float4 z1 = *reinterpret_cast<const float4*>(planes + 3 * P + o + 4);
+        // the hi planes' last use in the batch: streaming loads (first in line for eviction)
+        const float4 p0 = __ldcs(reinterpret_cast<const float4*>(planes + o));
+        const float4 p1 = __ldcs(reinterpret_cast<const float4*>(planes + o + 4));
+        const float4 x0 = __ldcs(reinterpret_cast<const float4*>(planes + P + o));
+        const float4 x1 = __ldcs(reinterpret_cast<const float4*>(planes + P + o + 4));
+        const float4 y0 = __ldcs(reinterpret_cast<const float4*>(planes + 2 * P + o));
+        const float4 y1 = __ldcs(reinterpret_cast<const float4*>(planes + 2 * P + o + 4));
+        const float4 z0 = __ldcs(reinterpret_cast<const float4*>(planes + 3 * P + o));
+        const float4 z1 = __ldcs(reinterpret_cast<const float4*>(planes + 3 * P + o + 4));
         ph[0] = p0.x; ph[1] = p0.y; ph[2] = p0.z; ph[3] = p0.w; ph[4] = p1.x; ph[5] = p1.y; ph[6] = p1.z; ph[7] = p1.w;
         const float dxv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
         const float dyv[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
@@ -613,8 +619,8 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
               const int pa = half ? 0 : 3, pb = half ? 3 : 0;  // first piece of the A and B images
 #pragma unroll
               for (int t = 0; t < 3; ++t) {
-                bulk_g2s(sb + t * 16384, img + img_tile(pa + t, I >> 7, kb2, n_ib), 16384, tbar);
-                bulk_g2s(sb + (3 + t) * 16384, img + img_tile(pb + t, J >> 7, kb2, n_ib), 16384, tbar);
+                bulk_g2s_hint(sb + t * 16384, img + img_tile(pa + t, I >> 7, kb2, n_ib), 16384, tbar, pol_keep);
+                bulk_g2s_hint(sb + (3 + t) * 16384, img + img_tile(pb + t, J >> 7, kb2, n_ib), 16384, tbar, pol_keep);
               }
               tma_busy = true;
             }
