@@ -42,10 +42,12 @@ SIGNATURES = {
     "calchem_xc_grid_release": (_I, [_U64]),
     "calchem_xc_upload_points": (_I, [_P, _I, _P, _I, _P, _I, _P, _I, _I, _U64, _SZ]),
     "calchem_xc_upload_points_ex": (_I, [_P, _I, _P, _I, _P, _I, _P, _I, _I, _I, _U64, _SZ]),
+    "calchem_xc_upload_points_spatial": (_I, [_P, _I, _P, _I, _P, _I, _P, _I, _I, _I, _U64, _SZ]),
     "calchem_xc_set_weights": (_I, [_U64, _P, _I]),
     "calchem_xc_plan_stats": (_I, [_U64, _P, _P, _P, _P]),
     "calchem_xc_evaluate_rks": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
     "calchem_xc_evaluate_rks_points": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
+    "calchem_xc_eval_closed_shell": (_I, [_I, _I, _I, _P, _P, _P]),
     "calchem_xc_evaluate_uks": (_I, [_U64, _I, _I, _P, _P, _P, _P, _P, _P]),
     "calchem_xc_evaluate_rks_device": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
     "calchem_xc_evaluate_uks_device": (_I, [_U64, _I, _I, _P, _P, _P, _P, _P, _P]),

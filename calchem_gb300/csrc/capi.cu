@@ -953,9 +953,9 @@ int calchem_xc_grid_release(uint64_t grid_handle) {
   return 0;
 }
 
-int calchem_xc_upload_points_ex(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
-                                const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
-                                int batch_pts, uint64_t grid_id, size_t memory_limit_bytes) {
+static int upload_points_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
+                              const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
+                              int batch_pts, uint64_t grid_id, size_t memory_limit_bytes, bool spatial) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!h_shells || !h_prims || !h_comps || !h_xyzw || n_shells <= 0 || n_prims <= 0 || n_comps <= 0 || n_pts <= 0 ||
       n_ao <= 0 || grid_id == 0 || batch_pts < 16 || batch_pts > kBlockPts)
@@ -964,7 +964,10 @@ int calchem_xc_upload_points_ex(const AoShellGpu* h_shells, int n_shells, const 
   for (int s = 0; s < n_shells; ++s)
     if (!(h_shells[s].r2_cutoff >= 0.0)) return -1;
   Plan plan;
-  plan_batches(h_shells, n_shells, h_xyzw, n_pts, plan, batch_pts);
+  if (spatial)
+    plan_batches_spatial(h_shells, n_shells, h_xyzw, n_pts, plan, batch_pts);
+  else
+    plan_batches(h_shells, n_shells, h_xyzw, n_pts, plan, batch_pts);
   if (plan.pts.empty()) return -1;
   const int rc = upload_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, plan.pts.data(),
                              (int)plan.pts.size(), plan.cand_offsets.data(), (int)plan.cand_offsets.size(),
@@ -976,6 +979,21 @@ int calchem_xc_upload_points_ex(const AoShellGpu* h_shells, int n_shells, const 
     e->n_orig = n_pts;
   }
   return rc;
+}
+
+int calchem_xc_upload_points_ex(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
+                                const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
+                                int batch_pts, uint64_t grid_id, size_t memory_limit_bytes) {
+  return upload_points_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, h_xyzw, n_pts, n_ao, batch_pts,
+                            grid_id, memory_limit_bytes, false);
+}
+
+int calchem_xc_upload_points_spatial(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims,
+                                     int n_prims, const AoCompGpu* h_comps, int n_comps, const double* h_xyzw,
+                                     int n_pts, int n_ao, int batch_pts, uint64_t grid_id,
+                                     size_t memory_limit_bytes) {
+  return upload_points_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, h_xyzw, n_pts, n_ao, batch_pts,
+                            grid_id, memory_limit_bytes, true);
 }
 
 int calchem_xc_upload_points(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
@@ -1006,6 +1024,28 @@ int calchem_xc_plan_stats(uint64_t grid_id, int* n_batches, double* sum_m2n, dou
   if (sum_m2) *sum_m2 = e->sum_m2;
   if (max_m) *max_m = e->max_m;
   return 0;
+}
+
+int calchem_xc_eval_closed_shell(int xc_code, int precision, int n, const double* h_rho, const double* h_gamma,
+                                 double* h_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_rho || !h_gamma || !h_out || n <= 0 || !valid_xc(xc_code) || (precision != CALCHEM_XC_FP64 &&
+                                                                       precision != CALCHEM_XC_MIXED))
+    return -1;
+  if (!device_ok()) return -3;
+  double* d = nullptr;
+  if (cudaMalloc(&d, (size_t)n * 5 * sizeof(double)) != cudaSuccess) return -4;
+  double* d_rho = d;
+  double* d_gam = d + n;
+  double* d_out = d + 2 * (size_t)n;
+  int rc = 0;
+  if (cudaMemcpy(d_rho, h_rho, (size_t)n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(d_gam, h_gamma, (size_t)n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      launch_closed_shell_points(xc_code, precision, n, d_rho, d_gam, d_out, 0) != cudaSuccess ||
+      cudaMemcpy(h_out, d_out, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = -5;
+  cudaFree(d);
+  return rc;
 }
 
 int calchem_xc_evaluate_rks(uint64_t grid_id, int xc_code, int precision, const double* h_d_total, double* exc_out,

@@ -431,6 +431,111 @@ void becke_tables(int n, const int* z, const double* xyz, std::vector<double>& i
     }
 }
 
+// Candidate shells of one batch (points xyzw[4 idx[k]..], k < n) by the reference's rule
+// (vxc.rs:449-489): the shells whose cut-off sphere meets the bounding sphere of the batch's box.
+// With `reach`, only those with r^2 <= r2_cutoff (1 + 1e-6) at one point at least are kept: the
+// others give exact zeros at every point of the batch (the kernels test r^2 > r2_cutoff per point;
+// the margin covers their FP32 form of that test).
+static void batch_candidates(const AoShellGpu* shells, int n_shells, const double* xyzw, const int* idx, int n,
+                             bool reach, std::vector<int>& out) {
+  out.clear();
+  double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int k = 0; k < n; ++k) {
+    const double* p = xyzw + 4 * (size_t)idx[k];
+    for (int q = 0; q < 3; ++q) {
+      if (p[q] < mn[q]) mn[q] = p[q];
+      if (p[q] > mx[q]) mx[q] = p[q];
+    }
+  }
+  const double c[3] = {0.5 * (mn[0] + mx[0]), 0.5 * (mn[1] + mx[1]), 0.5 * (mn[2] + mx[2])};
+  const double ex = mx[0] - c[0], ey = mx[1] - c[1], ez = mx[2] - c[2];
+  const double rbox = std::sqrt(ex * ex + ey * ey + ez * ez);
+  for (int s = 0; s < n_shells; ++s) {
+    const double dx = shells[s].center[0] - c[0], dy = shells[s].center[1] - c[1], dz = shells[s].center[2] - c[2];
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    const double th = rbox + std::sqrt(shells[s].r2_cutoff);
+    if (!(d2 <= th * th)) continue;
+    if (reach) {
+      const double lim = shells[s].r2_cutoff * (1.0 + 1e-6);
+      bool hit = false;
+      for (int k = 0; k < n && !hit; ++k) {
+        const double* p = xyzw + 4 * (size_t)idx[k];
+        const double px = p[0] - shells[s].center[0], py = p[1] - shells[s].center[1], pz = p[2] - shells[s].center[2];
+        hit = px * px + py * py + pz * pz <= lim;
+      }
+      if (!hit) continue;
+    }
+    out.push_back(s);
+  }
+}
+
+int plan_batches_spatial(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan,
+                         int batch_pts) {
+  plan = Plan();
+  std::vector<int> order;
+  order.reserve(n_pts);
+  for (int g = 0; g < n_pts; ++g)
+    if (!(std::fabs(xyzw[4 * (size_t)g + 3]) < 1e-24)) order.push_back(g);
+  // recursive bisection along the longest axis of each part's box; the lower part takes a multiple
+  // of batch_pts points, so every leaf but the last of a part is a full batch
+  std::vector<std::pair<int, int>> stack{{0, (int)order.size()}};
+  std::vector<std::pair<int, int>> leaves;
+  while (!stack.empty()) {
+    const auto [lo, hi] = stack.back();
+    stack.pop_back();
+    const int len = hi - lo;
+    if (len <= batch_pts) {
+      if (len > 0) leaves.push_back({lo, hi});
+      continue;
+    }
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = lo; k < hi; ++k) {
+      const double* p = xyzw + 4 * (size_t)order[k];
+      for (int q = 0; q < 3; ++q) {
+        if (p[q] < mn[q]) mn[q] = p[q];
+        if (p[q] > mx[q]) mx[q] = p[q];
+      }
+    }
+    int ax = 0;
+    for (int q = 1; q < 3; ++q)
+      if (mx[q] - mn[q] > mx[ax] - mn[ax]) ax = q;
+    const int nl = len >= 2 * batch_pts ? (len / batch_pts / 2) * batch_pts : len / 2;
+    auto key = [&](int a, int b) {
+      const double ka = xyzw[4 * (size_t)a + ax], kb = xyzw[4 * (size_t)b + ax];
+      return ka < kb || (ka == kb && a < b);  // total order: the same plan on every machine
+    };
+    std::nth_element(order.begin() + lo, order.begin() + lo + nl, order.begin() + hi, key);
+    stack.push_back({lo + nl, hi});
+    stack.push_back({lo, lo + nl});
+  }
+  const int nb = (int)leaves.size();
+  std::vector<std::vector<int>> cand(nb);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int b = 0; b < nb; ++b)
+    batch_candidates(shells, n_shells, xyzw, order.data() + leaves[b].first, leaves[b].second - leaves[b].first,
+                     true, cand[b]);
+  plan.cand_offsets.push_back(0);
+  for (int b = 0; b < nb; ++b) {
+    if (cand[b].empty()) continue;  // no AO reaches these points: they contribute nothing
+    plan.cand_shells.insert(plan.cand_shells.end(), cand[b].begin(), cand[b].end());
+    plan.cand_offsets.push_back((int)plan.cand_shells.size());
+    for (int k = leaves[b].first; k < leaves[b].second; ++k) {
+      const int g = order[k];
+      const double* p = xyzw + 4 * (size_t)g;
+      GridPtGpu gp;
+      gp.x = p[0];
+      gp.y = p[1];
+      gp.z = p[2];
+      gp.batch_id = (int)plan.cand_offsets.size() - 2;
+      gp.host_atom = 0;
+      plan.pts.push_back(gp);
+      plan.weights.push_back(p[3]);
+      plan.orig.push_back(g);
+    }
+  }
+  return 0;
+}
+
 int plan_batches(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan, int batch_pts) {
   plan = Plan();
   std::vector<int> keep;

@@ -59,5 +59,10 @@ struct Plan {
 // Chunks of batch_pts consecutive points (kPlanBatch = 128 in the reference, vxc.rs:96).
 int plan_batches(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan,
                  int batch_pts = kPlanBatch);
+// Spatially compact batches: the kept points ordered by recursive bisection (leaves of batch_pts
+// points), then chunked; candidates by the reference's rule, narrowed to the shells that reach at
+// least one point of the batch.  Every point sees the same nonzero AOs as under plan_batches.
+int plan_batches_spatial(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan,
+                         int batch_pts = kPlanBatch);
 
 }  // namespace cxc

@@ -23,6 +23,8 @@ int mixed_supported(int mode);
 size_t mixed_slab_doubles(int max_m);
 int mixed_ctas_per_sm();
 int mixed_max_m();
+cudaError_t launch_closed_shell_points(int xc, int precision, int n, const double* rho, const double* gam,
+                                       double* out, cudaStream_t st);
 cudaError_t launch_mixed(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st);
 cudaError_t launch_mixed_prepare(const double* P, int n_total, const int* mol_n, const long long* mol_off,
                                  const int* mol_ao_off, int n_mols, void* out, int* fexp, cudaStream_t st);

@@ -41,6 +41,7 @@
 #include "mixed_ops.cuh"
 #include "tc_ptx.cuh"
 #include "xc_device.cuh"
+#include "xc_df.cuh"
 
 namespace cxc {
 
@@ -517,7 +518,7 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
           const double w = G.pw[pt];
           const double rs = 0.5 * ra;
           const double gss = 0.25 * (gax * gax + gay * gay + gaz * gaz);
-          const XcCs o = xc_eval_cs(A.xc, rs, gss);
+          const XcCs o = xc_eval_cs_fast(A.xc, rs, gss, s_tab);
           e_loc = w * o.f;
           na_loc = w * ra;
           const double us = w * o.vg;
@@ -736,6 +737,31 @@ __global__ void __launch_bounds__(256) split_density_kernel(const double* __rest
     out[(size_t)row * n + j] = make_uint2(pack_bf16x2(__float2bfloat16_rn((float)h), __float2bfloat16_rn((float)m)),
                                           pack_bf16x2(__float2bfloat16_rn((float)l), __float2bfloat16_rn((float)q)));
   }
+}
+
+// The closed-shell point functional at n points (rho_a = rho_b = rho[i], all gammas = gam[i]):
+// out[3 i ..] = (f, v_rho_a, v_gamma_aa + v_gamma_ab / 2), the FP64 form (precision 0) or the form the
+// tensor-core kernels use (precision 1).
+__global__ void __launch_bounds__(256) closed_shell_points_kernel(int xc, int precision, int n,
+                                                                 const double* __restrict__ rho,
+                                                                 const double* __restrict__ gam,
+                                                                 double* __restrict__ out) {
+  __shared__ df32 tab[64];
+  if (threadIdx.x < 64) tab[threadIdx.x] = df_from_double(exp2(-(double)threadIdx.x / 64.0));
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const XcCs o = precision ? xc_eval_cs_fast(xc, rho[i], gam[i], tab) : xc_eval_cs(xc, rho[i], gam[i]);
+    out[3 * (size_t)i] = o.f;
+    out[3 * (size_t)i + 1] = o.vr;
+    out[3 * (size_t)i + 2] = o.vg;
+  }
+}
+
+cudaError_t launch_closed_shell_points(int xc, int precision, int n, const double* rho, const double* gam,
+                                       double* out, cudaStream_t st) {
+  const int blocks = std::min((n + 255) / 256, 4096);
+  closed_shell_points_kernel<<<blocks, 256, 0, st>>>(xc, precision, n, rho, gam, out);
+  return cudaGetLastError();
 }
 
 int mixed_supported(int mode) { return (mode == kModeRks || mode == kModeUks) ? 1 : 0; }

@@ -31,6 +31,25 @@ _ids = itertools.count(1 << 20)
 MAX_GPU_MEMORY_BYTES = 64 << 30
 
 
+def eval_closed_shell_gpu(func, rho_a, gamma, precision="fp64"):
+    """The closed-shell point functional on the device: eval_xc_spin (xc.rs:159-175) at
+    rho_a = rho_b = rho_a[i] and gamma_aa = gamma_ab = gamma_bb = gamma[i].  Returns an (n, 3) array
+    of (f, v_rho_a, v_gamma_aa + v_gamma_ab / 2).  precision "fp64": the FP64 quadrature's form;
+    "mixed": the tensor-core quadrature's form (double-float arithmetic for SVWN5..PBE0 at total
+    density >= 1e-12)."""
+    if isinstance(func, str):
+        func = XcFunctional.from_name(func)
+    r = np.ascontiguousarray(rho_a, dtype=np.float64).ravel()
+    g = np.ascontiguousarray(gamma, dtype=np.float64).ravel()
+    if r.shape != g.shape or r.size == 0:
+        raise ValueError("rho_a and gamma must be non-empty and of equal size")
+    out = np.empty((r.size, 3), dtype=np.float64)
+    lib = _native.load()
+    _native.check("calchem_xc_eval_closed_shell", lib.calchem_xc_eval_closed_shell(
+        int(func), _PRECISION[precision], r.size, _native.ptr(r), _native.ptr(g), _native.ptr(out)))
+    return out
+
+
 def resolve_gpu_memory_limit() -> int:
     """CALCHEM_MAX_GPU_MEM_MB when set (as calchem-cuda's resolve_gpu_memory_limit, lib.rs:531-538);
     otherwise 64 GiB, since the reference's 5 GiB ceiling targets 8 GB cards."""
@@ -128,15 +147,23 @@ class GpuVxcGrid:
             pass
 
 
-def _upload_points(basis, grid, batch_pts: int = 128) -> int:
-    """Batches and uploads one molecule's grid (calchem_xc_upload_points_ex); returns its grid id."""
+BATCHING = ("spatial", "reference")
+
+
+def _upload_points(basis, grid, batch_pts: int = 128, batching: str = "spatial") -> int:
+    """Batches and uploads one molecule's grid; returns its grid id.  batching "spatial": compact
+    batches (calchem_xc_upload_points_spatial); "reference": chunks of consecutive points as CalChem
+    forms them (calchem_xc_upload_points_ex).  The results agree up to summation order."""
+    if batching not in BATCHING:
+        raise ValueError(f"batching must be one of {BATCHING}")
     lib = _native.load()
     sh, pr, co = basis.gpu_arrays()
     xyzw = np.ascontiguousarray(grid.xyzw, dtype=np.float64)
     if len(xyzw) == 0:
         raise ValueError("empty grid")
     gid = next(_ids)
-    _native.check("calchem_xc_upload_points_ex", lib.calchem_xc_upload_points_ex(
+    fn = "calchem_xc_upload_points_spatial" if batching == "spatial" else "calchem_xc_upload_points_ex"
+    _native.check(fn, getattr(lib, fn)(
         _native.ptr(sh), len(sh), _native.ptr(pr), len(pr), _native.ptr(co), len(co), _native.ptr(xyzw),
         len(xyzw), basis.n_ao, int(batch_pts), gid, resolve_gpu_memory_limit()))
     return gid
@@ -144,9 +171,12 @@ def _upload_points(basis, grid, batch_pts: int = 128) -> int:
 
 class _EngineBase:
     """batch_pts: points per batch (16..128; the reference's 128 by default), or "auto" to take
-    the autotuner's choice for this workload (tuned on first use, then cached)."""
+    the autotuner's choice for this workload (tuned on first use, then cached).  batching:
+    "spatial" (compact batches, the default) or "reference" (CalChem's chunks of consecutive
+    points); the results agree up to summation order."""
 
-    def __init__(self, basis, grid, use_gpu=True, precision="fp64", batch_pts=128, func="b3lyp"):
+    def __init__(self, basis, grid, use_gpu=True, precision="fp64", batch_pts=128, func="b3lyp",
+                 batching="spatial"):
         if not use_gpu:
             raise NotImplementedError("calchem_gb300 evaluates Vxc on the GPU only; there is no CPU engine")
         self.n_ao = basis.n_ao
@@ -160,11 +190,12 @@ class _EngineBase:
             batch_pts = autotune.choose_batch_pts(basis, grid, func, precision,
                                                   spin="uks" if isinstance(self, UksVxcEngine) else "rks")
         self.batch_pts = int(batch_pts)
-        self.grid_id = _upload_points(basis, grid, self.batch_pts)
+        self.batching = batching
+        self.grid_id = _upload_points(basis, grid, self.batch_pts, batching)
 
     @classmethod
-    def new_with_gpu(cls, basis, grid, use_gpu=True, precision="fp64", batch_pts=128):
-        return cls(basis, grid, use_gpu, precision, batch_pts)
+    def new_with_gpu(cls, basis, grid, use_gpu=True, precision="fp64", batch_pts=128, batching="spatial"):
+        return cls(basis, grid, use_gpu, precision, batch_pts, batching=batching)
 
     def set_profiling(self, enable: bool = True):
         _native.check("calchem_xc_set_profiling", _native.load().calchem_xc_set_profiling(self.grid_id, int(enable)))
@@ -317,14 +348,14 @@ class VxcGroup:
     vector whose member blocks start at ``offsets`` (device and graph paths).
     """
 
-    def __init__(self, members, precision="fp64", batch_pts=128):
+    def __init__(self, members, precision="fp64", batch_pts=128, batching="spatial"):
         lib = _native.load()
         self.precision = _PRECISION[precision]
         self.grid_id = 0
         ids = []
         try:
             for basis, grid in members:
-                ids.append(_upload_points(basis, grid, batch_pts))
+                ids.append(_upload_points(basis, grid, batch_pts, batching))
             gid = next(_ids)
             arr = np.array(ids, dtype=np.uint64)
             _native.check("calchem_xc_group_create", lib.calchem_xc_group_create(

@@ -174,6 +174,19 @@ int calchem_xc_upload_points_ex(const AoShellGpu* h_shells, int n_shells, const 
                                 const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
                                 int batch_pts, uint64_t grid_id, size_t memory_limit_bytes);
 
+/* As calchem_xc_upload_points_ex with spatially compact batches instead of consecutive chunks: the
+ * points are ordered by recursive bisection along the longest axis of their box (leaves of batch_pts
+ * points; ties broken by index, so the plan is the same on every machine) before chunking, and each
+ * batch's candidate list (the reference's bounding-sphere rule) is narrowed to the shells whose
+ * cut-off sphere holds at least one of its points.  A chunk of the reference's order spans whole
+ * Lebedev spheres, so its candidates are nearly every shell; a compact batch has far fewer AOs.
+ * Every point sees the same nonzero AO values as under the reference's batching, so the results are
+ * the same up to summation order. */
+int calchem_xc_upload_points_spatial(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims,
+                                     int n_prims, const AoCompGpu* h_comps, int n_comps, const double* h_xyzw,
+                                     int n_pts, int n_ao, int batch_pts, uint64_t grid_id,
+                                     size_t memory_limit_bytes);
+
 /* Attaches quadrature weights to a grid uploaded with calchem_cuda_vxc_upload_grid
  * (weights in the uploaded point order). */
 int calchem_xc_set_weights(uint64_t grid_id, const double* h_weights, int n_pts);
@@ -202,6 +215,14 @@ int calchem_xc_evaluate_rks(uint64_t grid_id, int xc_code, int precision, const 
  * reaches, get 0.  Single grids only (-2 for a group). */
 int calchem_xc_evaluate_rks_points(uint64_t grid_id, int xc_code, int precision, const double* h_d_total,
                                    double* exc_out, double* nelec_out, double* h_point_out);
+
+/* The closed-shell point functional on the device (eval_xc_spin, crates/calchem-dft/src/xc.rs:159-175,
+ * at rho_a = rho_b = h_rho[i], gamma_aa = gamma_ab = gamma_bb = h_gamma[i]): h_out[3 i ..] =
+ * (f, v_rho_a, v_gamma_aa + v_gamma_ab / 2) for i < n.  precision CALCHEM_XC_FP64: the FP64 form of
+ * the FP64 quadrature; CALCHEM_XC_MIXED: the form of the tensor-core quadrature (double-float
+ * arithmetic on the FP32 pipe for xc codes 0-5 at total density >= 1e-12, FP64 otherwise). */
+int calchem_xc_eval_closed_shell(int xc_code, int precision, int n, const double* h_rho, const double* h_gamma,
+                                 double* h_out);
 
 /* Open shell (UksVxcEngine::evaluate, vxc.rs:1662-1669).  nelec_out[0..1] = (N_alpha, N_beta);
  * on a group, exc_out[i] and nelec_out[2 i .. 2 i + 1] for member i. */

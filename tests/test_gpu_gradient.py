@@ -181,15 +181,16 @@ def test_mixed_gradient_octane_matches_fp64():
 
 
 def test_mixed_gradient_long_contractions_and_many_atoms():
-    """(H2O)61, 183 atoms, 1159 AOs, Coarse grid: batches of more than 1024 AOs take the running-sum
-    path of the tensor-core contractions, and 183 atoms exceed the shared-memory pair tables of the
-    weight derivative (the per-warp scratch path).  Tensor-core vs FP64 gradient within 5e-9."""
+    """(H2O)61, 183 atoms, 1159 AOs, Coarse grid: batches of more than 1024 AOs (CalChem's batching of
+    consecutive points; compact batches stay near 500) take the running-sum path of the tensor-core
+    contractions, and 183 atoms exceed the shared-memory pair tables of the weight derivative (the
+    per-warp scratch path).  Tensor-core vs FP64 gradient within 5e-9."""
     from calchem_gb300 import BasisSet as BS, RksVxcEngine, workloads
     mol = workloads.water_cluster(61, 61)
     basis = BS.from_name("6-31g(d)", mol)
     grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.COARSE)
     D = workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, 7)
-    eng = RksVxcEngine(basis, grid)
+    eng = RksVxcEngine(basis, grid, batching="reference")
     assert eng.plan_stats()[3] > 1024
     g64 = eng.nuclear_gradient(mol, grid, "pbe", 0.5 * D)
     gm = eng.nuclear_gradient(mol, grid, "pbe", 0.5 * D, precision="mixed")

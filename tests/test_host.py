@@ -66,6 +66,13 @@ def test_no_device_means_error_codes_not_fallback(native_lib):
                                                   1, 0) == -3
     assert native_lib.calchem_cuda_vxc_grad_force(1, _native.ptr(P), None, 0, _native.ptr(wxc), _native.ptr(g), 8, 4,
                                                   1, 0) == -1
+    # the device point functional: argument checks, then "no device"
+    x = np.ones(4)
+    f3 = np.empty(12)
+    assert native_lib.calchem_xc_eval_closed_shell(3, 1, 4, _native.ptr(x), _native.ptr(x), _native.ptr(f3)) == -3
+    assert native_lib.calchem_xc_eval_closed_shell(9, 0, 4, _native.ptr(x), _native.ptr(x), _native.ptr(f3)) == -1
+    assert native_lib.calchem_xc_eval_closed_shell(3, 2, 4, _native.ptr(x), _native.ptr(x), _native.ptr(f3)) == -1
+    assert native_lib.calchem_xc_eval_closed_shell(3, 0, 0, _native.ptr(x), _native.ptr(x), _native.ptr(f3)) == -1
 
 
 def test_gradient_has_no_cpu_path():
