@@ -2,10 +2,11 @@
 //
 // Two persistent CTAs of 256 threads per SM (each 256 TMEM columns, ~110 KB of shared memory) take
 // 128-point batches from a device queue, so that one CTA's SIMT and FP64 phases run under the
-// other's contractions.  For each batch of m candidate AOs (padded to m_pad, a multiple of 128):
+// other's contractions.  For each batch of m candidate AOs (GEMM1's K dimension padded with zero rows
+// to a multiple of 64; GEMM2's tiles to a multiple of 128 with rows that are never read back):
 //   (A) AO values and gradients in double-float arithmetic on the FP32 pipe (48-bit: error-free
 //       transformations, a table-driven exp, basis constants and coordinates as float pairs) into
-//       the CTA's scratch slab as [m_pad][128] planes (FP32 hi and BF16 lo of phi, d/dx, d/dy, d/dz),
+//       the CTA's scratch slab as [m][128] planes (FP32 hi and BF16 lo of phi, d/dx, d/dy, d/dz),
 //       with the reference's screening (ao_grid.rs:182-230).  Plain FP32 AO values carry errors of
 //       a few ulp that are identical at the 302 angular points of a radial shell and so do not
 //       average out; at 48 bits they are negligible;
@@ -75,7 +76,7 @@ static_assert(2 * (kSmemBytes + 1024) <= 233472, "two CTAs must fit in one SM's 
 // keeps ~32 significant bits), at lo_planes + p * P; row = local AO, column = point.
 // Returns the largest |phi| hi part this thread wrote (the point's row scale needs the maximum).
 __device__ float ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __restrict__ planes,
-                            __nv_bfloat16* __restrict__ lo_planes, size_t P, int m_pad, const df32* tab) {
+                            __nv_bfloat16* __restrict__ lo_planes, size_t P, int m_k, const df32* tab) {
   float vmax = 0.f;
   const int tid = threadIdx.x;
   const int g = tid & 127;
@@ -198,8 +199,8 @@ __device__ float ao_eval_df(const DevGrid& G, const BatchDesc& bd, float* __rest
       lo_planes[3 * P + o] = __float2bfloat16_rn(gz.lo);
     }
   }
-  // zero the padding rows [m, m_pad)
-  const int pad = (m_pad - bd.m) * 128;
+  // zero the rows [m, m_k) of the last GEMM1 K block (the A operand's padding must be finite zeros)
+  const int pad = (m_k - bd.m) * 128;
   for (int e = tid; e < pad; e += kMT) {
     const size_t o = (size_t)bd.m * 128 + e;
 #pragma unroll
@@ -346,10 +347,9 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
     const int n = mol_nao(G, bd.mol);
     const long long moff = mol_mat(G, bd.mol);
     const int roff = mol_row(G, bd.mol);
-    const int m_pad = (m + 127) / 128 * 128;
     const int nkb = (m + 63) / 64;
     for (int i = tid; i < m; i += kMT) s_ao[i] = G.batch_ao[bd.ao_start + i];
-    const float vmax = ao_eval_df(G, bd, planes, lo_planes, P, m_pad, s_tab);
+    const float vmax = ao_eval_df(G, bd, planes, lo_planes, P, nkb * 64, s_tab);
     {  // e_g: power-of-two exponent with max_mu |Phi[g][mu]| 2^-e_g < 1
       dens[0][0][g + 128 * h] = (double)vmax;  // scratch: the stage is idle
       __syncthreads();
@@ -569,7 +569,9 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
 
     // (F)+(G) per spin: image tiles Phi^T / Z^T, then lower tile pairs of W
     for (int s = 0; s < nspin && !failed; ++s) {
-      for (int e = tid; e < m_pad * 16; e += kMT) {
+      // rows [m, m_pad) of the tiles are left as they are: a W entry depends on its own row of A and
+      // of B only, and the drain reads rows and columns below m
+      for (int e = tid; e < m * 16; e += kMT) {
         const int mu = e >> 4, c16 = e & 15;
         const size_t o = (size_t)mu * 128 + c16 * 8;
         float ph[8], zz[8];
