@@ -78,10 +78,11 @@ __device__ __forceinline__ df32 ld_df(const float* hi, const __nv_bfloat16* lo, 
 
 __device__ __forceinline__ df32 df_fma(df32 a, df32 b, df32 c) { return df_add(df_mul(a, b), c); }
 
-// (A) values, gradients and Hessians of the batch's AOs in double-float (rows [m, m_pad) zeroed).
+// (A) values, gradients and Hessians of the batch's AOs in double-float (rows [m, m_k) of the last
+// 64-row K block zeroed).
 // Returns the largest |phi| hi part this thread wrote.
 __device__ float ao_eval_df_hess(const DevGrid& G, const BatchDesc& bd, float* __restrict__ hi,
-                                 __nv_bfloat16* __restrict__ lo, size_t P, int m_pad, const df32* tab) {
+                                 __nv_bfloat16* __restrict__ lo, size_t P, int m_k, const df32* tab) {
   float vmax = 0.f;
   const int tid = threadIdx.x;
   const int g = tid & 127;
@@ -172,7 +173,7 @@ __device__ float ao_eval_df_hess(const DevGrid& G, const BatchDesc& bd, float* _
       }
     }
   }
-  const int pad = (m_pad - bd.m) * 128;
+  const int pad = (m_k - bd.m) * 128;
   for (int e = tid; e < pad; e += kGM) {
     const size_t o = (size_t)bd.m * 128 + e;
 #pragma unroll
@@ -391,14 +392,14 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
     const BatchDesc bd = G.batches[b];
     const int m = bd.m;
     const int n = mol_nao(G, bd.mol);
-    const int m_pad = (m + 127) / 128 * 128;
     const int nkb = (m + 63) / 64;
+    const int m_k = nkb * 64;  // rows read by the packed operand and the chunked epilogues
     const bool live = g < bd.n_pts;
     const size_t pt = (size_t)bd.pt_start + g;
     double* out = A.part + (size_t)b * na3;
     for (int i = tid; i < m; i += kGM) s_ao[i] = G.batch_ao[bd.ao_start + i];
     if (tid < 128) s_host[g] = live ? A.host[pt] : -1;
-    const float vmax = ao_eval_df_hess(G, bd, hi, lo, P, m_pad, s_tab);
+    const float vmax = ao_eval_df_hess(G, bd, hi, lo, P, m_k, s_tab);
     {  // e_g: power-of-two exponent with max_mu |Phi[g][mu]| 2^-e_g < 1
       dens[0][0][g + 128 * h] = (double)vmax;  // scratch: the stage is idle
       __syncthreads();
@@ -510,9 +511,9 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
       const df32 ux = df_from_double(coef[(4 * s + 1) * 128 + g]);
       const df32 uy = df_from_double(coef[(4 * s + 2) * 128 + g]);
       const df32 uz = df_from_double(coef[(4 * s + 3) * 128 + g]);
-      {  // Psi into its plane (rows up to m_pad: the padding rows give zeros), and e'_g
+      {  // Psi into its plane (rows up to m_k: the padding rows give zeros), and e'_g
         float mx = 0.f;
-        for (int i = h; i < m_pad; i += 2) {
+        for (int i = h; i < m_k; i += 2) {
           const size_t o = (size_t)i * 128 + g;
           const df32 ps = psi_at(hi, lo, P, o, ux, uy, uz);
           p_hi[o] = ps.hi;
