@@ -26,7 +26,8 @@
 //   (E) the functional in FP64 per point, Exc and Nelec partial sums in FP64 (vxc.rs:890-920);
 //   (F) GEMM2  W = Z^T Phi + Phi^T Z  (Z = (w v_rho / 2) Phi + (w u) . grad Phi) on lower
 //       128 x 128 AO tile pairs, K = 64 points per step: Phi and Z split into three BF16 pieces
-//       (floating, 24 bits), written as swizzled tiles and loaded by bulk copies, six products per
+//       (floating, 24 bits), written as swizzled tiles and loaded by bulk copies (for m <= 128, one
+//       tile pair: written straight into the shared-memory stage per K half), six products per
 //       half step, the hh products in one accumulator and the corrections in another;
 //   (G) the W tile is drained from TMEM and added to V's upper triangle with FP64 atomics,
 //       coalesced across lanes; a final kernel mirrors the upper triangle into the lower.
@@ -567,51 +568,123 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
       }
     }
 
-    // (F)+(G) per spin: image tiles Phi^T / Z^T, then lower tile pairs of W
+    // (F)+(G) per spin: image tiles Phi^T / Z^T, then lower tile pairs of W.  Rows [m, 128 n_ib) of
+    // the tiles are left as they are: a W entry depends on its own row of A and of B only, and the
+    // drain reads rows and columns below m.
+    const uint32_t idesc2 = idesc_bf16_f32(128, 128);
+    // 8 points (c16 * 8 ..) of AO row mu: Phi^T and Z^T, three BF16 pieces each
+    auto image8 = [&](int s, int mu, int c16, uint4 (&p3)[3], uint4 (&z3)[3]) {
+      const size_t o = (size_t)mu * 128 + c16 * 8;
+      float ph[8], zz[8];
+      // the hi planes' last use in the batch: streaming loads (first in line for eviction)
+      const float4 p0 = __ldcs(reinterpret_cast<const float4*>(planes + o));
+      const float4 p1 = __ldcs(reinterpret_cast<const float4*>(planes + o + 4));
+      const float4 x0 = __ldcs(reinterpret_cast<const float4*>(planes + P + o));
+      const float4 x1 = __ldcs(reinterpret_cast<const float4*>(planes + P + o + 4));
+      const float4 y0 = __ldcs(reinterpret_cast<const float4*>(planes + 2 * P + o));
+      const float4 y1 = __ldcs(reinterpret_cast<const float4*>(planes + 2 * P + o + 4));
+      const float4 z0 = __ldcs(reinterpret_cast<const float4*>(planes + 3 * P + o));
+      const float4 z1 = __ldcs(reinterpret_cast<const float4*>(planes + 3 * P + o + 4));
+      ph[0] = p0.x; ph[1] = p0.y; ph[2] = p0.z; ph[3] = p0.w; ph[4] = p1.x; ph[5] = p1.y; ph[6] = p1.z; ph[7] = p1.w;
+      const float dxv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+      const float dyv[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+      const float dzv[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int gg = c16 * 8 + k;
+        zz[k] = coef[4 * s][gg] * ph[k] + coef[4 * s + 1][gg] * dxv[k] + coef[4 * s + 2][gg] * dyv[k] +
+                coef[4 * s + 3][gg] * dzv[k];
+      }
+      pack8x3(ph, p3[0], p3[1], p3[2]);
+      pack8x3(zz, z3[0], z3[1], z3[2]);
+    };
+    // one K step of 64 points for a tile pair whose A and B images sit at stage slots da.. and db..
+    auto mma_half = [&](int da, int db, bool first) {
+      uint64_t d[6];
+#pragma unroll
+      for (int t = 0; t < 6; ++t) d[t] = sdesc_sw128(sb + t * 16384);
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) {
+        const uint64_t o = (uint64_t)(ks * 2);
+        const uint32_t acc = (!first || ks > 0) ? 1u : 0u;
+        mma_bf16_ss(tW, d[da] + o, d[db] + o, idesc2, acc);
+        mma_bf16_ss(tWc, d[da] + o, d[db + 1] + o, idesc2, acc);
+        mma_bf16_ss(tWc, d[da + 1] + o, d[db] + o, idesc2, 1u);
+        mma_bf16_ss(tWc, d[da] + o, d[db + 2] + o, idesc2, 1u);
+        mma_bf16_ss(tWc, d[da + 1] + o, d[db + 1] + o, idesc2, 1u);
+        mma_bf16_ss(tWc, d[da + 2] + o, d[db] + o, idesc2, 1u);
+      }
+    };
+    // drain: lane = AO row i of tile I, this group's 64 columns of tile J
+    auto drain = [&](double* V, int I, int J) {
+      const int i = I + g;
+      for (int c0 = h * 64; c0 < h * 64 + 64; c0 += 32) {
+        float wv[32], wc[32];
+        tmem_ld32(tW + lane_base + (uint32_t)c0, wv);
+        tmem_ld32(tWc + lane_base + (uint32_t)c0, wc);
+#pragma unroll
+        for (int jj = 0; jj < 32; ++jj) wv[jj] += wc[jj];
+        if (i < m) {
+          const int ai = s_ao[i];
+#pragma unroll
+          for (int jj = 0; jj < 32; ++jj) {
+            const int j = J + c0 + jj;
+            if (j < m && (I != J || i >= j)) {
+              const int aj = s_ao[j];
+              const int r = ai < aj ? ai : aj, c = ai < aj ? aj : ai;
+              atomicAdd(&V[(size_t)r * n + c], (double)wv[jj]);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncthreads();
+    };
     for (int s = 0; s < nspin && !failed; ++s) {
-      // rows [m, m_pad) of the tiles are left as they are: a W entry depends on its own row of A and
-      // of B only, and the drain reads rows and columns below m
+      double* V = (s ? A.Vb : A.Va) + moff;
+      if (m <= 128) {
+        // one tile pair: the six image tiles of each 64-point K half are built in the stage and
+        // consumed there (slots 0..2 Phi^T, 3..5 Z^T), with no global round trip
+        for (int kb2 = 0; kb2 < 2 && !failed; ++kb2) {
+          for (int e = tid; e < m * 8; e += kMT) {
+            const int mu = e >> 3, cc = e & 7;
+            uint4 p3[3], z3[3];
+            image8(s, mu, kb2 * 8 + cc, p3, z3);
+            const uint32_t sw = sw128(mu, cc);
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+              *reinterpret_cast<uint4*>(stage + t * 16384 + sw) = p3[t];
+              *reinterpret_cast<uint4*>(stage + (3 + t) * 16384 + sw) = z3[t];
+            }
+          }
+          fence_proxy_async_smem();  // the tiles are read by the tensor core
+          __syncthreads();
+          if (tid == 0) {
+            tc_fence_after();
+            mma_half(3, 0, kb2 == 0);  // A = Z, B = Phi
+            mma_half(0, 3, false);     // A = Phi, B = Z
+            mma_commit(mbar);
+          }
+          if (!wait_mma()) { failed = true; break; }
+        }
+        if (failed) break;
+        drain(V, 0, 0);
+        continue;
+      }
       for (int e = tid; e < m * 16; e += kMT) {
         const int mu = e >> 4, c16 = e & 15;
-        const size_t o = (size_t)mu * 128 + c16 * 8;
-        float ph[8], zz[8];
-        // the hi planes' last use in the batch: streaming loads (first in line for eviction)
-        const float4 p0 = __ldcs(reinterpret_cast<const float4*>(planes + o));
-        const float4 p1 = __ldcs(reinterpret_cast<const float4*>(planes + o + 4));
-        const float4 x0 = __ldcs(reinterpret_cast<const float4*>(planes + P + o));
-        const float4 x1 = __ldcs(reinterpret_cast<const float4*>(planes + P + o + 4));
-        const float4 y0 = __ldcs(reinterpret_cast<const float4*>(planes + 2 * P + o));
-        const float4 y1 = __ldcs(reinterpret_cast<const float4*>(planes + 2 * P + o + 4));
-        const float4 z0 = __ldcs(reinterpret_cast<const float4*>(planes + 3 * P + o));
-        const float4 z1 = __ldcs(reinterpret_cast<const float4*>(planes + 3 * P + o + 4));
-        ph[0] = p0.x; ph[1] = p0.y; ph[2] = p0.z; ph[3] = p0.w; ph[4] = p1.x; ph[5] = p1.y; ph[6] = p1.z; ph[7] = p1.w;
-        const float dxv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
-        const float dyv[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
-        const float dzv[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          const int gg = c16 * 8 + k;
-          zz[k] = coef[4 * s][gg] * ph[k] + coef[4 * s + 1][gg] * dxv[k] + coef[4 * s + 2][gg] * dyv[k] +
-                  coef[4 * s + 3][gg] * dzv[k];
-        }
+        uint4 p3[3], z3[3];
+        image8(s, mu, c16, p3, z3);
         const int ib = mu >> 7, r = mu & 127, kb2 = c16 >> 3, cc = c16 & 7;
         const uint32_t sw = sw128(r, cc);
-        uint4 hi, mid, lo;
-        if (s == 0) {
-          pack8x3(ph, hi, mid, lo);
-          *reinterpret_cast<uint4*>(img + img_tile(0, ib, kb2, n_ib) + sw) = hi;
-          *reinterpret_cast<uint4*>(img + img_tile(1, ib, kb2, n_ib) + sw) = mid;
-          *reinterpret_cast<uint4*>(img + img_tile(2, ib, kb2, n_ib) + sw) = lo;
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+          if (s == 0) *reinterpret_cast<uint4*>(img + img_tile(t, ib, kb2, n_ib) + sw) = p3[t];
+          *reinterpret_cast<uint4*>(img + img_tile(3 + t, ib, kb2, n_ib) + sw) = z3[t];
         }
-        pack8x3(zz, hi, mid, lo);
-        *reinterpret_cast<uint4*>(img + img_tile(3, ib, kb2, n_ib) + sw) = hi;
-        *reinterpret_cast<uint4*>(img + img_tile(4, ib, kb2, n_ib) + sw) = mid;
-        *reinterpret_cast<uint4*>(img + img_tile(5, ib, kb2, n_ib) + sw) = lo;
       }
       fence_proxy_async_global();  // the tiles are read by bulk copies
       __syncthreads();
-      double* V = (s ? A.Vb : A.Va) + moff;
-      const uint32_t idesc = idesc_bf16_f32(128, 128);
       for (int I = 0; I < m && !failed; I += 128) {
         for (int J = 0; J <= I && !failed; J += 128) {
           // four rounds: (kb2, half); half 0 A = Z_I, B = Phi_J; half 1 A = Phi_I, B = Z_J
@@ -630,49 +703,13 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
             if (!wait_tma()) { failed = true; break; }
             if (tid == 0) {
               tc_fence_after();
-              uint64_t d[6];
-#pragma unroll
-              for (int t = 0; t < 6; ++t) d[t] = sdesc_sw128(sb + t * 16384);
-              // d[0..2] A (hi, mid, lo), d[3..5] B (hi, mid, lo)
-#pragma unroll
-              for (int ks = 0; ks < 4; ++ks) {
-                const uint64_t o = (uint64_t)(ks * 2);
-                const uint32_t acc = (rnd > 0 || ks > 0) ? 1u : 0u;
-                mma_bf16_ss(tW, d[0] + o, d[3] + o, idesc, acc);
-                mma_bf16_ss(tWc, d[0] + o, d[4] + o, idesc, acc);
-                mma_bf16_ss(tWc, d[1] + o, d[3] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[0] + o, d[5] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[1] + o, d[4] + o, idesc, 1u);
-                mma_bf16_ss(tWc, d[2] + o, d[3] + o, idesc, 1u);
-              }
+              mma_half(0, 3, rnd == 0);  // d[0..2] A (hi, mid, lo), d[3..5] B (hi, mid, lo)
               mma_commit(mbar);
             }
             if (!wait_mma()) { failed = true; break; }
           }
           if (failed) break;
-          // drain: lane = AO row i of tile I, this group's 64 columns of tile J
-          const int i = I + g;
-          for (int c0 = h * 64; c0 < h * 64 + 64; c0 += 32) {
-            float wv[32], wc[32];
-            tmem_ld32(tW + lane_base + (uint32_t)c0, wv);
-            tmem_ld32(tWc + lane_base + (uint32_t)c0, wc);
-#pragma unroll
-            for (int jj = 0; jj < 32; ++jj) wv[jj] += wc[jj];
-            if (i < m) {
-              const int ai = s_ao[i];
-#pragma unroll
-              for (int jj = 0; jj < 32; ++jj) {
-                const int j = J + c0 + jj;
-                if (j < m && (I != J || i >= j)) {
-                  const int aj = s_ao[j];
-                  const int r = ai < aj ? ai : aj, c = ai < aj ? aj : ai;
-                  atomicAdd(&V[(size_t)r * n + c], (double)wv[jj]);
-                }
-              }
-            }
-          }
-          tc_fence_before();
-          __syncthreads();
+          drain(V, I, J);
         }
       }
     }
