@@ -75,6 +75,22 @@ def test_no_device_means_error_codes_not_fallback(native_lib):
     assert native_lib.calchem_xc_eval_closed_shell(3, 0, 0, _native.ptr(x), _native.ptr(x), _native.ptr(f3)) == -1
 
 
+def test_spatial_upload_argument_checks(native_lib):
+    """calchem_xc_upload_points_spatial checks its arguments and plans before touching a device: a
+    grid whose only point has zero weight leaves nothing to upload (-1, as the reference drops the
+    chunk, vxc.rs:2744-2783), and batch sizes outside 16..128 are rejected."""
+    from tests.helpers import distorted_water
+    basis = BasisSet.from_name("sto-3g", distorted_water())
+    sh, pr, co = basis.gpu_arrays()
+    args = (_native.ptr(sh), len(sh), _native.ptr(pr), len(pr), _native.ptr(co), len(co))
+    zero = np.array([[0.0, 0.0, 0.0, 0.0]])
+    assert native_lib.calchem_xc_upload_points_spatial(*args, _native.ptr(zero), 1, basis.n_ao, 128, 7, 1 << 30) == -1
+    one = np.array([[0.1, 0.2, 0.3, 0.5]])
+    assert native_lib.calchem_xc_upload_points_spatial(*args, _native.ptr(one), 1, basis.n_ao, 8, 7, 1 << 30) == -1
+    assert native_lib.calchem_xc_upload_points_spatial(*args, _native.ptr(one), 1, basis.n_ao, 256, 7, 1 << 30) == -1
+    assert native_lib.calchem_xc_upload_points_spatial(*args, _native.ptr(one), 1, basis.n_ao, 128, 0, 1 << 30) == -1
+
+
 def test_gradient_has_no_cpu_path():
     from calchem_gb300 import xc_nuclear_gradient_with_gpu
     from tests.helpers import distorted_water
