@@ -330,18 +330,22 @@ class _Work:
         _native.check("calchem_xc_set_profiling", self.lib.calchem_xc_set_profiling(self.gid, 1))
 
     def capture(self):
-        """The group's iteration is replayed from a CUDA graph (device buffers fixed)."""
+        """Each timed build is replayed from a CUDA graph (device buffers fixed): split, quadrature,
+        reductions and symmetrisation in one launch."""
         from calchem_gb300 import _native
+        uks = self.kind == "uks"
         _native.check("calchem_xc_graph_capture", self.lib.calchem_xc_graph_capture(
-            self.gid, 0, self.xc, self.prec, self.dP[0].data_ptr(), None, self.dres.data_ptr(),
-            self.dV[0].data_ptr(), None))
+            self.gid, 1 if uks else 0, self.xc, self.prec, self.dP[0].data_ptr(),
+            self.dP[1].data_ptr() if uks else None, self.dres.data_ptr(), self.dV[0].data_ptr(),
+            self.dV[1].data_ptr() if uks else None))
         self.graph = True
 
-    def device_step(self, stream, prec=None, plain=False):
-        """plain: the FP64-plain comparison object (prec is then FP64 unless given)."""
+    def device_step(self, stream, prec=None, plain=False, direct=False):
+        """plain: the FP64-plain comparison object (prec is then FP64 unless given); direct: enqueue
+        the calls instead of replaying the captured graph."""
         prec = (0 if plain else self.prec) if prec is None else prec
         gid = self.plain.grid_id if plain else self.gid
-        if self.graph and prec == self.prec and not plain:
+        if self.graph and prec == self.prec and not plain and not direct:
             return self.lib.calchem_xc_graph_launch(self.gid, stream.cuda_stream)
         if self.kind == "uks":
             return self.lib.calchem_xc_evaluate_uks_device(
@@ -400,10 +404,9 @@ def run_ours(args):
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     W.enable_profiling()
-    if W.kind == "group":
-        W.host_step()  # allocates the workspace outside the capture
-        torch.cuda.synchronize()
-        W.capture()
+    W.host_step()  # allocates the workspace outside the capture
+    torch.cuda.synchronize()
+    W.capture()
     torch.cuda.synchronize()
 
     for _ in range(max(3, args.warmup)):
@@ -443,10 +446,11 @@ def run_ours(args):
     _native.check("device status", lib.calchem_xc_last_status(W.gid))
     res_dev = W.dres.cpu().numpy()
     ms = statistics.mean(step_ms)
-    if not kern_ms:  # graph replays: time the kernel once outside the graph
+    if not kern_ms:  # graph replays: time the kernel outside the graph
         for _ in range(3):
-            _native.check("evaluate", lib.calchem_xc_evaluate_rks_device(
-                W.gid, W.xc, W.prec, W.dP[0].data_ptr(), W.dres.data_ptr(), W.dV[0].data_ptr(), stream.cuda_stream))
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            _native.check("evaluate", W.device_step(stream, direct=True))
             km = np.zeros(1, np.float32)
             _native.check("last_kernel_ms", lib.calchem_xc_last_kernel_ms(W.gid, _native.ptr(km)))
             kern_ms.append(float(km[0]))
@@ -525,6 +529,7 @@ def run_ours(args):
                    "graph": "CUDA-graph replay per step" if W.graph else "direct launches",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "grid_points_per_s": round(W.n_points / (ms * 1e-3), 1),
+        "median_ms_per_step": round(statistics.median(step_ms), 4),
         "exc": float(res_dev[0]), "nelec": float(res_dev[1]),
         "roofline": roofline(W.flops, bytes_alg, kms, tc_peak, peak_note, traffic, "vxc quadrature kernel",
                              f"{'8' if W.kind == 'uks' else '4'}*sum(m^2 n) = {W.flops:.4e} flop; "
