@@ -404,8 +404,11 @@ def run_ours(args):
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     W.enable_profiling()
-    W.host_step()  # allocates the workspace outside the capture
     torch.cuda.synchronize()
+    t_first = time.perf_counter()
+    W.host_step()  # allocates the workspace (and fills the AO cache) outside the capture
+    torch.cuda.synchronize()
+    first_ms = (time.perf_counter() - t_first) * 1e3
     W.capture()
     torch.cuda.synchronize()
 
@@ -505,6 +508,25 @@ def run_ours(args):
                     "max_abs_dV_vs_fp64": float(max(np.max(np.abs(a - b)) for a, b in zip(host[2], Vf)))}
         if W.n_mols > 1:
             ref_fp64["dExc_vs_fp64_is"] = "largest |dExc| over the molecules"
+    if W.prec == 1:
+        # the AO cache (per-batch AO values, gradients and packed operand, kept across evaluations as
+        # CalChem's engine keeps its AO cache across SCF iterations): its size, the first build
+        # (which fills it) and a build with it off
+        W.grid_info["ao_cache_bytes"] = W.obj.ao_cache_bytes()
+        W.grid_info["first_build_wall_ms"] = round(first_ms, 4)  # host call: workspace and cache allocation, fill
+        W.obj.set_ao_cache(False)
+        nts = []
+        for _ in range(3):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            _native.check("evaluate", W.device_step(stream, direct=True))
+            e.record(stream)
+            e.synchronize()
+            nts.append(s.elapsed_time(e))
+        W.grid_info["no_ao_cache_ms"] = round(statistics.mean(nts), 4)
     pk, pk_kind = peaks()
     if W.prec == 1:
         tc_peak, peak_note = pk.get("bf16_tflops", 1900.0), f"dense bf16 burst, {pk_kind}"

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -42,6 +43,7 @@ struct Entry {
   int* d_mol_boff = nullptr;
   bool ws = false;  // evaluation workspace allocated (ensure_ws)
   size_t bytes = 0;
+  size_t mem_limit = SIZE_MAX;  // the caller's device-memory budget for this grid
   bool has_w = false;
   double sum_m2n = 0, sum_m2 = 0;
   AoShellGpu* d_shells = nullptr;
@@ -83,6 +85,13 @@ struct Entry {
   double* d_fxc_m = nullptr;        // trial matrices / results of host-buffer contractions
   double* d_fxc_v = nullptr;
   int fxc_cap = 0;                  // trial matrices d_fxc_m and d_fxc_v hold
+  // AO cache of the tensor-core form (EvalArgs::ao_cache): 0 = decide at the next tensor-core
+  // evaluation, 1 = off (disabled, over the cap or no memory), 2 = allocated
+  int ao_cache_state = 0;
+  unsigned char* d_ao_cache = nullptr;
+  long long* d_ao_cache_off = nullptr;
+  int* d_ao_cache_ok = nullptr;
+  size_t ao_cache_bytes = 0;
   std::vector<int> h_host;          // host atom of every uploaded point (reference-layout uploads)
   std::vector<int> h_orig;          // caller's index of every uploaded point (empty: identity)
   int n_orig = 0;                   // points the caller passed (calchem_xc_upload_points*)
@@ -91,7 +100,7 @@ struct Entry {
     void* ptrs[] = {d_shells, d_prims, d_comps, d_prim_f, d_comp_f, d_shell_cf, d_pts,  d_batches, d_cand,  d_cand_loc, d_bao,   d_order,
                     d_P,      d_Pb,    d_V,     d_Vb,   d_rg,      d_red,   d_res,      d_counter, d_slab,
                     d_mixed_ws, d_mixed_slab, d_mol_n, d_mol_off, d_mol_ao_off, d_mol_boff, d_pt_out,
-                    d_fxc, d_fxc_m, d_fxc_v};
+                    d_fxc, d_fxc_m, d_fxc_v, d_ao_cache, d_ao_cache_off, d_ao_cache_ok};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (graph) cudaGraphExecDestroy(graph);
@@ -303,6 +312,7 @@ int upload_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_pri
   e->n_batches = nb;
   e->max_m = hp.max_m;
   e->bytes = total;
+  e->mem_limit = mem_limit;
   e->sum_m2n = hp.sum_m2n;
   e->sum_m2 = hp.sum_m2;
   e->n_ctas = n_ctas;
@@ -412,6 +422,70 @@ DevGrid dev_grid(const Entry& e) {
 }
 
 // Enqueues one evaluation.  Pa/Pb/Va/Vb are device pointers; result gets (exc, n_a[, n_b]).
+// The AO cache's byte cap: CALCHEM_MAX_AO_GRID_BYTES when set (CalChem's variable for the cap of
+// its cache of per-batch AO values and gradients, vxc.rs:600-640), else 32 GiB: CalChem's default
+// of 2560 MiB sizes host memory, and the cache here lives in the GPU's HBM.
+size_t ao_cache_cap() {
+  const char* v = std::getenv("CALCHEM_MAX_AO_GRID_BYTES");
+  if (v && *v) {
+    char* end = nullptr;
+    const unsigned long long x = std::strtoull(v, &end, 10);
+    if (end && *end == '\0') return (size_t)x;
+  }
+  return (size_t)32 << 30;
+}
+
+void ao_cache_free(Entry& e) {
+  if (e.d_ao_cache) cudaFree(e.d_ao_cache);
+  if (e.d_ao_cache_off) cudaFree(e.d_ao_cache_off);
+  if (e.d_ao_cache_ok) cudaFree(e.d_ao_cache_ok);
+  e.d_ao_cache = nullptr;
+  e.d_ao_cache_off = nullptr;
+  e.d_ao_cache_ok = nullptr;
+  e.ao_cache_bytes = 0;
+}
+
+// Decides and allocates the AO cache on the first tensor-core evaluation (not inside a stream
+// capture: callers that capture decide first).  The per-batch AO values and gradients depend only on
+// the grid and basis, so CalChem's engine computes them once per geometry and reuses them every
+// SCF iteration (vxc.rs:386-394, 600-716); here the cache also holds the packed GEMM1 operand and
+// the row exponents.  Off when the blocks exceed the cap or the free device memory (minus 1 GiB).
+void ao_cache_decide(Entry& e) {
+  if (e.ao_cache_state != 0) return;
+  e.ao_cache_state = 1;
+  std::vector<BatchDesc> hb(e.n_batches);
+  if (cudaMemcpy(hb.data(), e.d_batches, hb.size() * sizeof(BatchDesc), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  std::vector<long long> off(e.n_batches);
+  size_t total = 0;
+  for (int b = 0; b < e.n_batches; ++b) {
+    off[b] = (long long)total;
+    total += ao_cache_block_bytes(hb[b].m);
+  }
+  size_t free_b = 0, tot_b = 0;
+  if (cudaMemGetInfo(&free_b, &tot_b) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  const size_t budget = e.mem_limit > e.bytes ? e.mem_limit - e.bytes : 0;  // within the grid's budget
+  if (total == 0 || total > ao_cache_cap() || total > budget || total + ((size_t)1 << 30) > free_b) return;
+  const bool ok = cudaMalloc(&e.d_ao_cache, total) == cudaSuccess &&
+                  cudaMalloc(&e.d_ao_cache_off, off.size() * sizeof(long long)) == cudaSuccess &&
+                  cudaMalloc(&e.d_ao_cache_ok, (size_t)e.n_batches * sizeof(int)) == cudaSuccess &&
+                  cudaMemcpy(e.d_ao_cache_off, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice) ==
+                      cudaSuccess &&
+                  cudaMemset(e.d_ao_cache_ok, 0, (size_t)e.n_batches * sizeof(int)) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    ao_cache_free(e);
+    return;
+  }
+  e.ao_cache_bytes = total;
+  e.ao_cache_state = 2;
+}
+
 int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, const double* Pb, double* Va,
                  double* Vb, const double* wv, double* rho_out, double* result, cudaStream_t st,
                  double* point_out = nullptr) {
@@ -455,6 +529,13 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
     A.slab = e.d_mixed_slab;
     A.slab_stride = e.mixed_slab_stride;
     A.Pa = (const double*)e.d_mixed_ws;  // the tensor-core kernel reads the split copies
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) ao_cache_decide(e);
+    if (e.ao_cache_state == 2) {
+      A.ao_cache = e.d_ao_cache;
+      A.ao_cache_off = e.d_ao_cache_off;
+      A.ao_cache_ok = e.d_ao_cache_ok;
+    }
     if (prof) cudaEventRecord(e.ev0, st);
     err = launch_mixed(G, A, e.mixed_ctas, st);
     if (prof) cudaEventRecord(e.ev1, st);
@@ -1015,6 +1096,25 @@ int calchem_xc_set_weights(uint64_t grid_id, const double* h_weights, int n_pts)
   return 0;
 }
 
+int calchem_xc_set_ao_cache(uint64_t grid_id, int enable, size_t* bytes_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (enable < 0) {  // query only
+    if (bytes_out) *bytes_out = e->ao_cache_bytes;
+    return 0;
+  }
+  if (e->graph) {  // a captured graph holds the cache pointers
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  ao_cache_free(*e);
+  e->ao_cache_state = enable ? 0 : 1;
+  if (bytes_out) *bytes_out = 0;
+  return 0;
+}
+
 int calchem_xc_plan_stats(uint64_t grid_id, int* n_batches, double* sum_m2n, double* sum_m2, int* max_m) {
   std::lock_guard<std::mutex> lk(g_mu);
   Entry* e = find(grid_id);
@@ -1366,6 +1466,7 @@ int calchem_xc_group_create(const uint64_t* member_ids, int n_members, uint64_t 
                  (size_t)n_cand * 2 * sizeof(int) + (size_t)n_bao * sizeof(int) + (size_t)n_members * 32;
   total += workspace_bytes(*g);
   g->bytes = total;
+  g->mem_limit = memory_limit_bytes;
   if (total > memory_limit_bytes) {
     delete g;
     return -3;
@@ -1476,8 +1577,9 @@ int calchem_xc_graph_capture(uint64_t grid_id, int mode, int xc_code, int precis
   if (!e) return -2;
   if (!e->has_w) return -1;
   if (int rc0 = ensure_ws(*e)) return rc0;
-  // kernel attributes are set outside the capture
+  // kernel attributes are set, and the AO cache decided, outside the capture
   if (fp64_set_attributes() != cudaSuccess || mixed_set_attributes() != cudaSuccess) return -5;
+  if (precision == CALCHEM_XC_MIXED) ao_cache_decide(*e);
   if (e->graph) {
     cudaGraphExecDestroy(e->graph);
     e->graph = nullptr;

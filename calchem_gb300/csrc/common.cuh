@@ -89,7 +89,21 @@ struct EvalArgs {
   int n_trials;
   int triplet;
   const double* fxc_coef;
+  // Tensor-core form: the AO cache (nullptr: none).  Batch b's AO planes, packed GEMM1 operand and
+  // row exponents live at ao_cache + ao_cache_off[b] (ao_cache_block_bytes); ao_cache_ok[b] != 0
+  // once a launch has written them, and later launches read them instead of evaluating the AOs.
+  unsigned char* ao_cache;
+  const long long* ao_cache_off;
+  int* ao_cache_ok;
 };
+
+// Bytes of one batch's AO-cache block for m AOs: with m_k = m rounded up to 64, four FP32 planes
+// and four BF16 planes [m_k][128] (24 B per AO and point), the packed operand (m_k / 64 blocks of
+// 64 KB) and 128 row exponents, rounded up to 1 KB.
+inline size_t ao_cache_block_bytes(int m) {
+  const size_t m_k = (size_t)(m + 63) / 64 * 64;
+  return (m_k * 128 * 24 + m_k * 1024 + 512 + 1023) / 1024 * 1024;
+}
 
 // XC nuclear gradient (xc_grad.cu).  xc >= 0: fused form (densities, functional, AO and Becke
 // terms); xc < 0: drop-in form, per-point coefficients wxc[8 g ..] = (w v_rho_a, w u_a, w v_rho_b,

@@ -69,7 +69,7 @@ constexpr int kSmemBytes = kOffMisc + 64 + 1024;         // + alignment slack
 // dens [kGroups][4][128] doubles (8 KB) lives in the stage at +64 KB while the stage is idle
 constexpr int kOffDensInStage = 65536;
 static_assert(kRing * kRingBytes <= kStageBytes, "the epilogue ring lives in the stage");
-static_assert(20 + 8 * kRing + 4 <= 64, "misc area holds the barriers, the TMEM slot and the batch index");
+static_assert(24 + 8 * kRing + 8 <= 64, "misc area holds the barriers, the TMEM slot, the batch index and the planes' base");
 static_assert(2 * (kSmemBytes + 1024) <= 233472, "two CTAs must fit in one SM's shared memory");
 
 // (A) AO values and gradients in double-float.  Planes p = 0..3 (phi, d/dx, d/dy, d/dz) hold the
@@ -255,6 +255,9 @@ __device__ __forceinline__ double cta_sum(double v, double* red_row) {
 
 }  // namespace
 
+// kCache: the grid has an AO cache (EvalArgs::ao_cache); the instantiation without it keeps the
+// batch's planes in the CTA's slab at fixed addresses.
+template <bool kCache>
 __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -268,6 +271,9 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
   uint64_t* ring = reinterpret_cast<uint64_t*>(base + kOffMisc + 16); // kRing barriers of the epilogue ring
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffMisc + 16 + 8 * kRing);
   int* s_batch = reinterpret_cast<int*>(base + kOffMisc + 20 + 8 * kRing);
+  // the batch's planes (the AO cache block or the slab), kept in shared memory rather than in a
+  // register for the whole batch: read back where needed
+  float** s_planes = reinterpret_cast<float**>(base + kOffMisc + 24 + 8 * kRing);
   int* s_eg = reinterpret_cast<int*>(base + kOffEg);
   df32* s_tab = reinterpret_cast<df32*>(base + kOffTab);
   int* s_fx = reinterpret_cast<int*>(base + kOffFx);
@@ -305,11 +311,12 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
 
   const int m_pad_all = (A.max_m + 127) / 128 * 128;
   const int n_ib = m_pad_all / 128;
-  const size_t P = (size_t)m_pad_all * 128;  // floats per plane
-  float* planes = reinterpret_cast<float*>(A.slab + (size_t)blockIdx.x * A.slab_stride);
-  __nv_bfloat16* lo_planes = reinterpret_cast<__nv_bfloat16*>(planes + 4 * P);
-  unsigned char* apack = reinterpret_cast<unsigned char*>(lo_planes + 4 * P);  // m_pad_all / 64 x 64 KB
-  unsigned char* img = apack + (size_t)m_pad_all * 1024;                    // 6 x n_ib x 2 x 16 KB
+  // the CTA's scratch slab: FP32 planes [4][m_pad_all][128], BF16 planes, the packed operand
+  // (m_pad_all / 64 x 64 KB), the GEMM2 image tiles (6 x n_ib x 2 x 16 KB)
+  const size_t P_slab = (size_t)m_pad_all * 128;  // floats per plane
+  float* const planes_slab = reinterpret_cast<float*>(A.slab + (size_t)blockIdx.x * A.slab_stride);
+  unsigned char* const img = reinterpret_cast<unsigned char*>(planes_slab + 4 * P_slab) + P_slab * 4 * 2 +
+                             (size_t)m_pad_all * 1024;
   const uint2* Dhl_a0 = reinterpret_cast<const uint2*>(A.Pa);
   const uint2* Dhl_b0 = Dhl_a0 + G.nn_total;
   const int* fexp_a0 = reinterpret_cast<const int*>(Dhl_a0 + 2 * G.nn_total);
@@ -350,22 +357,54 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
     const int roff = mol_row(G, bd.mol);
     const int nkb = (m + 63) / 64;
     for (int i = tid; i < m; i += kMT) s_ao[i] = G.batch_ao[bd.ao_start + i];
-    const float vmax = ao_eval_df(G, bd, planes, lo_planes, P, nkb * 64, s_tab);
-    {  // e_g: power-of-two exponent with max_mu |Phi[g][mu]| 2^-e_g < 1
-      dens[0][0][g + 128 * h] = (double)vmax;  // scratch: the stage is idle
-      __syncthreads();
-      if (h == 0) {
-        float t = 0.f;
-        for (int k = 0; k < kGroups; ++k) t = fmaxf(t, (float)dens[0][0][g + 128 * k]);
-        int ex = 0;
-        frexpf(t, &ex);
-        s_eg[g] = ex;
-      }
+    // the batch's AO planes, packed operand and row exponents: in the AO cache when the grid has
+    // one (written by the first launch that reaches the batch, read by later ones), else in the
+    // CTA's scratch slab
+    // (both layouts: the FP32 planes, then the BF16 planes, then the packed operand)
+    const size_t P = kCache ? (size_t)nkb * 64 * 128 : P_slab;  // floats per plane
+    auto batch_planes = [&]() -> float* {
+      if constexpr (kCache) return *reinterpret_cast<float* volatile*>(s_planes);
+      return planes_slab;
+    };
+    bool cached = false;
+    if constexpr (kCache) {
+      if (tid == 0) *s_planes = reinterpret_cast<float*>(A.ao_cache + A.ao_cache_off[b]);
+      // the flag has the same value in every thread: only this CTA writes it, after the reads below
+      cached = *reinterpret_cast<volatile int*>(A.ao_cache_ok + b) != 0;
       __syncthreads();
     }
-    pack_a(apack, planes, lo_planes, s_eg, nkb);
-    fence_proxy_async_global();  // the packed tiles are read by bulk copies
-    __syncthreads();
+    if (cached) {
+      const int* eg_cached = reinterpret_cast<const int*>(
+          reinterpret_cast<const unsigned char*>(batch_planes() + 6 * P) + (size_t)nkb * 65536);
+      if (h == 0) s_eg[g] = eg_cached[g];
+      __syncthreads();
+    } else {
+      float* const planes = batch_planes();
+      __nv_bfloat16* const lo_planes = reinterpret_cast<__nv_bfloat16*>(planes + 4 * P);
+      unsigned char* const apack = reinterpret_cast<unsigned char*>(lo_planes + 4 * P);
+      int* const eg_cached = kCache ? reinterpret_cast<int*>(apack + (size_t)nkb * 65536) : nullptr;
+      const float vmax = ao_eval_df(G, bd, planes, lo_planes, P, nkb * 64, s_tab);
+      {  // e_g: power-of-two exponent with max_mu |Phi[g][mu]| 2^-e_g < 1
+        dens[0][0][g + 128 * h] = (double)vmax;  // scratch: the stage is idle
+        __syncthreads();
+        if (h == 0) {
+          float t = 0.f;
+          for (int k = 0; k < kGroups; ++k) t = fmaxf(t, (float)dens[0][0][g + 128 * k]);
+          int ex = 0;
+          frexpf(t, &ex);
+          s_eg[g] = ex;
+          if (eg_cached) eg_cached[g] = ex;
+        }
+        __syncthreads();
+      }
+      pack_a(apack, planes, lo_planes, s_eg, nkb);
+      fence_proxy_async_global();  // the packed tiles are read by bulk copies
+      __syncthreads();
+      if (eg_cached && tid == 0) {
+        __threadfence();
+        A.ao_cache_ok[b] = 1;  // read by later launches only
+      }
+    }
 
     double spin_rho[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     for (int s = 0; s < nspin && !failed; ++s) {
@@ -383,7 +422,9 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
             mbar_arrive_expect_tx(tbar, 65536);
 #pragma unroll
             for (int t = 0; t < 4; ++t)
-              bulk_g2s_hint(sb + t * 16384, apack + (size_t)kb * 65536 + t * 16384, 16384, tbar, pol_keep);
+              bulk_g2s_hint(sb + t * 16384,
+                            reinterpret_cast<unsigned char*>(batch_planes() + 6 * P) + (size_t)kb * 65536 + t * 16384,
+                            16384, tbar, pol_keep);
             tma_busy = true;
           }
           gather_b(stage, Dhl, s_ao, n, m, kb, nc);
@@ -440,6 +481,8 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
               const int r = st % kRing;
               mbar_arrive_expect_tx(ring + r, 4 * 4096 + 4 * 2048);
               const size_t row0 = (size_t)(nc + 8 * st) * 128;
+              const float* planes = batch_planes();
+              const __nv_bfloat16* lo_planes = reinterpret_cast<const __nv_bfloat16*>(planes + 4 * P);
 #pragma unroll
               for (int pl = 0; pl < 4; ++pl) {
                 bulk_g2s(sb + r * kRingBytes + pl * 4096, planes + pl * P + row0, 4096, ring + r);
@@ -573,6 +616,7 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
     // drain reads rows and columns below m.
     const uint32_t idesc2 = idesc_bf16_f32(128, 128);
     // 8 points (c16 * 8 ..) of AO row mu: Phi^T and Z^T, three BF16 pieces each
+    const float* const planes = batch_planes();
     auto image8 = [&](int s, int mu, int c16, uint4 (&p3)[3], uint4 (&z3)[3]) {
       const size_t o = (size_t)mu * 128 + c16 * 8;
       float ph[8], zz[8];
@@ -820,7 +864,9 @@ int mixed_max_m() { return kMaxMixedM; }
 cudaError_t mixed_set_attributes() {
   static bool attr = false;
   if (attr) return cudaSuccess;
-  const cudaError_t e = cudaFuncSetAttribute(vxc_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  cudaError_t e = cudaFuncSetAttribute(vxc_mixed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(vxc_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
   if (e == cudaSuccess) attr = true;
   return e;
 }
@@ -829,7 +875,10 @@ cudaError_t launch_mixed(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaSt
   if (A.max_m > kMaxMixedM) return cudaErrorInvalidValue;
   const cudaError_t e = mixed_set_attributes();
   if (e != cudaSuccess) return e;
-  vxc_mixed_kernel<<<n_ctas, kMT, kSmemBytes, st>>>(G, A);
+  if (A.ao_cache)
+    vxc_mixed_kernel<true><<<n_ctas, kMT, kSmemBytes, st>>>(G, A);
+  else
+    vxc_mixed_kernel<false><<<n_ctas, kMT, kSmemBytes, st>>>(G, A);
   return cudaGetLastError();
 }
 

@@ -221,6 +221,20 @@ class _EngineBase:
             self.grid_id, _native.ptr(nb), _native.ptr(s1), _native.ptr(s2), _native.ptr(mm)))
         return int(nb[0]), float(s1[0]), float(s2[0]), int(mm[0])
 
+    def set_ao_cache(self, enable: bool = True):
+        """Allows (default) or frees and disables the tensor-core form's AO cache
+        (calchem_xc_set_ao_cache): per-batch AO values, gradients and the packed operand kept in
+        device memory across evaluations, as CalChem's engine keeps its AO cache across SCF
+        iterations.  Results are the same either way."""
+        _native.check("calchem_xc_set_ao_cache", _native.load().calchem_xc_set_ao_cache(
+            self.grid_id, 1 if enable else 0, None))
+
+    def ao_cache_bytes(self) -> int:
+        """Bytes of the AO cache (0 before the first tensor-core evaluation, or when off)."""
+        out = (ctypes.c_size_t * 1)()
+        _native.check("calchem_xc_set_ao_cache", _native.load().calchem_xc_set_ao_cache(self.grid_id, -1, out))
+        return int(out[0])
+
     def last_launch_count(self) -> int:
         return int(_native.load().calchem_xc_last_launch_count(self.grid_id))
 
@@ -395,6 +409,20 @@ class VxcGroup:
         _native.check("calchem_xc_plan_stats", lib.calchem_xc_plan_stats(
             self.grid_id, _native.ptr(nb), _native.ptr(s1), _native.ptr(s2), _native.ptr(mm)))
         return int(nb[0]), float(s1[0]), float(s2[0]), int(mm[0])
+
+    def set_ao_cache(self, enable: bool = True):
+        """Allows (default) or frees and disables the tensor-core form's AO cache
+        (calchem_xc_set_ao_cache): per-batch AO values, gradients and the packed operand kept in
+        device memory across evaluations, as CalChem's engine keeps its AO cache across SCF
+        iterations.  Results are the same either way."""
+        _native.check("calchem_xc_set_ao_cache", _native.load().calchem_xc_set_ao_cache(
+            self.grid_id, 1 if enable else 0, None))
+
+    def ao_cache_bytes(self) -> int:
+        """Bytes of the AO cache (0 before the first tensor-core evaluation, or when off)."""
+        out = (ctypes.c_size_t * 1)()
+        _native.check("calchem_xc_set_ao_cache", _native.load().calchem_xc_set_ao_cache(self.grid_id, -1, out))
+        return int(out[0])
 
     def evaluate_rks(self, func, densities, precision=None):
         """-> (exc[n_mols], nelec[n_mols], [Vxc per member])."""

@@ -191,6 +191,20 @@ int calchem_xc_upload_points_spatial(const AoShellGpu* h_shells, int n_shells, c
  * (weights in the uploaded point order). */
 int calchem_xc_set_weights(uint64_t grid_id, const double* h_weights, int n_pts);
 
+/* The AO cache of the tensor-core form.  AO values and gradients depend only on the grid and the
+ * basis, so, as CalChem's RksVxcEngine caches them per batch for every SCF iteration
+ * (crates/calchem-dft/src/vxc.rs:386-394, 600-716), the first tensor-core evaluation of a grid
+ * allocates a cache of each batch's AO planes (FP32 + BF16 parts), packed GEMM1 operand and row
+ * exponents (32 B per AO and point), the first launch to reach a batch fills its block, and later
+ * evaluations read it instead of evaluating the AOs.  It is used when its size is within
+ * CALCHEM_MAX_AO_GRID_BYTES (the reference's variable for its AO cache; default here 32 GiB, since
+ * the cache lives in HBM where the reference's 2560 MiB default sizes host memory), within the
+ * grid's memory budget (memory_limit_bytes of its upload or group) and within the free device
+ * memory less 1 GiB; otherwise the AOs are evaluated every time.  enable = 1 (the default) allows it, 0
+ * frees and disables it, -1 only reports its size in *bytes_out (0 when none); 0 and 1 drop a
+ * captured graph.  Results are the same with and without the cache. */
+int calchem_xc_set_ao_cache(uint64_t grid_id, int enable, size_t* bytes_out);
+
 /* Number of batches and the sum over batches of m_b^2 * n_b (m_b AOs, n_b points): the
  * algorithmic contraction work is 4x (RKS) that sum in flops. */
 int calchem_xc_plan_stats(uint64_t grid_id, int* n_batches, double* sum_m2n, double* sum_m2, int* max_m);
