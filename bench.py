@@ -7,7 +7,10 @@ Lebedev, Becke partition), seeded S-orthonormal density (33 occupied orbitals,
 PCG64 seed 7).  One step = one full Vxc build (D -> Exc, Nelec, Vxc).  The timed
 build runs on the learned grid with spatially compact batches (points ordered by
 recursive bisection); the FP64-plain comparison runs CalChem's batching (chunks
-of consecutive points) on the Fine grid.
+of consecutive points) on the Fine grid.  A step is one SCF iteration of a
+built engine: the AO cache (per-batch AO values, gradients and packed operand,
+kept across iterations as CalChem's RksVxcEngine keeps its AO cache) is filled
+before the timed steps, and the line reports the build without it as well.
 
 * value: mean device time of one build with D already resident in HBM, CUDA
   events on the launch stream, L2 flushed (256 MiB write) before every step.
