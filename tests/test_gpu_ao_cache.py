@@ -103,3 +103,32 @@ def test_cache_cap_from_environment():
     assert out.returncode == 0, out.stderr[-2000:]
     nbytes, _ = out.stdout.split()[-2:]
     assert int(nbytes) == 0
+
+
+def test_per_point_shares_with_cache(octane):
+    """calchem_xc_evaluate_rks_points (per-point w f and w v.rho, in the caller's order) reads the
+    same cache: the cached call repeats the filling call bit for bit, and both equal the call with
+    the cache off."""
+    from calchem_gb300 import _native
+    from calchem_gb300.vxc import _xc_code
+    mol, basis, grid, D = octane
+    eng = RksVxcEngine(basis, grid, precision="mixed")
+    lib = _native.load()
+
+    def points():
+        out = np.zeros(2 * len(grid))
+        exc, ne = np.zeros(1), np.zeros(1)
+        _native.check("calchem_xc_evaluate_rks_points", lib.calchem_xc_evaluate_rks_points(
+            eng.grid_id, _xc_code("b3lyp"), 1, _native.ptr(np.ascontiguousarray(D)), _native.ptr(exc),
+            _native.ptr(ne), _native.ptr(out)))
+        return exc[0], out
+
+    e1, p1 = points()
+    assert eng.ao_cache_bytes() > 0
+    e2, p2 = points()
+    eng.set_ao_cache(False)
+    e3, p3 = points()
+    eng.close()
+    assert e1 == e2 == e3
+    assert np.array_equal(p1, p2) and np.array_equal(p2, p3)
+    assert abs(p1[0::2].sum() - e1) < 1e-9
