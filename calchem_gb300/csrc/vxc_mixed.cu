@@ -65,11 +65,12 @@ constexpr int kOffEg = kOffRed + 3 * (kMT / 32) * 8;     // int [128]: per-point
 constexpr int kOffTab = kOffEg + 128 * 4;                // df32 [64]: 2^(-j/64)
 constexpr int kOffFx = kOffTab + 64 * 8;                 // int [kNc]: row exponents of the chunk's AOs
 constexpr int kOffMisc = kOffFx + kNc * 4;               // mbarriers, tmem slot, batch
-constexpr int kSmemBytes = kOffMisc + 64 + 1024;         // + alignment slack
+constexpr int kSmemBytes = kOffMisc + 96 + 1024;         // + alignment slack
 // dens [kGroups][4][128] doubles (8 KB) lives in the stage at +64 KB while the stage is idle
 constexpr int kOffDensInStage = 65536;
 static_assert(kRing * kRingBytes <= kStageBytes, "the epilogue ring lives in the stage");
 static_assert(24 + 8 * kRing + 8 <= 64, "misc area holds the barriers, the TMEM slot, the batch index and the planes' base");
+static_assert(64 + 8 * kRing <= 96, "the ring's release barriers follow at +64");
 static_assert(2 * (kSmemBytes + 1024) <= 233472, "two CTAs must fit in one SM's shared memory");
 
 // (A) AO values and gradients in double-float.  Planes p = 0..3 (phi, d/dx, d/dy, d/dz) hold the
@@ -274,6 +275,8 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
   // the batch's planes (the AO cache block or the slab), kept in shared memory rather than in a
   // register for the whole batch: read back where needed
   float** s_planes = reinterpret_cast<float**>(base + kOffMisc + 24 + 8 * kRing);
+  // per ring buffer: every warp arrives once it has read the buffer; the thread that refills it waits
+  uint64_t* ring_free = reinterpret_cast<uint64_t*>(base + kOffMisc + 64);
   int* s_eg = reinterpret_cast<int*>(base + kOffEg);
   df32* s_tab = reinterpret_cast<df32*>(base + kOffTab);
   int* s_fx = reinterpret_cast<int*>(base + kOffFx);
@@ -287,6 +290,7 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
     mbar_init(mbar, 1);
     mbar_init(tbar, 1);
     for (int r = 0; r < kRing; ++r) mbar_init(ring + r, 1);
+    for (int r = 0; r < kRing; ++r) mbar_init(ring_free + r, kMT / 32);
     fence_mbar_init();
   }
   if (tid < 64) s_tab[tid] = df_from_double(exp2(-(double)tid / 64.0));
@@ -304,7 +308,7 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
   const uint32_t tH = tmem, tC1 = tmem + 64, tC2 = tmem + 128, tS = tmem + 192;
   const uint32_t tW = tmem, tWc = tmem + 128;
   uint32_t phase = 0, tphase = 0;
-  uint32_t ring_uses[kRing] = {0, 0, 0, 0};
+  uint32_t ring_uses[kRing] = {0, 0, 0, 0};  // uses of each buffer (its fill and release phases alike)
   bool ring_busy[kRing] = {false, false, false, false};  // a bulk copy issued and not yet waited for
   bool tma_busy = false;
   bool failed = false;
@@ -495,14 +499,18 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
               fence_proxy_async_smem();
               for (int st = 0; st < min(kRing, n_steps); ++st) issue(st);
             }
+            // each buffer is released by an arrival of every warp (no block-wide barrier per step); an
+            // expired wait marks the chunk failed, and the flag is combined after the loop
+            bool efail = false;
             for (int st = 0; st < n_steps; ++st) {
               const int r = st % kRing;
-              const bool ok = mbar_wait_bounded(ring + r, ring_uses[r] & 1u, kWaitLimit);
+              const bool ok = !efail && mbar_wait_bounded(ring + r, ring_uses[r] & 1u, kWaitLimit);
               if (ok) {  // on expiry the copy stays pending and teardown waits for it again
                 ring_uses[r]++;
                 ring_busy[r] = false;
+              } else {
+                efail = true;
               }
-              if (__syncthreads_or(!ok)) { failed = true; break; }
               const int c0 = 8 * st + 4 * h;
               float a[4], bb[4], c2[4], cc[4];
               tmem_ld4x4(tH + lane_base + (uint32_t)c0, tC1 + lane_base + (uint32_t)c0, tC2 + lane_base + (uint32_t)c0,
@@ -514,7 +522,7 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
 #pragma unroll
               for (int j = 0; j < 4; ++j) {
                 const int nu = nc + c0 + j;
-                if (nu < m) {
+                if (ok && nu < m) {
                   df32 t = first_group ? two_sum(a[j], bb[j]) : df_add_f(two_sum(cc[j], a[j]), bb[j]);
                   t = df_ldexp(t, eg + s_fx[c0 + j]);
                   const int o = (4 * h + j) * 128 + g;  // row within the step, point g
@@ -524,13 +532,20 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
                   acc_prod(sgz, df32{buf[3 * 1024 + o], __bfloat162float(lbuf[3 * 1024 + o])}, t);
                 }
               }
-              __syncthreads();  // buffer r is free
+              __syncwarp();
+              if ((tid & 31) == 0) mbar_arrive(ring_free + r);  // this warp is done with buffer r
               if (tid == 0 && st + kRing < n_steps) {
-                fence_proxy_async_smem();
-                issue(st + kRing);
+                // refill buffer r once every warp has released it (the release of this use: the
+                // phase with the parity of the use's index)
+                if (!efail && mbar_wait_bounded(ring_free + r, (ring_uses[r] - 1u) & 1u, kWaitLimit)) {
+                  fence_proxy_async_smem();
+                  issue(st + kRing);
+                } else {
+                  efail = true;
+                }
               }
             }
-            if (failed) break;
+            if (__syncthreads_or(efail)) { failed = true; break; }
           }
           tc_fence_before();
           __syncthreads();
