@@ -48,7 +48,7 @@ PRUNE_TOL = 5e-7  # per-molecule quadrature tolerance of the learned grid agains
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # DRAM bytes (read + write) per launch of the quadrature kernel from one ncu capture of this
 # workload; see profiles/.  None until a capture exists for the precision.
-NCU_TRAFFIC_BYTES = {"fp64": 4.120501e9, "mixed": 2.661e9}  # profiles/vxc_fp64_kernel_octane_b3lyp.md, vxc_mixed_kernel_octane_b3lyp_learned_grid.md
+NCU_TRAFFIC_BYTES = {"fp64": 4.120501e9, "mixed": 2.656e9}  # profiles/vxc_fp64_kernel_octane_b3lyp.md, vxc_mixed_kernel_octane_b3lyp_learned_grid.md
 
 
 def parse():
