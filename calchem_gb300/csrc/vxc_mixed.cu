@@ -6,8 +6,10 @@
 // to a multiple of 64; GEMM2's tiles to a multiple of 128 with rows that are never read back):
 //   (A) AO values and gradients in double-float arithmetic on the FP32 pipe (48-bit: error-free
 //       transformations, a table-driven exp, basis constants and coordinates as float pairs) into
-//       the CTA's scratch slab as [m][128] planes (FP32 hi and BF16 lo of phi, d/dx, d/dy, d/dz),
-//       with the reference's screening (ao_grid.rs:182-230).  Plain FP32 AO values carry errors of
+//       the CTA's scratch slab -- or, when the grid has an AO cache, into the batch's cache block,
+//       which later launches read instead of evaluating (steps A and B depend on the grid and basis
+//       only) -- as [m][128] planes (FP32 hi and BF16 lo of phi, d/dx, d/dy, d/dz), with the
+//       reference's screening (ao_grid.rs:182-230).  Plain FP32 AO values carry errors of
 //       a few ulp that are identical at the 302 angular points of a radial shell and so do not
 //       average out; at 48 bits they are negligible;
 //   (B) every Phi row (point) is scaled by a power of two to |x| < 1 and cut into four fixed-point
@@ -21,9 +23,11 @@
 //       i + j = 2 and 3) are at least 2^8 smaller and accumulate separately, over up to 16 K
 //       blocks; longer contractions are combined into a fourth accumulator;
 //   (D) epilogue: each thread owns one point (its TMEM lane); T = hh + corrections is kept as a
-//       double-float; the planes stream through shared memory by bulk copies and rho,
+//       double-float; the planes stream through a ring of shared-memory buffers by bulk copies (a
+//       buffer is refilled once every warp has arrived on its release barrier) and rho,
 //       grad rho = 2 sum grad Phi T are compensated sums of double-float products;
-//   (E) the functional in FP64 per point, Exc and Nelec partial sums in FP64 (vxc.rs:890-920);
+//   (E) the functional per point (double-float for the closed-shell codes 0-5 above 1e-12, FP64
+//       otherwise), Exc and Nelec partial sums in FP64 (vxc.rs:890-920);
 //   (F) GEMM2  W = Z^T Phi + Phi^T Z  (Z = (w v_rho / 2) Phi + (w u) . grad Phi) on lower
 //       128 x 128 AO tile pairs, K = 64 points per step: Phi and Z split into three BF16 pieces
 //       (floating, 24 bits), written as swizzled tiles and loaded by bulk copies (for m <= 128, one
