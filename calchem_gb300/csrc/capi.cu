@@ -1100,18 +1100,24 @@ int calchem_xc_set_ao_cache(uint64_t grid_id, int enable, size_t* bytes_out) {
   std::lock_guard<std::mutex> lk(g_mu);
   Entry* e = find(grid_id);
   if (!e) return -2;
-  if (e->stream) cudaStreamSynchronize(e->stream);
   if (enable < 0) {  // query only
     if (bytes_out) *bytes_out = e->ao_cache_bytes;
     return 0;
   }
+  if (bytes_out) *bytes_out = 0;
+  const int want = enable ? 0 : 1;  // 0: allowed (decided at the next evaluation), 1: off
+  if (enable && e->ao_cache_state != 1) {  // already allowed
+    if (bytes_out) *bytes_out = e->ao_cache_bytes;
+    return 0;
+  }
+  // evaluations in flight on any stream may still read the cache
+  if (cudaDeviceSynchronize() != cudaSuccess) return -5;
   if (e->graph) {  // a captured graph holds the cache pointers
     cudaGraphExecDestroy(e->graph);
     e->graph = nullptr;
   }
   ao_cache_free(*e);
-  e->ao_cache_state = enable ? 0 : 1;
-  if (bytes_out) *bytes_out = 0;
+  e->ao_cache_state = want;
   return 0;
 }
 

@@ -200,9 +200,10 @@ int calchem_xc_set_weights(uint64_t grid_id, const double* h_weights, int n_pts)
  * CALCHEM_MAX_AO_GRID_BYTES (the reference's variable for its AO cache; default here 32 GiB, since
  * the cache lives in HBM where the reference's 2560 MiB default sizes host memory), within the
  * grid's memory budget (memory_limit_bytes of its upload or group) and within the free device
- * memory less 1 GiB; otherwise the AOs are evaluated every time.  enable = 1 (the default) allows it, 0
- * frees and disables it, -1 only reports its size in *bytes_out (0 when none); 0 and 1 drop a
- * captured graph.  Results are the same with and without the cache. */
+ * memory less 1 GiB; otherwise the AOs are evaluated every time.  enable = 0 waits for the device,
+ * frees the cache, disables it and drops a captured graph; enable = 1 allows it again (a no-op when
+ * allowed, the default); -1 only reports its size in *bytes_out (0 when none).  Results are the
+ * same with and without the cache. */
 int calchem_xc_set_ao_cache(uint64_t grid_id, int enable, size_t* bytes_out);
 
 /* Number of batches and the sum over batches of m_b^2 * n_b (m_b AOs, n_b points): the
