@@ -90,3 +90,34 @@ def test_mixed_long_contractions_reference_batching():
     eng.close()
     assert abs(em - e64) < 1e-7
     assert np.max(np.abs(Vm - V64)) < 2e-6
+
+
+@pytest.mark.parametrize("shape", ["one_point", "coincident", "colinear"])
+def test_spatial_batches_degenerate_grids(shape):
+    """Degenerate point sets (one point; 1000 coincident points; 1000 points on a line) plan and
+    evaluate under compact batches as under CalChem's chunks."""
+    from calchem_gb300.grid import MolecularGrid as MG
+    from tests.helpers import distorted_water, make_positive_density
+    mol = distorted_water()
+    basis = BasisSet.from_name("6-31g(d)", mol)
+    rng = np.random.default_rng(11)
+    if shape == "one_point":
+        xyz = np.array([[0.1, 0.2, 0.3]])
+    elif shape == "coincident":
+        xyz = np.tile([[0.3, -0.2, 0.5]], (1000, 1))
+    else:
+        xyz = np.stack([np.linspace(-3.0, 3.0, 1000), np.zeros(1000), np.zeros(1000)], axis=1)
+    w = rng.uniform(0.01, 0.1, len(xyz))
+    xyzw = np.concatenate([xyz, w[:, None]], axis=1)
+    g = MG(xyzw, w.copy(), np.zeros(len(xyz), np.int32), GridLevel.COARSE)
+    P = make_positive_density(basis.n_ao, 5)
+    for prec in ("fp64", "mixed"):
+        ref = RksVxcEngine(basis, g, precision=prec, batching="reference")
+        sp = RksVxcEngine(basis, g, precision=prec, batching="spatial")
+        e_ref, V_ref = ref.evaluate(basis, g, "pbe", P)
+        e_sp, V_sp = sp.evaluate(basis, g, "pbe", P)
+        ref.close()
+        sp.close()
+        tol_e, tol_v = (1e-11, 1e-12) if prec == "fp64" else (1e-7, 2e-6)
+        assert abs(e_sp - e_ref) < tol_e * max(1.0, abs(e_ref))
+        assert np.max(np.abs(V_sp - V_ref)) < tol_v
