@@ -49,6 +49,7 @@ SIGNATURES = {
     "calchem_xc_evaluate_rks_points": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
     "calchem_xc_eval_closed_shell": (_I, [_I, _I, _I, _P, _P, _P]),
     "calchem_xc_set_ao_cache": (_I, [_U64, _I, _P]),
+    "calchem_xc_fxc_contract_ex": (_I, [_U64, _I, _I, _P, _I, _P]),
     "calchem_xc_evaluate_uks": (_I, [_U64, _I, _I, _P, _P, _P, _P, _P, _P]),
     "calchem_xc_evaluate_rks_device": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
     "calchem_xc_evaluate_uks_device": (_I, [_U64, _I, _I, _P, _P, _P, _P, _P, _P]),

@@ -590,6 +590,48 @@ int enqueue_fxc(Entry& e, int triplet, const double* d_m, int n_trials, double* 
   return 0;
 }
 
+// The same contraction in the tensor-core form: one launch per trial matrix, each the closed-shell
+// pipeline with M_b in place of D and the kernel coefficients in place of the functional; the AO cache
+// (filled by the first launch) serves every trial.  The upper triangles the kernel adds are mirrored.
+int enqueue_fxc_mixed(Entry& e, int triplet, const double* d_m, int n_trials, double* d_v, cudaStream_t st) {
+  const size_t nn = (size_t)e.n_ao * e.n_ao;
+  if (mixed_set_attributes() != cudaSuccess) return -5;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) ao_cache_decide(e);
+  uint2* pk = reinterpret_cast<uint2*>(e.d_mixed_ws);
+  int* fx = reinterpret_cast<int*>(pk + 2 * nn);
+  const DevGrid G = dev_grid(e);
+  for (int t = 0; t < n_trials; ++t) {
+    double* v = d_v + t * nn;
+    if (cudaMemsetAsync(v, 0, nn * sizeof(double), st) != cudaSuccess ||
+        cudaMemsetAsync(e.d_counter, 0, 4 * sizeof(int), st) != cudaSuccess)
+      return -5;
+    if (launch_mixed_prepare(d_m + t * nn, e.n_ao, nullptr, nullptr, nullptr, 1, pk, fx, st) != cudaSuccess)
+      return -5;
+    EvalArgs A{};
+    A.mode = kModeFxc;
+    A.Pa = (const double*)e.d_mixed_ws;
+    A.Va = v;
+    A.fxc_coef = e.d_fxc;
+    A.triplet = triplet ? 1 : 0;
+    A.n_trials = 1;
+    A.batch_red = e.d_red;
+    A.counter = e.d_counter;
+    A.max_m = e.max_m;
+    A.slab = e.d_mixed_slab;
+    A.slab_stride = e.mixed_slab_stride;
+    if (e.ao_cache_state == 2) {
+      A.ao_cache = e.d_ao_cache;
+      A.ao_cache_off = e.d_ao_cache_off;
+      A.ao_cache_ok = e.d_ao_cache_ok;
+    }
+    if (launch_mixed(G, A, e.mixed_ctas, st) != cudaSuccess) return -5;
+    if (launch_mirror(v, e.n_ao, 1, st) != cudaSuccess) return -5;
+  }
+  e.last_launches = 3 * n_trials;
+  return 0;
+}
+
 bool valid_xc(int xc) { return xc >= 0 && xc <= 8; }
 bool valid_prec(int p, int mode) {
   if (p == CALCHEM_XC_FP64) return true;
@@ -1344,8 +1386,14 @@ int calchem_xc_fxc_contract_device(uint64_t grid_id, int triplet, const double* 
 }
 
 int calchem_xc_fxc_contract(uint64_t grid_id, int triplet, const double* h_m, int n_trials, double* h_v_out) {
+  return calchem_xc_fxc_contract_ex(grid_id, triplet, CALCHEM_XC_FP64, h_m, n_trials, h_v_out);
+}
+
+int calchem_xc_fxc_contract_ex(uint64_t grid_id, int triplet, int precision, const double* h_m, int n_trials,
+                               double* h_v_out) {
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!h_m || !h_v_out || n_trials <= 0) return -1;
+  if (!h_m || !h_v_out || n_trials <= 0 || (precision != CALCHEM_XC_FP64 && precision != CALCHEM_XC_MIXED))
+    return -1;
   if (!device_ok()) return -3;
   Entry* e = find(grid_id);
   if (!e || e->n_mols != 1) return -2;
@@ -1366,7 +1414,11 @@ int calchem_xc_fxc_contract(uint64_t grid_id, int triplet, const double* h_m, in
   if (cudaMemcpyAsync(e->d_fxc_m, h_m, nn * n_trials * sizeof(double), cudaMemcpyHostToDevice, e->stream) !=
       cudaSuccess)
     return -5;
-  if (int rc = enqueue_fxc(*e, triplet, e->d_fxc_m, n_trials, e->d_fxc_v, e->stream)) return rc;
+  if (precision == CALCHEM_XC_MIXED && e->max_m > mixed_max_m()) return -2;
+  if (int rc = precision == CALCHEM_XC_MIXED
+                   ? enqueue_fxc_mixed(*e, triplet, e->d_fxc_m, n_trials, e->d_fxc_v, e->stream)
+                   : enqueue_fxc(*e, triplet, e->d_fxc_m, n_trials, e->d_fxc_v, e->stream))
+    return rc;
   if (cudaMemcpyAsync(h_v_out, e->d_fxc_v, nn * n_trials * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
           cudaSuccess ||
       cudaMemcpyAsync(&st, e->d_counter + 2, sizeof(int), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||

@@ -576,7 +576,22 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
       const double ra = spin_rho[0][0];
       const double gax = 2.0 * spin_rho[0][1], gay = 2.0 * spin_rho[0][2], gaz = 2.0 * spin_rho[0][3];
       const size_t pt = (size_t)bd.pt_start + g;
-      if (!uks) {
+      if (A.mode == kModeFxc) {
+        // TD-DFT kernel contraction (fxc.rs:374-645; the FP64 form's coefficients): the batch's
+        // density is the trial matrix M, so ra = eta = sum M phi phi and (gax, gay, gaz) = xi
+        if (live) {
+          const double* c = A.fxc_coef + 11 * pt;
+          const double* kc = c + (A.triplet ? 7 : 3);
+          const double w = G.pw[pt];
+          const double sigma = c[0] * gax + c[1] * gay + c[2] * gaz;
+          const double dv = kc[0] * ra + kc[1] * sigma;
+          const double gc = kc[1] * ra + kc[2] * sigma;
+          coef[0][g] = (float)(0.5 * w * dv);
+          coef[1][g] = (float)(w * (kc[3] * gax + gc * c[0]));
+          coef[2][g] = (float)(w * (kc[3] * gay + gc * c[1]));
+          coef[3][g] = (float)(w * (kc[3] * gaz + gc * c[2]));
+        }
+      } else if (!uks) {
         if (live && !(ra < 1e-18)) {
           const double w = G.pw[pt];
           const double rs = 0.5 * ra;

@@ -477,11 +477,13 @@ class VxcGroup:
 
 class FxcKernel:
     """TD-DFT exchange-correlation kernel (FxcKernel, fxc.rs:176-647): built from the ground-state
-    total density, then contracted with batches of symmetric trial matrices on the GPU."""
+    total density, then contracted with batches of symmetric trial matrices on the GPU.  precision
+    "fp64" (default) or "mixed" (the tensor-core contraction, calchem_xc_fxc_contract_ex)."""
 
-    def __init__(self, basis, grid, func, density_total):
+    def __init__(self, basis, grid, func, density_total, precision="fp64"):
         lib = _native.load()
         self.n_ao = basis.n_ao
+        self.precision = _PRECISION[precision]
         self.func = XcFunctional.from_name(func) if isinstance(func, str) else XcFunctional(func)
         self.grid_id = _upload_points(basis, grid)
         P = _as_matrix(density_total, self.n_ao)
@@ -493,25 +495,26 @@ class FxcKernel:
             raise
 
     @classmethod
-    def new(cls, basis, grid, func, density_total):
-        return cls(basis, grid, func, density_total)
+    def new(cls, basis, grid, func, density_total, precision="fp64"):
+        return cls(basis, grid, func, density_total, precision)
 
     def functional(self):
         return self.func
 
-    def contract_batch(self, d_sym_list, triplet=False):
+    def contract_batch(self, d_sym_list, triplet=False, precision=None):
         """[dV_b] for the symmetric trial matrices (contract_batch, fxc.rs:374)."""
         if len(d_sym_list) == 0:
             return []
         n = self.n_ao
         M = np.ascontiguousarray(np.stack([_as_matrix(m, n) for m in d_sym_list]))
         out = np.zeros_like(M)
-        _native.check("calchem_xc_fxc_contract", _native.load().calchem_xc_fxc_contract(
-            self.grid_id, int(bool(triplet)), _native.ptr(M), len(d_sym_list), _native.ptr(out)))
+        prec = self.precision if precision is None else _PRECISION[precision]
+        _native.check("calchem_xc_fxc_contract_ex", _native.load().calchem_xc_fxc_contract_ex(
+            self.grid_id, int(bool(triplet)), prec, _native.ptr(M), len(d_sym_list), _native.ptr(out)))
         return [out[b] for b in range(len(d_sym_list))]
 
-    def contract(self, m_sym, triplet=False):
-        return self.contract_batch([m_sym], triplet)[0]
+    def contract(self, m_sym, triplet=False, precision=None):
+        return self.contract_batch([m_sym], triplet, precision)[0]
 
     def close(self):
         if self.grid_id:

@@ -262,6 +262,12 @@ int calchem_xc_evaluate_uks_device(uint64_t grid_id, int xc_code, int precision,
  * once per batch for all trial matrices.  -1 when the kernel was not prepared; single grids only. */
 int calchem_xc_fxc_prepare(uint64_t grid_id, int xc_code, const double* h_d_total);
 int calchem_xc_fxc_contract(uint64_t grid_id, int triplet, const double* h_m, int n_trials, double* h_v_out);
+/* As calchem_xc_fxc_contract with a precision: CALCHEM_XC_FP64 (the above) or CALCHEM_XC_MIXED, the
+ * tensor-core form: per trial matrix the closed-shell tensor-core pipeline with M_b in place of the
+ * density and the prepared kernel coefficients in place of the functional (the AO cache, filled by
+ * the first launch, serves every trial); dV agrees with the FP64 form to ~1e-7 of its largest entry. */
+int calchem_xc_fxc_contract_ex(uint64_t grid_id, int triplet, int precision, const double* h_m, int n_trials,
+                               double* h_v_out);
 /* Device-pointer variant of the contraction (enqueued on `stream`, not synchronised). */
 int calchem_xc_fxc_contract_device(uint64_t grid_id, int triplet, const double* d_m, int n_trials, double* d_v_out,
                                    void* stream);

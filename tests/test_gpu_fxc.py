@@ -56,3 +56,41 @@ def test_batch_equals_single_contractions_and_zero_trials(setup):
         assert np.all(batch[2] == 0.0)
     assert ker.contract_batch([], False) == []
     ker.close()
+
+
+@pytest.mark.parametrize("func", ["svwn5", "blyp", "pbe", "b3lyp", "b3lyp5", "pbe0"])
+def test_tensor_core_contraction_matches_fp64(setup, func):
+    """calchem_xc_fxc_contract_ex with CALCHEM_XC_MIXED (the closed-shell tensor-core pipeline per trial
+    matrix, the AO cache shared by the trials) against the FP64 contraction: within 1e-6 of the
+    largest dV entry, symmetric, exact zeros for a zero trial matrix."""
+    mol, basis, grid, P0, M = setup
+    ker = FxcKernel(basis, grid, func, P0)
+    rng = np.random.default_rng(5)
+    mats = [M, 0.5 * (lambda a: a + a.T)(rng.normal(size=M.shape)) * 0.01, np.zeros_like(M)]
+    for triplet in (False, True):
+        ref = ker.contract_batch(mats, triplet, precision="fp64")
+        got = ker.contract_batch(mats, triplet, precision="mixed")
+        for r, d in zip(ref[:2], got[:2]):
+            scale = np.max(np.abs(r))
+            assert scale > 0
+            assert np.max(np.abs(d - r)) < 1e-6 * scale, (func, triplet, np.max(np.abs(d - r)) / scale)
+            assert np.array_equal(d, d.T)
+        assert np.all(got[2] == 0.0)
+    ker.close()
+
+
+def test_tensor_core_contraction_octane():
+    """C8H18 B3LYP/6-31G(d,p), Medium grid, five trial matrices: the tensor-core contraction against FP64."""
+    from calchem_gb300 import workloads
+    mol = workloads.octane()
+    basis = BasisSet.from_name("6-31g(d,p)", mol)
+    grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.MEDIUM)
+    D = workloads.seeded_density_rks(basis.overlap(), 33, 7)
+    ker = FxcKernel(basis, grid, "b3lyp", D, precision="mixed")
+    rng = np.random.default_rng(9)
+    mats = [0.01 * (lambda a: a + a.T)(rng.normal(size=D.shape)) for _ in range(5)]
+    got = ker.contract_batch(mats)
+    ref = ker.contract_batch(mats, precision="fp64")
+    ker.close()
+    for r, d in zip(ref, got):
+        assert np.max(np.abs(d - r)) < 1e-6 * np.max(np.abs(r))
