@@ -62,10 +62,12 @@ def parse():
     ap.add_argument("--grid", default="learned", choices=["learned", "fine"],
                     help="learned: the MLP-pruned grid with the Fine-grid judge (headline workload only)")
     ap.add_argument("--workload", default="octane_b3lyp",
-                    choices=["octane_b3lyp", "c54h18_pbe0_uks", "water_clusters_pbe", "octane_b3lyp_gradient"],
+                    choices=["octane_b3lyp", "c54h18_pbe0_uks", "water_clusters_pbe", "octane_b3lyp_gradient",
+                             "octane_b3lyp_fxc"],
                     help="octane_b3lyp is the headline; the others report the same line for the UKS flake "
                          "and the 64-cluster batched launch; octane_b3lyp_gradient times the XC nuclear "
-                         "gradient (its own metric) on the headline molecule")
+                         "gradient and octane_b3lyp_fxc the TD-DFT kernel contraction (each its own "
+                         "metric) on the headline molecule")
     return ap.parse_args()
 
 
@@ -685,12 +687,81 @@ def run_gradient(args):
     return 0
 
 
+FXC_METRIC = "TD-DFT kernel contraction ms per batch of 16 trial matrices on 1 GB300: tensor-core vs FP64"
+FXC_TRIALS = 16
+
+
+def run_fxc(args):
+    """One step = one FxcKernel.contract_batch of 16 seeded symmetric trial matrices (host buffers in
+    and out, calchem_xc_fxc_contract_ex) on the headline molecule's Fine grid at its ground-state
+    density; the tensor-core form unless --precision fp64, with the FP64 form timed beside it."""
+    import torch
+
+    from calchem_gb300 import FxcKernel, GridLevel, MolecularGrid
+
+    ws, rank, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    prec = "fp64" if args.precision == "fp64" else "mixed"
+    mol, basis, D = build_inputs()
+    grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
+    ker = FxcKernel(basis, grid, "b3lyp", D, precision=prec)
+    rng = np.random.default_rng(SEED)
+    mats = [0.01 * (lambda a: a + a.T)(rng.normal(size=D.shape)) for _ in range(FXC_TRIALS)]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def timed(precision, steps):
+        ts, out = [], None
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = ker.contract_batch(mats, precision=precision)
+            ts.append((time.perf_counter() - t0) * 1e3)
+        return ts, out
+
+    timed(prec, max(3, args.warmup))
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ts, out = timed(prec, args.steps)
+    clk = clocks.stop()
+    t64, ref = timed("fp64", 2)
+    ms = statistics.mean(ts)
+    n = basis.n_ao
+    rel = max(float(np.max(np.abs(a - b)) / np.max(np.abs(b))) for a, b in zip(out, ref))
+    line = {
+        "metric": FXC_METRIC, "value": round(ms, 4), "unit": "ms", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "bf16x4 fixed-point / bf16x3 split contractions",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD + f"; TD-DFT kernel contraction of {FXC_TRIALS} seeded symmetric trial "
+                                          "matrices (singlet) at the ground-state density",
+                   "name": args.workload, "precision": prec, "grid_points": len(grid), "trials": FXC_TRIALS,
+                   "l2": "flushed before every timed step (256 MiB write)", "timing": "host wall clock of the "
+                   "host-buffer call, copies included"},
+        "e2e": {"value": round(ms, 4), "unit": "ms", "h2d_bytes_per_step": FXC_TRIALS * n * n * 8,
+                "d2h_bytes_per_step": FXC_TRIALS * n * n * 8},
+        "gpu_launches": 3 * FXC_TRIALS if prec == "mixed" else 1 + FXC_TRIALS,
+        "clocks": clk,
+        "fp64_plain_ms": round(statistics.mean(t64), 4),
+        "speedup_vs_fp64_plain": round(statistics.mean(t64) / ms, 3),
+        "max_rel_dV_vs_fp64": rel,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ker.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "octane_b3lyp_gradient":
         return run_gradient(args)
+    if args.workload == "octane_b3lyp_fxc":
+        return run_fxc(args)
     return run_ours(args)
 
 
