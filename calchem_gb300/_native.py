@@ -61,6 +61,7 @@ SIGNATURES = {
     "calchem_xc_fxc_prepare": (_I, [_U64, _I, _P]),
     "calchem_xc_fxc_contract": (_I, [_U64, _I, _P, _I, _P]),
     "calchem_xc_fxc_contract_device": (_I, [_U64, _I, _P, _I, _P, _P]),
+    "calchem_xc_fxc_contract_device_ex": (_I, [_U64, _I, _I, _P, _I, _P, _P]),
     "calchem_xc_nuclear_gradient": (_I, [_U64, _I, _I, _I, _P, _P, _P, _P, _I, _P, _P, _P]),
     "calchem_xc_group_create": (_I, [_P, _I, _U64, ctypes.c_size_t]),
     "calchem_xc_group_layout": (_I, [_U64, _P, _P, _P]),

@@ -1377,11 +1377,21 @@ int calchem_xc_fxc_prepare(uint64_t grid_id, int xc_code, const double* h_d_tota
 
 int calchem_xc_fxc_contract_device(uint64_t grid_id, int triplet, const double* d_m, int n_trials, double* d_v_out,
                                    void* stream) {
+  return calchem_xc_fxc_contract_device_ex(grid_id, triplet, CALCHEM_XC_FP64, d_m, n_trials, d_v_out, stream);
+}
+
+int calchem_xc_fxc_contract_device_ex(uint64_t grid_id, int triplet, int precision, const double* d_m, int n_trials,
+                                      double* d_v_out, void* stream) {
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!d_m || !d_v_out || n_trials <= 0) return -1;
+  if (!d_m || !d_v_out || n_trials <= 0 || (precision != CALCHEM_XC_FP64 && precision != CALCHEM_XC_MIXED))
+    return -1;
   Entry* e = find(grid_id);
   if (!e || e->n_mols != 1) return -2;
   if (e->fxc_code < 0) return -1;
+  if (precision == CALCHEM_XC_MIXED) {
+    if (e->max_m > mixed_max_m()) return -2;
+    return enqueue_fxc_mixed(*e, triplet, d_m, n_trials, d_v_out, (cudaStream_t)stream);
+  }
   return enqueue_fxc(*e, triplet, d_m, n_trials, d_v_out, (cudaStream_t)stream);
 }
 

@@ -271,6 +271,9 @@ int calchem_xc_fxc_contract_ex(uint64_t grid_id, int triplet, int precision, con
 /* Device-pointer variant of the contraction (enqueued on `stream`, not synchronised). */
 int calchem_xc_fxc_contract_device(uint64_t grid_id, int triplet, const double* d_m, int n_trials, double* d_v_out,
                                    void* stream);
+/* The device-pointer contraction with a precision (see calchem_xc_fxc_contract_ex). */
+int calchem_xc_fxc_contract_device_ex(uint64_t grid_id, int triplet, int precision, const double* d_m, int n_trials,
+                                      double* d_v_out, void* stream);
 
 /* XC nuclear gradient dExc/dR at fixed densities (xc_nuclear_gradient, vxc.rs:1903-1912 and the
  * Becke weight derivative grid.rs:423-584), entirely on the device: densities, functional, AO force

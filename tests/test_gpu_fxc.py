@@ -94,3 +94,29 @@ def test_tensor_core_contraction_octane():
     ker.close()
     for r, d in zip(ref, got):
         assert np.max(np.abs(d - r)) < 1e-6 * np.max(np.abs(r))
+
+
+def test_device_pointer_contraction_with_precision(setup):
+    """calchem_xc_fxc_contract_device_ex (device buffers, caller's stream) equals the host-buffer call
+    in both precisions."""
+    torch = pytest.importorskip("torch")
+    from calchem_gb300 import _native
+    mol, basis, grid, P0, M = setup
+    ker = FxcKernel(basis, grid, "pbe0", P0)
+    lib = _native.load()
+    dev = torch.device("cuda:0")
+    mats = np.ascontiguousarray(np.stack([M, 0.5 * M.T + 0.5 * M]))
+    d_m = torch.from_numpy(mats).to(dev)
+    d_v = torch.zeros_like(d_m)
+    stream = torch.cuda.current_stream(dev)
+    for prec in ("fp64", "mixed"):
+        host = ker.contract_batch(list(mats), precision=prec)
+        d_v.fill_(7.0)
+        assert lib.calchem_xc_fxc_contract_device_ex(ker.grid_id, 0, 0 if prec == "fp64" else 1, d_m.data_ptr(), 2,
+                                                     d_v.data_ptr(), stream.cuda_stream) == 0
+        torch.cuda.synchronize(dev)
+        out = d_v.cpu().numpy()
+        for a, b in zip(host, out):
+            assert np.max(np.abs(a - b)) < 1e-13 * max(1.0, np.max(np.abs(a)))
+    assert lib.calchem_xc_fxc_contract_device_ex(ker.grid_id, 0, 5, d_m.data_ptr(), 2, d_v.data_ptr(), None) == -1
+    ker.close()
