@@ -97,3 +97,31 @@ def test_mixed_is_deterministic_in_exc(lib):
     n1 = eng.last_nelec
     e2, _ = eng.evaluate(basis, grid, "b3lyp", D)
     assert e1 == e2 and n1 == eng.last_nelec
+
+
+@pytest.mark.parametrize("func", ["svwn5", "blyp", "pbe", "b3lyp", "pbe0"])
+def test_fully_polarised_uks(lib, oracle, func):
+    """A doublet with no beta density anywhere (zeta = 1 at every point: the polarised PW92 / VWN
+    channels, f(zeta) at its end point): both GPU forms against the oracle.  The empty spin's
+    potential follows the reference's formulas there, which for PBE correlation reach ~1e6 through
+    f'(zeta) at zeta = 1, so the potentials are compared relative to their largest entry."""
+    from calchem_gb300.molecule import Atom, Molecule
+    mol = Molecule([Atom.from_angstrom("H", [0.0, 0.0, 0.0])], 0, 2)
+    basis = BasisSet.from_name("6-31g(d,p)", mol)
+    grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.MEDIUM)
+    S = basis.overlap()
+    c = np.zeros(basis.n_ao)
+    c[0], c[1] = 0.6, 0.5
+    c /= np.sqrt(c @ S @ c)  # one normalised alpha orbital
+    Pa = np.outer(c, c)
+    Pb = np.zeros_like(Pa)
+    e_ref, na, nb, Va_ref, Vb_ref = oracle.vxc_uks_points(oracle_basis(oracle, "6-31g(d,p)", mol),
+                                                          oracle.Grid.from_points(grid.xyzw), Pa, Pb, func)
+    assert nb == 0.0 and abs(na - 1.0) < 1e-3
+    for prec, etol, vtol in (("fp64", 1e-9, 1e-10), ("mixed", EXC_TOL, V_TOL)):
+        eng = UksVxcEngine(basis, grid, precision=prec)
+        exc, Va, Vb = eng.evaluate(basis, grid, func, Pa, Pb)
+        eng.close()
+        assert abs(exc - e_ref) < etol, (prec, exc - e_ref)
+        for V, V_ref in ((Va, Va_ref), (Vb, Vb_ref)):
+            assert np.max(np.abs(V - V_ref)) < vtol * max(1.0, np.max(np.abs(V_ref))), prec
