@@ -48,7 +48,7 @@ PRUNE_TOL = 5e-7  # per-molecule quadrature tolerance of the learned grid agains
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # DRAM bytes (read + write) per launch of the quadrature kernel from one ncu capture of this
 # workload; see profiles/.  None until a capture exists for the precision.
-NCU_TRAFFIC_BYTES = {"fp64": 4.120501e9, "mixed": 2.656e9}  # profiles/vxc_fp64_kernel_octane_b3lyp.md, vxc_mixed_kernel_octane_b3lyp_learned_grid.md
+NCU_TRAFFIC_BYTES = {"fp64": 1.746e9, "mixed": 2.656e9}  # profiles/vxc_fp64_kernel_octane_b3lyp.md, vxc_mixed_kernel_octane_b3lyp_learned_grid.md
 
 
 def parse():
@@ -538,7 +538,9 @@ def run_ours(args):
     else:
         tc_peak = fp64_peak_tflops(torch, dev)
         peak_note = "FP64 pipe: cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in the measured peaks)"
-    traffic = NCU_TRAFFIC_BYTES.get(prec_name) if W.name == "octane_b3lyp" else None
+    # the committed captures are of the default (learned-grid) headline build
+    traffic = NCU_TRAFFIC_BYTES.get(prec_name) if (W.name == "octane_b3lyp" and
+                                                   "grid_points_pruned" in W.grid_info) else None
     nspin = 2 if W.kind == "uks" else 1
     # algorithmic bytes per build: D_sub gathered and V_sub scattered per batch and spin (8 B each per
     # AO pair), the points (x, y, z, w), and D in and V out once
