@@ -40,6 +40,7 @@
 #include "mixed_ops.cuh"
 #include "tc_ptx.cuh"
 #include "xc_device.cuh"
+#include "xc_df.cuh"
 
 namespace cxc {
 
@@ -466,7 +467,7 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
       const double rpa = fmax(ra, 0.0), rpb = fmax(rb, 0.0);
       if (live && A.closed && !(rpa + rpb < 1e-18)) {
         // closed shell: the one-spin form (u_a = (2 v_gamma_aa + v_gamma_ab) grad rho_a = 2 v_g grad rho_a)
-        const XcCs o = xc_eval_cs(A.xc, rpa, gax * gax + gay * gay + gaz * gaz);
+        const XcCs o = xc_eval_cs_fast(A.xc, rpa, gax * gax + gay * gay + gaz * gaz, s_tab);
         const double w = G.pw[pt];
         if (fabs(w) > 1e-24) {
           const double us = 2.0 * w * o.vg;
