@@ -11,11 +11,12 @@ from .grid import GridLevel, MolecularGrid
 from .molecule import ANGSTROM_TO_BOHR, Atom, Molecule
 from . import autotune
 from .vxc import (FP64, MIXED, FxcKernel, GpuVxcGrid, RksVxcEngine, UksVxcEngine, VxcGroup, eval_closed_shell_gpu,
-                  evaluate_vxc_rks, evaluate_vxc_uks, is_cuda_available, xc_nuclear_gradient, xc_nuclear_gradient_with_gpu)
+                  evaluate_vxc_rks, evaluate_vxc_uks, is_cuda_available, plan_points, xc_nuclear_gradient,
+                  xc_nuclear_gradient_with_gpu)
 from .xc import XcFunctional
 
 __all__ = [
     "ANGSTROM_TO_BOHR", "Atom", "Molecule", "BasisSet", "GridLevel", "MolecularGrid", "XcFunctional",
     "RksVxcEngine", "UksVxcEngine", "VxcGroup", "FxcKernel", "GpuVxcGrid", "evaluate_vxc_rks", "evaluate_vxc_uks", "is_cuda_available",
-    "xc_nuclear_gradient", "xc_nuclear_gradient_with_gpu", "eval_closed_shell_gpu", "FP64", "MIXED",
+    "xc_nuclear_gradient", "xc_nuclear_gradient_with_gpu", "eval_closed_shell_gpu", "plan_points", "FP64", "MIXED",
 ]

@@ -1104,6 +1104,44 @@ static int upload_points_impl(const AoShellGpu* h_shells, int n_shells, const Ao
   return rc;
 }
 
+int calchem_xc_plan_points(const AoShellGpu* h_shells, int n_shells, const double* h_xyzw, int n_pts, int batch_pts,
+                           int spatial, int* n_batches, int* n_kept, int* n_cand, double* sum_m2n, int* max_m,
+                           int* h_order, int* h_batch_of, int* h_cand_offsets, int* h_cand_shells, int cand_capacity) {
+  if (!h_shells || !h_xyzw || n_shells <= 0 || n_pts <= 0 || batch_pts < 16 || batch_pts > kBlockPts) return -1;
+  for (int s = 0; s < n_shells; ++s)
+    if (!(h_shells[s].r2_cutoff >= 0.0)) return -1;
+  Plan plan;
+  if (spatial)
+    plan_batches_spatial(h_shells, n_shells, h_xyzw, n_pts, plan, batch_pts);
+  else
+    plan_batches(h_shells, n_shells, h_xyzw, n_pts, plan, batch_pts);
+  const int nb = (int)plan.cand_offsets.size() - 1;
+  double s2 = 0.0;
+  int mm = 0;
+  std::vector<int> bpts(std::max(nb, 0), 0);
+  for (const GridPtGpu& p : plan.pts) ++bpts[p.batch_id];
+  for (int b = 0; b < nb; ++b) {
+    int m = 0;
+    for (int c = plan.cand_offsets[b]; c < plan.cand_offsets[b + 1]; ++c) m += h_shells[plan.cand_shells[c]].n_funcs;
+    s2 += (double)m * m * bpts[b];
+    mm = std::max(mm, m);
+  }
+  if (n_batches) *n_batches = nb;
+  if (n_kept) *n_kept = (int)plan.orig.size();
+  if (n_cand) *n_cand = (int)plan.cand_shells.size();
+  if (sum_m2n) *sum_m2n = s2;
+  if (max_m) *max_m = mm;
+  if (h_order) std::copy(plan.orig.begin(), plan.orig.end(), h_order);
+  if (h_batch_of)
+    for (size_t k = 0; k < plan.pts.size(); ++k) h_batch_of[k] = plan.pts[k].batch_id;
+  if (h_cand_offsets) std::copy(plan.cand_offsets.begin(), plan.cand_offsets.end(), h_cand_offsets);
+  if (h_cand_shells) {
+    if ((int)plan.cand_shells.size() > cand_capacity) return -2;
+    std::copy(plan.cand_shells.begin(), plan.cand_shells.end(), h_cand_shells);
+  }
+  return 0;
+}
+
 int calchem_xc_upload_points_ex(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
                                 const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
                                 int batch_pts, uint64_t grid_id, size_t memory_limit_bytes) {

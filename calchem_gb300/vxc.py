@@ -169,6 +169,35 @@ def _upload_points(basis, grid, batch_pts: int = 128, batching: str = "spatial")
     return gid
 
 
+def plan_points(basis, xyzw, batch_pts: int = 128, batching: str = "spatial") -> dict:
+    """The batch plan an engine would upload for these points, computed on the host alone
+    (calchem_xc_plan_points): "order" (the caller's index of each planned point), "batch_of" (its
+    batch), "cand_offsets"/"cand_shells" (candidate shells per batch), "sum_m2n" (sum over batches
+    of m_b^2 n_b, the contraction work), "max_m" (the largest batch's AO count)."""
+    if batching not in BATCHING:
+        raise ValueError(f"batching must be one of {BATCHING}")
+    lib = _native.load()
+    sh, _, _ = basis.gpu_arrays()
+    xyzw = np.ascontiguousarray(getattr(xyzw, "xyzw", xyzw), dtype=np.float64).reshape(-1, 4)
+    n = len(xyzw)
+    if n == 0:
+        raise ValueError("empty grid")
+    nb, nk, nc, mm = (np.zeros(1, np.int32) for _ in range(4))
+    s2 = np.zeros(1)
+    spatial = int(batching == "spatial")
+    args = (_native.ptr(sh), len(sh), _native.ptr(xyzw), n, int(batch_pts), spatial)
+    _native.check("calchem_xc_plan_points", lib.calchem_xc_plan_points(
+        *args, _native.ptr(nb), _native.ptr(nk), _native.ptr(nc), None, None, None, None, None, None, 0))
+    order, batch_of = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    offs, cand = np.zeros(int(nb[0]) + 1, np.int32), np.zeros(max(int(nc[0]), 1), np.int32)
+    _native.check("calchem_xc_plan_points", lib.calchem_xc_plan_points(
+        *args, None, None, None, _native.ptr(s2), _native.ptr(mm), _native.ptr(order), _native.ptr(batch_of),
+        _native.ptr(offs), _native.ptr(cand), len(cand)))
+    k = int(nk[0])
+    return {"order": order[:k], "batch_of": batch_of[:k], "cand_offsets": offs, "cand_shells": cand[:int(nc[0])],
+            "sum_m2n": float(s2[0]), "max_m": int(mm[0])}
+
+
 class _EngineBase:
     """batch_pts: points per batch (16..128; the reference's 128 by default), or "auto" to take
     the autotuner's choice for this workload (tuned on first use, then cached).  batching:

@@ -174,6 +174,18 @@ int calchem_xc_upload_points_ex(const AoShellGpu* h_shells, int n_shells, const 
                                 const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
                                 int batch_pts, uint64_t grid_id, size_t memory_limit_bytes);
 
+/* The batch plan of the two upload functions below, computed on the host only (no device): spatial = 0
+ * CalChem's chunks (calchem_xc_upload_points_ex), 1 compact batches (calchem_xc_upload_points_spatial).
+ * Outputs (each may be NULL): the number of batches, of kept points (|w| >= 1e-24, in a batch with a
+ * candidate shell) and of candidate entries; sum over batches of m_b^2 n_b (m_b the batch's AO count)
+ * and the largest m_b; h_order[k] = the caller's index of the k-th planned point and h_batch_of[k]
+ * its batch (n_kept entries each: n_pts always suffice); h_cand_offsets (n_batches + 1 entries,
+ * n_pts + 1 suffice) and h_cand_shells (n_cand entries, at most cand_capacity: -2 if more) the
+ * candidate shells per batch.  Returns 0, -1 on bad arguments. */
+int calchem_xc_plan_points(const AoShellGpu* h_shells, int n_shells, const double* h_xyzw, int n_pts, int batch_pts,
+                           int spatial, int* n_batches, int* n_kept, int* n_cand, double* sum_m2n, int* max_m,
+                           int* h_order, int* h_batch_of, int* h_cand_offsets, int* h_cand_shells, int cand_capacity);
+
 /* As calchem_xc_upload_points_ex with spatially compact batches instead of consecutive chunks: the
  * points are ordered by recursive bisection along the longest axis of their box (leaves of batch_pts
  * points; ties broken by index, so the plan is the same on every machine) before chunking, and each
