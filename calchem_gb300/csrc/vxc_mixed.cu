@@ -568,7 +568,23 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
     }
     if (failed) break;
 
-    // (E) functional, one thread per point (threads with h == 0)
+    // (E) functional, one thread per point (threads with h == 0).  The closed-shell functional is
+    // split between the halves: exchange terms in threads h == 0, correlation terms in threads
+    // h == 1 (passed through dens, idle until the image pass), summed as xc_eval_cs_fast sums them.
+    XcCs xpart{0.0, 0.0, 0.0};
+    if (!uks && A.mode != kModeFxc) {
+      const double ra = spin_rho[0][0];
+      if (g < bd.n_pts && !(ra < 1e-18)) {
+        const double gax = 2.0 * spin_rho[0][1], gay = 2.0 * spin_rho[0][2], gaz = 2.0 * spin_rho[0][3];
+        xpart = xc_eval_cs_fast_part(A.xc, 0.5 * ra, 0.25 * (gax * gax + gay * gay + gaz * gaz), s_tab, h);
+      }
+      if (h == 1) {
+        dens[1][0][g] = xpart.f;
+        dens[1][1][g] = xpart.vr;
+        dens[1][2][g] = xpart.vg;
+      }
+      __syncthreads();
+    }
     double e_loc = 0, na_loc = 0, nb_loc = 0;
     if (h == 0) {
       const bool live = g < bd.n_pts;
@@ -594,9 +610,7 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
       } else if (!uks) {
         if (live && !(ra < 1e-18)) {
           const double w = G.pw[pt];
-          const double rs = 0.5 * ra;
-          const double gss = 0.25 * (gax * gax + gay * gay + gaz * gaz);
-          const XcCs o = xc_eval_cs_fast(A.xc, rs, gss, s_tab);
+          const XcCs o{xpart.f + dens[1][0][g], xpart.vr + dens[1][1][g], xpart.vg + dens[1][2][g]};
           e_loc = w * o.f;
           na_loc = w * ra;
           const double us = w * o.vg;

@@ -147,20 +147,23 @@ __device__ __forceinline__ void pw92_df(df32 rs, const df32* tab, df32& g, df32&
 }
 
 // xc_eval_cs for codes 0-5 (SVWN5, BLYP, PBE, B3LYP, B3LYP5, PBE0) at spin density r and
-// gamma_ss g, for r + r >= kDfRhoMin.  tab: the 2^(-j/64) table of df_exp_neg.
-__device__ __forceinline__ XcCsDf xc_eval_cs_df(int code, df32 r, df32 g, const df32* tab) {
+// gamma_ss g, for r + r >= kDfRhoMin: part 0 the exchange terms (Slater, B88, PBE exchange), part 1
+// the correlation terms (VWN, LYP, PBE correlation); the functional is their sum.  tab: the
+// 2^(-j/64) table of df_exp_neg.
+__device__ __forceinline__ XcCsDf xc_eval_cs_df(int code, df32 r, df32 g, const df32* tab, int part) {
   using namespace dfo;
   XcCsDf o{df32{0.f, 0.f}, df32{0.f, 0.f}, df32{0.f, 0.f}};
   if (g.hi < 0.f) g = df32{0.f, 0.f};
   const df32 rho = r * 2.f;
   const df32 c13 = df_cbrt(r);
   const df32 rho13 = dfc(kCsCbrt2) * c13;
-  if (code == 0 || code == 1 || code == 3 || code == 4) {  // Slater
+  const bool xpart = part == 0, cpart = !xpart;
+  if (xpart && (code == 0 || code == 1 || code == 3 || code == 4)) {  // Slater
     const df32 sc = (code == 3 || code == 4) ? dfc(0.80) : df32{1.f, 0.f};
     o.f += sc * (dfc(-2.0 * kCsCx) * r * c13);
     o.vr += sc * (dfc(-(4.0 / 3.0) * kCsCx) * c13);
   }
-  if (code == 1 || code == 3 || code == 4) {  // B88
+  if (xpart && (code == 1 || code == 3 || code == 4)) {  // B88
     const df32 sc = code == 1 ? df32{1.f, 0.f} : dfc(0.72);
     const df32 beta = dfc(0.0042);
     const df32 r43 = r * c13;
@@ -176,7 +179,7 @@ __device__ __forceinline__ XcCsDf xc_eval_cs_df(int code, df32 r, df32 g, const 
     o.vr += sc * (dfc(4.0 / 3.0) * c13 * (gfun - s2 * h));
     o.vg += sc * (0.5f * h / r43);
   }
-  if (code == 2 || code == 5) {  // PBE exchange (spin scaling: rho_u = rho, gamma_u = 4g)
+  if (xpart && (code == 2 || code == 5)) {  // PBE exchange (spin scaling: rho_u = rho, gamma_u = 4g)
     const float sc = code == 2 ? 1.f : 0.75f;
     const df32 r43 = rho * rho13;
     const df32 exl = dfc(kCsCxu) * r43;
@@ -190,7 +193,7 @@ __device__ __forceinline__ XcCsDf xc_eval_cs_df(int code, df32 r, df32 g, const 
     o.vr += sc * (dfc((4.0 / 3.0) * kCsCxu) * rho13 * fx + exl * dfx * (dfc(-(8.0 / 3.0)) * s2 / rho));
     o.vg += sc * (2.f * (exl * dfx / den_s2));
   }
-  if (code == 0 || code == 3 || code == 4) {  // VWN5 / VWN_RPA, paramagnetic channel
+  if (cpart && (code == 0 || code == 3 || code == 4)) {  // VWN5 / VWN_RPA, paramagnetic channel
     const df32 sc = code == 0 ? df32{1.f, 0.f} : dfc(0.19);
     const VwnDf ch = code == 3 ? vwn_df(kVwnRpaPara) : vwn_df(kVwn5Para);
     const df32 x = df_sqrt(dfc(kCsRsK) / rho13);
@@ -202,7 +205,7 @@ __device__ __forceinline__ XcCsDf xc_eval_cs_df(int code, df32 r, df32 g, const 
     o.f += sc * (rho * ep);
     o.vr += sc * (ep - dfc(1.0 / 3.0) * dp);
   }
-  if (code == 1 || code == 3 || code == 4) {  // LYP
+  if (cpart && (code == 1 || code == 3 || code == 4)) {  // LYP
     const df32 sc = code == 1 ? df32{1.f, 0.f} : dfc(0.81);
     constexpr double A = 0.04918, B = 0.132, C = 0.2533, D = 0.349;
     const df32 rm13 = df32{1.f, 0.f} / rho13;
@@ -246,7 +249,7 @@ __device__ __forceinline__ XcCsDf xc_eval_cs_df(int code, df32 r, df32 g, const 
       o.vg += sc * (-(ab * omega * (aaa + 0.5f * aab)));
     }
   }
-  if (code == 2 || code == 5) {  // PBE correlation on the paramagnetic PW92 channel
+  if (cpart && (code == 2 || code == 5)) {  // PBE correlation on the paramagnetic PW92 channel
     const df32 gt = 4.f * g;
     const df32 rs = dfc(kCsRsK) / rho13;
     const df32 drs = -rs / (3.f * rho);
@@ -286,14 +289,23 @@ __device__ __forceinline__ XcCsDf xc_eval_cs_df(int code, df32 r, df32 g, const 
   return o;
 }
 
-// The closed-shell functional for the tensor-core kernels: the double-float form for codes 0-5 at
-// total density >= kDfRhoMin, xc_eval_cs (FP64) otherwise.  Results as doubles.
-__device__ __forceinline__ XcCs xc_eval_cs_fast(int code, double r, double g, const df32* tab) {
+// One part (0 exchange, 1 correlation) of the closed-shell functional for the tensor-core kernels:
+// the double-float form for codes 0-5 at total density >= kDfRhoMin; otherwise part 0 is all of
+// xc_eval_cs (FP64) and part 1 zero.  Results as doubles.
+__device__ __forceinline__ XcCs xc_eval_cs_fast_part(int code, double r, double g, const df32* tab, int part) {
   if (code <= 5 && !(r + r < kDfRhoMin)) {
-    const XcCsDf d = xc_eval_cs_df(code, df_from_double(r), df_from_double(fmax(g, 0.0)), tab);
+    const XcCsDf d = xc_eval_cs_df(code, df_from_double(r), df_from_double(fmax(g, 0.0)), tab, part);
     return XcCs{df_to_double(d.f), df_to_double(d.vr), df_to_double(d.vg)};
   }
+  if (part != 0) return XcCs{0.0, 0.0, 0.0};
   return xc_eval_cs(code, r, g);
+}
+
+// The two parts summed in FP64 (part 0 + part 1), as the Vxc kernel sums them across its halves.
+__device__ __forceinline__ XcCs xc_eval_cs_fast(int code, double r, double g, const df32* tab) {
+  const XcCs x = xc_eval_cs_fast_part(code, r, g, tab, 0);
+  const XcCs c = xc_eval_cs_fast_part(code, r, g, tab, 1);
+  return XcCs{x.f + c.f, x.vr + c.vr, x.vg + c.vg};
 }
 
 }  // namespace cxc

@@ -456,7 +456,23 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
     }
     if (failed) break;
 
-    // (C) functional, one thread per point: coef rows (w v_rho_a, w u_a, w v_rho_b, w u_b, f)
+    // (C) functional, one thread per point: coef rows (w v_rho_a, w u_a, w v_rho_b, w u_b, f).  A
+    // closed shell's functional is split between the halves: exchange terms in threads h == 0,
+    // correlation terms in threads h == 1 (passed through dens), summed as xc_eval_cs_fast sums them.
+    XcCs xpart{0.0, 0.0, 0.0};
+    if (A.closed) {
+      const double rpa = fmax(spin_rho[0][0], 0.0);
+      if (live && !(rpa + rpa < 1e-18)) {
+        const double gax = 2.0 * spin_rho[0][1], gay = 2.0 * spin_rho[0][2], gaz = 2.0 * spin_rho[0][3];
+        xpart = xc_eval_cs_fast_part(A.xc, rpa, gax * gax + gay * gay + gaz * gaz, s_tab, h);
+      }
+      if (h == 1) {
+        dens[1][0][g] = xpart.f;
+        dens[1][1][g] = xpart.vr;
+        dens[1][2][g] = xpart.vg;
+      }
+      __syncthreads();
+    }
     if (h == 0) {
       double cf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
       const double ra = spin_rho[0][0];
@@ -467,7 +483,7 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
       const double rpa = fmax(ra, 0.0), rpb = fmax(rb, 0.0);
       if (live && A.closed && !(rpa + rpb < 1e-18)) {
         // closed shell: the one-spin form (u_a = (2 v_gamma_aa + v_gamma_ab) grad rho_a = 2 v_g grad rho_a)
-        const XcCs o = xc_eval_cs_fast(A.xc, rpa, gax * gax + gay * gay + gaz * gaz, s_tab);
+        const XcCs o{xpart.f + dens[1][0][g], xpart.vr + dens[1][1][g], xpart.vg + dens[1][2][g]};
         const double w = G.pw[pt];
         if (fabs(w) > 1e-24) {
           const double us = 2.0 * w * o.vg;
