@@ -78,6 +78,18 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(dist, value, device):
+    """The largest of every rank's value (N replicas: the job takes as long as its slowest rank);
+    the value itself with no process group."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def build_inputs():
     from calchem_gb300 import BasisSet, workloads
 
@@ -463,10 +475,7 @@ def run_ours(args):
             _native.check("last_kernel_ms", lib.calchem_xc_last_kernel_ms(W.gid, _native.ptr(km)))
             kern_ms.append(float(km[0]))
     kms = statistics.mean(kern_ms)
-    if dist:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(dist, ms, dev)
     # ---- e2e through the host-buffer C ABI call (copies inside the timed region)
     e2e = []
     host = None
