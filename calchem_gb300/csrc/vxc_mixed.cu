@@ -27,7 +27,8 @@
 //       buffer is refilled once every warp has arrived on its release barrier) and rho,
 //       grad rho = 2 sum grad Phi T are compensated sums of double-float products;
 //   (E) the functional per point (double-float for the closed-shell codes 0-5 above 1e-12, FP64
-//       otherwise), Exc and Nelec partial sums in FP64 (vxc.rs:890-920);
+//       otherwise; a closed shell's exchange and correlation terms in the two 128-thread halves),
+//       Exc and Nelec partial sums in FP64 (vxc.rs:890-920);
 //   (F) GEMM2  W = Z^T Phi + Phi^T Z  (Z = (w v_rho / 2) Phi + (w u) . grad Phi) on lower
 //       128 x 128 AO tile pairs, K = 64 points per step: Phi and Z split into three BF16 pieces
 //       (floating, 24 bits), written as swizzled tiles and loaded by bulk copies (for m <= 128, one
