@@ -127,6 +127,11 @@ def test_ragged_and_degenerate_point_sets():
         assert np.bincount(p["batch_of"]).max() <= 128
     sp = plan_points(basis, xyzw, 128, "spatial")
     assert all(np.array_equal(sp[k], plan_points(basis, xyzw, 128, "spatial")[k]) for k in sp)
+    # every weight zero: no batch and no point in either plan (the uploads then refuse the grid)
+    xyzw[:, 3] = 0.0
+    for batching in ("reference", "spatial"):
+        p = plan_points(basis, xyzw, 128, batching)
+        assert len(p["order"]) == 0 and list(p["cand_offsets"]) == [0] and p["max_m"] == 0
 
 
 def test_argument_checks(native_lib):
