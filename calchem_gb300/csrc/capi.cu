@@ -1126,6 +1126,8 @@ int calchem_xc_plan_points(const AoShellGpu* h_shells, int n_shells, const doubl
     s2 += (double)m * m * bpts[b];
     mm = std::max(mm, m);
   }
+  // a candidate buffer that is too small fails the call before any output is written
+  if (h_cand_shells && (int)plan.cand_shells.size() > cand_capacity) return -2;
   if (n_batches) *n_batches = nb;
   if (n_kept) *n_kept = (int)plan.orig.size();
   if (n_cand) *n_cand = (int)plan.cand_shells.size();
@@ -1135,10 +1137,7 @@ int calchem_xc_plan_points(const AoShellGpu* h_shells, int n_shells, const doubl
   if (h_batch_of)
     for (size_t k = 0; k < plan.pts.size(); ++k) h_batch_of[k] = plan.pts[k].batch_id;
   if (h_cand_offsets) std::copy(plan.cand_offsets.begin(), plan.cand_offsets.end(), h_cand_offsets);
-  if (h_cand_shells) {
-    if ((int)plan.cand_shells.size() > cand_capacity) return -2;
-    std::copy(plan.cand_shells.begin(), plan.cand_shells.end(), h_cand_shells);
-  }
+  if (h_cand_shells) std::copy(plan.cand_shells.begin(), plan.cand_shells.end(), h_cand_shells);
   return 0;
 }
 

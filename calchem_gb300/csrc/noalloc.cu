@@ -12,7 +12,9 @@
 //     loads this library holds it until the process exits;
 //   * host code cannot use the symbol name as a device address, so the first call on each device
 //     looks the address up with cudaGetSymbolAddress while that device is current and caches it;
-//     that first call should therefore come before any stream capture on the device;
+//     that first call should therefore come before any stream capture on the device.  The cached
+//     address belongs to the device's current primary context: after a cudaDeviceReset the entry
+//     point must not be called again in the same process;
 //   * every call reuses it and it keeps the previous call's contents: the queue head and status
 //     word are cleared at the start of each call, everything else is overwritten before it is read;
 //   * calls whose work overlaps on the GPU (other streams, other host threads) race on it.  The
@@ -46,12 +48,17 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // Status bits written by the table kernels when the caller's layout is inconsistent.
 enum : int { kBadBatch = 1, kBadShell = 2, kBadSize = 4 };
 
-// Points (AoS with batch ids) -> SoA coordinates and weights.
+// Points (AoS with batch ids) -> SoA coordinates and weights.  Also checks the batch ids: each in
+// [0, n_batches) and none smaller than its predecessor's (the later kernels find a batch's points by
+// binary search over the ids).  With ids in range and in order, the per-batch point ranges partition
+// the points, so their counts add up to n_pts.
 __global__ void soa_points_kernel(const GridPtGpu* __restrict__ pts, const double* __restrict__ w, int n_pts,
-                                  double* __restrict__ soa) {
+                                  int n_batches, double* __restrict__ soa, int* __restrict__ status) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n_pts) return;
   const GridPtGpu p = pts[g];
+  if (p.batch_id < 0 || p.batch_id >= n_batches || (g > 0 && pts[g - 1].batch_id > p.batch_id))
+    atomicOr(status, kBadBatch);
   soa[g] = p.x;
   soa[(size_t)n_pts + g] = p.y;
   soa[2 * (size_t)n_pts + g] = p.z;
@@ -134,12 +141,14 @@ __global__ void __launch_bounds__(1024) ao_offsets_kernel(const int* __restrict_
   }
 }
 
-// One thread per batch: local AO offset of each candidate and the local -> global AO list.
+// One thread per batch: local AO offset of each candidate and the local -> global AO list.  Skipped
+// entirely when an earlier kernel flagged the layout: the AO list's capacity (10 entries per
+// candidate) holds only for candidate ranges that are all valid.
 __global__ void ao_lists_kernel(const AoShellGpu* __restrict__ shells, const int* __restrict__ cand_sh,
                                 const BatchDesc* __restrict__ bd, int n_batches, int* __restrict__ cand_loc,
-                                int* __restrict__ batch_ao) {
+                                int* __restrict__ batch_ao, const int* __restrict__ status) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= n_batches) return;
+  if (b >= n_batches || *status != 0) return;
   const BatchDesc d = bd[b];
   int loc = 0;
   for (int c = 0; c < d.n_cand; ++c) {
@@ -215,13 +224,13 @@ extern "C" int calchem_xc_evaluate_rks_static(const AoShellGpu* d_shells, int n_
 
   bool ok = cudaMemsetAsync(status, 0, 4 * sizeof(int), st) == cudaSuccess;
   if (ok) {
-    soa_points_kernel<<<(n_pts + 255) / 256, 256, 0, st>>>(d_pts, d_weights, n_pts, soa);
+    soa_points_kernel<<<(n_pts + 255) / 256, 256, 0, st>>>(d_pts, d_weights, n_pts, n_batches, soa, status);
     batch_tables_kernel<<<(n_batches + 127) / 128, 128, 0, st>>>(d_shells, n_shells, n_prims, n_comps, d_pts, n_pts,
                                                                  d_cand_offsets, d_cand_shells, n_batches,
                                                                  n_cand_shells, n_ao, max_batch_ao, bd, mcount, status);
     ao_offsets_kernel<<<1, 1024, 0, st>>>(mcount, n_batches, bd, order);
     ao_lists_kernel<<<(n_batches + 127) / 128, 128, 0, st>>>(d_shells, d_cand_shells, bd, n_batches, cand_loc,
-                                                             batch_ao);
+                                                             batch_ao, status);
     ok = cudaGetLastError() == cudaSuccess;
   }
   int h_status = 0;

@@ -45,4 +45,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python calchem_gb300/data/extract_basis.py /path/to/CalChem")
+    main(sys.argv[1])

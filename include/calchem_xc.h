@@ -181,7 +181,9 @@ int calchem_xc_upload_points_ex(const AoShellGpu* h_shells, int n_shells, const 
  * and the largest m_b; h_order[k] = the caller's index of the k-th planned point and h_batch_of[k]
  * its batch (n_kept entries each: n_pts always suffice); h_cand_offsets (n_batches + 1 entries,
  * n_pts + 1 suffice) and h_cand_shells (n_cand entries, at most cand_capacity: -2 if more) the
- * candidate shells per batch.  Returns 0, -1 on bad arguments. */
+ * candidate shells per batch.  Returns 0; -1 on bad arguments; -2 when h_cand_shells is given and
+ * the plan has more than cand_capacity candidates (checked before any output is written, so a
+ * failed call leaves every caller buffer as it was). */
 int calchem_xc_plan_points(const AoShellGpu* h_shells, int n_shells, const double* h_xyzw, int n_pts, int batch_pts,
                            int spatial, int* n_batches, int* n_kept, int* n_cand, double* sum_m2n, int* max_m,
                            int* h_order, int* h_batch_of, int* h_cand_offsets, int* h_cand_shells, int cand_capacity);
@@ -400,11 +402,13 @@ int calchem_scf_eri(const AoShellGpu* shells, int n_shells, const AoPrimGpu* pri
  * AOs of any batch, d_total (n_ao x n_ao), d_result (Exc, Nelec) and d_v (n_ao x n_ao, full symmetric).
  * All working memory comes from the static buffer above; nothing is allocated.
  *   - The first call on a device looks up the buffer's device address (cudaGetSymbolAddress); make
- *     that first call before any stream capture on that device.
+ *     that first call before any stream capture on that device.  The address is kept for the life of
+ *     the process, so do not call this entry point after a cudaDeviceReset.
  *   - Work on `stream` (a cudaStream_t, 0 for the legacy stream); returns after it completes.
  *   - Returns -3 when the points, tables and one CTA's working set do not fit in the buffer
- *     (large n_pts or max_batch_ao), -2 when the layout is inconsistent (a batch of more than 128
- *     points, a shell index or range out of bounds, a batch with more than max_batch_ao AOs), -1
+ *     (large n_pts or max_batch_ao), -2 when the layout is inconsistent (a batch id outside
+ *     [0, n_batches) or smaller than the previous point's, a batch of more than 128 points, a shell
+ *     index or range out of bounds, a batch with more than max_batch_ao AOs), -1
  *     for null pointers or non-positive sizes, -5 for a launch or copy failure.
  *   - Every call shares the buffer and finds the previous call's contents in it (the work-queue head
  *     and status word are cleared on entry, the rest is overwritten before use).  Calls through this
