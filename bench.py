@@ -1,29 +1,33 @@
 """Benchmark: Vxc build time per SCF iteration on one GB300.
 
-Workload (the configuration the headline metric is quoted on): n-octane C8H18
-(all-trans, C-C 1.54 / C-H 1.09 Angstrom, tetrahedral), B3LYP (VWN_RPA),
-6-31G(d,p) Cartesian (210 AOs), CalChem's Fine grid (99 radial shells, pruned
-Lebedev, Becke partition), seeded S-orthonormal density (33 occupied orbitals,
-PCG64 seed 7).  One step = one full Vxc build (D -> Exc, Nelec, Vxc).  The timed
-build runs on the learned grid with spatially compact batches (points ordered by
-recursive bisection); the FP64-plain comparison runs CalChem's batching (chunks
-of consecutive points) on the Fine grid.  A step is one SCF iteration of a
-built engine: the AO cache (per-batch AO values, gradients and packed operand,
-kept across iterations as CalChem's RksVxcEngine keeps its AO cache) is filled
-before the timed steps, and the line reports the build without it as well.
+Workload (the configuration the headline metric is quoted on): the 61-molecule water cluster
+(H2O)61, 183 atoms, rigid waters at 1 g/cm^3 with O-O >= 2.6 Angstrom (PCG64 seed 61), B3LYP
+(VWN_RPA), 6-31G(d) Cartesian (1159 AOs), seeded S-orthonormal density (244 occupied orbitals, seed
+7).  One step = one SCF iteration's XC work on a built engine: the Vxc build (D -> Exc, Nelec, Vxc)
+in the tensor-core form on the MLP-pruned grid with spatially compact batches, plus, on every
+JUDGE_EVERY-th iteration, the periodic full-grid judge (per-atom shares of the pruned atoms on their
+Fine and pruned points, tensor-core form, resident uploads), so the mean step is the per-iteration
+cost with the judge amortised.  The FP64-plain comparison runs CalChem's batching (chunks of
+consecutive points) on the full Fine grid.  The AO caches (per-batch AO values, gradients and packed
+operand, kept across iterations as CalChem's RksVxcEngine keeps its AO cache) are filled before the
+timed steps; the line reports the build without them as well.  ``--workload octane_b3lyp`` runs the
+same line on n-octane C8H18 / 6-31G(d,p).
 
-* value: mean device time of one build with D already resident in HBM, CUDA
-  events on the launch stream, L2 flushed (256 MiB write) before every step.
-* e2e: the same build through the host-buffer C ABI call
-  (calchem_xc_evaluate_rks), host<->device copies inside the timed region.
-* roofline: the quadrature kernel, algorithmic work 4 * sum_b m_b^2 n_b flops
-  (RKS contractions), timed by CUDA events around that kernel.
-* cpu_baseline: the oracle's restatement of CalChem's RksVxcEngine CPU path on
-  this host's cores (the reference's Rust cannot be built offline).
+* value: mean device time of one step with D already resident in HBM, CUDA events on the launch
+  stream, L2 flushed (256 MiB write) before every step.
+* e2e: the same step through the host-buffer C ABI calls (calchem_xc_evaluate_rks, and
+  calchem_xc_evaluate_rks_atoms for the judge), host<->device copies inside the timed region.
+* roofline: the quadrature kernel of the build, algorithmic work 4 * sum_b m_b^2 n_b flops (RKS
+  contractions) and 16 * sum_b m_b^2 + 32 N + 16 n^2 bytes, timed by CUDA events around that kernel.
+* cpu_baseline: the oracle's restatement of CalChem's RksVxcEngine cached-AO CPU path (two
+  contractions per batch by a register-blocked FMA GEMM, as CalChem's faer GEMM) on this host's
+  cores, timed on a strided sample of CalChem's 128-point chunks of the Fine grid and scaled to the
+  whole grid (the reference's Rust cannot be built offline).
 
-``--impl reference`` times that CPU restatement as the reference arm.
-With N > 1 GPUs (torchrun) every rank runs an independent replica (the path is
-one GPU by design), and the reported value is the maximum over ranks.
+``--impl reference`` times that CPU restatement as the reference arm (oracle only: the molecule,
+basis, overlap, density and grid all come from the oracle and numpy).  With N > 1 GPUs (torchrun)
+every rank runs an independent replica (the path is one GPU by design), and the reported value is
+the maximum over ranks.
 """
 
 import argparse
@@ -41,14 +45,23 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Vxc build ms/SCF iter on 1 GB300: mixed+pruned vs FP64 plain at dExc<=1e-6 Eh"
-WORKLOAD = ("C8H18 all-trans, B3LYP (VWN_RPA), 6-31G(d,p) Cartesian 210 AOs, CalChem Fine grid "
-            "(99 radial shells, pruned Lebedev, Becke), seeded S-orthonormal D (33 occ, seed 7)")
 SEED = 7
 PRUNE_TOL = 5e-7  # per-molecule quadrature tolerance of the learned grid against the Fine grid (Eh)
+JUDGE_EVERY = 5   # SCF iterations between full-grid checks (calchem_gb300.scf's default)
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
-# DRAM bytes (read + write) per launch of the quadrature kernel from one ncu capture of this
-# workload; see profiles/.  None until a capture exists for the precision.
-NCU_TRAFFIC_BYTES = {"fp64": 1.746e9, "mixed": 2.656e9}  # profiles/vxc_fp64_kernel_octane_b3lyp.md, vxc_mixed_kernel_octane_b3lyp_learned_grid.md
+# The learned-grid RKS workloads: (molecule builder name and argument, basis, functional, description)
+RKS_WORKLOADS = {
+    "water61_b3lyp": (("water_cluster", (61, 61)), "6-31g(d)", "b3lyp",
+                      "(H2O)61 water cluster, 183 atoms (rigid waters, 1 g/cm^3, O-O >= 2.6 A, PCG64 seed 61), "
+                      "B3LYP (VWN_RPA), 6-31G(d) Cartesian 1159 AOs, CalChem Fine grid (99 radial shells, pruned "
+                      "Lebedev, Becke) as judge, seeded S-orthonormal D (244 occ, seed 7)"),
+    "octane_b3lyp": (("octane", ()), "6-31g(d,p)", "b3lyp",
+                     "C8H18 all-trans, B3LYP (VWN_RPA), 6-31G(d,p) Cartesian 210 AOs, CalChem Fine grid "
+                     "(99 radial shells, pruned Lebedev, Becke) as judge, seeded S-orthonormal D (33 occ, seed 7)"),
+}
+# DRAM bytes (read + write) per launch of the quadrature kernel from one ncu capture of the workload's
+# timed build (profiles/); absent until a capture exists for the workload and precision.
+NCU_TRAFFIC_BYTES = {("octane_b3lyp", "fp64"): 1.746e9, ("octane_b3lyp", "mixed"): 2.656e9}
 
 
 def parse():
@@ -60,14 +73,13 @@ def parse():
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", default="learned", choices=["learned", "fine"],
-                    help="learned: the MLP-pruned grid with the Fine-grid judge (headline workload only)")
-    ap.add_argument("--workload", default="octane_b3lyp",
-                    choices=["octane_b3lyp", "c54h18_pbe0_uks", "water_clusters_pbe", "octane_b3lyp_gradient",
-                             "octane_b3lyp_fxc"],
-                    help="octane_b3lyp is the headline; the others report the same line for the UKS flake "
-                         "and the 64-cluster batched launch; octane_b3lyp_gradient times the XC nuclear "
-                         "gradient and octane_b3lyp_fxc the TD-DFT kernel contraction (each its own "
-                         "metric) on the headline molecule")
+                    help="learned: the MLP-pruned grid with the periodic Fine-grid judge (RKS workloads)")
+    ap.add_argument("--workload", default="water61_b3lyp",
+                    choices=["water61_b3lyp", "octane_b3lyp", "c54h18_pbe0_uks", "water_clusters_pbe",
+                             "octane_b3lyp_gradient", "octane_b3lyp_fxc"],
+                    help="water61_b3lyp is the headline; octane_b3lyp, the UKS flake and the 64-cluster batched "
+                         "launch report the same line; octane_b3lyp_gradient times the XC nuclear gradient and "
+                         "octane_b3lyp_fxc the TD-DFT kernel contraction (each its own metric)")
     return ap.parse_args()
 
 
@@ -90,13 +102,22 @@ def max_over_ranks(dist, value, device):
     return float(t.item())
 
 
-def build_inputs():
+def rks_molecule(name):
+    """(molecule, basis name, functional, description) of a learned-grid RKS workload (pure Python:
+    no native library is loaded)."""
+    from calchem_gb300 import workloads
+
+    (builder, args), bname, func, desc = RKS_WORKLOADS[name]
+    return getattr(workloads, builder)(*args), bname, func, desc
+
+
+def build_inputs(name="octane_b3lyp"):
+    """(molecule, basis, D) of an RKS workload with the product's basis and overlap."""
     from calchem_gb300 import BasisSet, workloads
 
-    mol = workloads.octane()
-    basis = BasisSet.from_name("6-31g(d,p)", mol)
-    S = basis.overlap()
-    D = workloads.seeded_density_rks(S, mol.nelectron() // 2, SEED)
+    mol, bname, _, _ = rks_molecule(name)
+    basis = BasisSet.from_name(bname, mol)
+    D = workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, SEED)
     return mol, basis, D
 
 
@@ -196,48 +217,68 @@ def roofline(flops, bytes_alg, kms, tc_peak, tc_unit_note, traffic, kernel, work
             "peak_source": note}
 
 
-def cpu_reference_run(basis, mol, D, steps, warmup, budget_s=150.0):
-    """Times the oracle's restatement of CalChem's RksVxcEngine CPU path (all host threads)."""
+def cpu_reference_run(name, steps, warmup, budget_s=20.0, fine_xyzw=None):
+    """Times the oracle's restatement of CalChem's RksVxcEngine CPU path (cached-AO, both contractions
+    by the register-blocked FMA GEMM, all host threads) on a strided sample of CalChem's 128-point
+    chunks of the Fine grid, scaled to the whole grid.  Everything comes from the oracle and numpy
+    (fine_xyzw: the Fine grid's points when the caller already has them; the oracle builds the same
+    grid bit for bit otherwise).  Returns (ms per build, threads, sample description)."""
+    from calchem_gb300 import workloads
     from oracle import oracle as O
 
-    og = O.Grid.build(mol.z, mol.coords_bohr, "fine")
-    ob = O.Basis.from_name("6-31g(d,p)", [a.symbol for a in mol.atoms], mol.coords_bohr)
-    eng = O.RksEngine(ob, og)
+    mol, bname, func, _ = rks_molecule(name)
+    ob = O.Basis.from_name(bname, [a.symbol for a in mol.atoms], mol.coords_bohr)
+    D = workloads.seeded_density_rks(ob.overlap(), mol.nelectron() // 2, SEED)
+    if fine_xyzw is None:
+        fine_xyzw = O.Grid.build(mol.z, mol.coords_bohr, "fine").points()[0]
     threads = O.max_threads()
+    n_chunks = (len(fine_xyzw) + 127) // 128
+
+    def sample(stride):
+        idx = np.concatenate([np.arange(c * 128, min(c * 128 + 128, len(fine_xyzw)))
+                              for c in range(0, n_chunks, stride)])
+        eng = O.RksEngine(ob, O.Grid.from_points(fine_xyzw[idx]), cap_bytes=1e12)
+        return eng, len(range(0, n_chunks, stride))
+
+    # probe with a sparse sample, then size the sample so that (warmup + steps) builds take ~budget_s
+    stride = max(1, n_chunks // 48)
+    eng, k = sample(stride)
     t0 = time.perf_counter()
-    e_full, n_full, _ = eng.evaluate(D, "b3lyp")
-    t_full = time.perf_counter() - t0
-    frac = 1.0
-    nb = eng.n_batches
-    if t_full * (steps + warmup) > budget_s and eng.cached:
-        frac = max(0.02, budget_s / (t_full * (steps + warmup)))
-    sample_b = max(1, int(nb * frac)) if eng.cached else nb
-    rng = (0, sample_b) if eng.cached else (-1, -1)
-    for _ in range(max(0, warmup - 1)):
-        eng.evaluate(D, "b3lyp", batch_range=rng)
+    eng.evaluate(D, func, blocked=True)
+    per_chunk = (time.perf_counter() - t0) / k
+    want = max(1, int(budget_s / ((warmup + steps) * per_chunk)))
+    if want > k:
+        stride = max(1, n_chunks // want)
+        eng, k = sample(stride)
+    for _ in range(warmup):
+        eng.evaluate(D, func, blocked=True)
     ts = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        eng.evaluate(D, "b3lyp", batch_range=rng)
+        eng.evaluate(D, func, blocked=True)
         ts.append(time.perf_counter() - t0)
-    scale = nb / sample_b if eng.cached else 1.0
+    scale = n_chunks / k
     ms = statistics.mean(ts) * 1e3 * scale
-    path = "cached-AO BLAS-3 RksVxcEngine::evaluate" if eng.cached else "per-point evaluate_vxc_rks"
-    sample = (f"{path} restated in C++ (oracle), {steps} timed builds over batches [0, {sample_b}) of {nb} "
-              f"({len(og)} points), scaled by {scale:.3f} to a full build")
-    return ms, threads, sample, e_full, n_full
+    desc = (f"CalChem RksVxcEngine::evaluate cached-AO path restated in C++ (oracle), both contractions by a "
+            f"register-blocked FMA GEMM, {threads} threads; {steps} timed builds over every {stride}-th of "
+            f"CalChem's {n_chunks} 128-point chunks of the Fine grid ({k} chunks, {len(fine_xyzw)} points in "
+            f"all), scaled by {scale:.2f} to a full build")
+    return ms, threads, desc
 
 
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    mol, basis, D = build_inputs()
-    ms, threads, sample, _, _ = cpu_reference_run(basis, mol, D, args.steps, args.warmup)
+    name = getattr(args, "workload", "water61_b3lyp")
+    if name not in RKS_WORKLOADS:
+        name = "water61_b3lyp"
+    ms, threads, sample = cpu_reference_run(name, args.steps, args.warmup, budget_s=60.0)
     line = {"metric": METRIC, "value": round(ms, 4), "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "path": "CPU, all host threads"},
+            "config": {"workload": RKS_WORKLOADS[name][3], "name": name,
+                       "path": "CPU, all host threads, Fine grid, CalChem's batching"},
             "cpu_baseline": {"value": round(ms, 4), "unit": "ms", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(ms, 4), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -246,8 +287,8 @@ def run_reference(args):
 
 
 class _Work:
-    """One benchmark workload: the GPU objects, device buffers and the three ways to run one build
-    (device step, host-buffer step, FP64 plain comparison)."""
+    """One benchmark workload: the GPU objects, device buffers and the ways to run one step (device
+    step, host-buffer step, FP64 plain comparison)."""
 
     def __init__(self, name, torch, dev, prec_name, grid_kind="fine"):
         from calchem_gb300 import (BasisSet, GridLevel, MolecularGrid, RksVxcEngine, UksVxcEngine, VxcGroup,
@@ -259,25 +300,34 @@ class _Work:
         self.prec = 1 if prec_name == "mixed" else 0
         self.prec_name = prec_name
         self.graph = False
+        self.lg = None       # learned grid with its resident judge
+        self.judge = None
         # the FP64-plain comparison: CalChem's batching (chunks of consecutive points) on the Fine grid
         self.plain = None
         self.grid_info = {"grid": "Fine"}
-        if name == "octane_b3lyp":
-            mol, basis, D = build_inputs()
+        self.fine_xyzw = None
+        if name in RKS_WORKLOADS:
+            mol, basis, D = build_inputs(name)
+            _, _, self.func, self.description = rks_molecule(name)
             grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
-            self.kind, self.func, self.xc = "rks", "b3lyp", 3
+            self.fine_xyzw = grid.xyzw
+            self.kind, self.xc = "rks", 3
             self.mats = [D]
-            self.description = WORKLOAD
             self.mol, self.basis = mol, basis
             if grid_kind == "learned":
                 t0 = time.perf_counter()
                 lg = pruner.LearnedGrid(mol, basis, tol=PRUNE_TOL)
                 picked = lg.levels.copy()
-                reverted, _ = lg.check(D, self.func)
+                reverted, _ = lg.check(D, self.func, precision=prec_name)
+                self.lg = lg
+                self.judge = lg.judge_engines()
                 self.grid_info = {"grid": f"MLP-pruned (per-atom tolerance {lg.tol_atom:.2e}, molecule {PRUNE_TOL:g}), "
-                                          f"Fine-grid judge on this density",
+                                          f"Fine-grid judge every {JUDGE_EVERY} iterations (timed, amortised into "
+                                          f"value and e2e)",
                                   "grid_points_fine": len(grid), "grid_points_pruned": len(lg.grid),
+                                  "atoms_pruned": int(len(lg.pruned_atoms())),
                                   "atoms_reverted_by_judge": len(reverted),
+                                  "judge_points": int(lg.judge_points()), "judge_every": JUDGE_EVERY,
                                   "levels_picked": np.bincount(picked, minlength=len(pruner.LEVELS)).tolist(),
                                   "pruner_setup_s": round(time.perf_counter() - t0, 3)}
                 grid_fine = grid
@@ -334,6 +384,10 @@ class _Work:
         self.dP = [torch.from_numpy(p).to(dev) for p in self.packed]
         self.dV = [torch.zeros(nn, dtype=torch.float64, device=dev) for _ in self.packed]
         self.dres = torch.zeros(3 * self.n_mols + 1, dtype=torch.float64, device=dev)
+        if self.judge is not None:
+            n_at = len(self.mol.atoms)
+            self.djudge_res = torch.zeros(4, dtype=torch.float64, device=dev)
+            self.djudge_atoms = torch.zeros(4 * n_at, dtype=torch.float64, device=dev)
 
     @property
     def gid(self):
@@ -372,6 +426,21 @@ class _Work:
                                                        self.dres.data_ptr(), self.dV[0].data_ptr(),
                                                        stream.cuda_stream)
 
+    def judge_step(self, stream):
+        """The periodic full-grid check on the device: per-atom shares of the pruned atoms on their
+        Fine points and on their pruned points (resident uploads, D already on the device)."""
+        n_at = len(self.mol.atoms)
+        for k, eng in enumerate(self.judge):
+            rc = eng.enqueue(self.dP[0].data_ptr(), self.djudge_res.data_ptr() + 16 * k,
+                             self.djudge_atoms.data_ptr() + 16 * n_at * k, stream.cuda_stream, self.func,
+                             self.prec_name)
+            if rc:
+                return rc
+        return 0
+
+    def judge_launches(self):
+        return sum(self.lib.calchem_xc_last_launch_count(e.grid_id) for e in self.judge) if self.judge else 0
+
     def host_step(self, prec=None, plain=False):
         """The reference-facing host-buffer call (copies inside); returns (exc[], nelec[], [V...])."""
         from calchem_gb300 import _native
@@ -391,14 +460,25 @@ class _Work:
             gid, self.xc, prec, _native.ptr(self.packed[0]), _native.ptr(exc), _native.ptr(ne), _native.ptr(V)))
         return exc, ne, [V]
 
+    def host_judge(self):
+        """The judge through the host-buffer call (D in, per-atom shares out), as the SCF loop runs it."""
+        return [e.shares(self.mats[0], self.func, self.prec_name) for e in self.judge]
+
     def io_bytes(self):
         k = len(self.packed)
         return k * self.nn * 8, k * self.nn * 8 + (3 if self.kind == "uks" else 2) * 8 * self.n_mols
+
+    def judge_io_bytes(self):
+        """Per judge: D in, two (Exc, Nelec) and the per-atom shares out, for each of the two uploads."""
+        n_at = len(self.mol.atoms)
+        return 2 * self.nn * 8, 2 * (2 * 8 + 2 * n_at * 8)
 
     def close(self):
         self.obj.close()
         if self.plain is not None:
             self.plain.close()
+        if self.lg is not None:
+            self.lg.close()
 
 
 def run_ours(args):
@@ -416,7 +496,7 @@ def run_ours(args):
         dist = None
     dev = torch.device("cuda", torch.cuda.current_device())
     prec_name = "mixed" if args.precision == "auto" else args.precision
-    W = _Work(args.workload, torch, dev, prec_name, args.grid)
+    W = _Work(args.workload, torch, dev, prec_name, args.grid if args.workload in RKS_WORKLOADS else "fine")
     lib = W.lib
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -428,11 +508,17 @@ def run_ours(args):
     first_ms = (time.perf_counter() - t_first) * 1e3
     W.capture()
     torch.cuda.synchronize()
+    judged = W.judge is not None
 
-    for _ in range(max(3, args.warmup)):
+    def step(i, direct=False):
+        _native.check("evaluate", W.device_step(stream, direct=direct))
+        if judged and i % JUDGE_EVERY == JUDGE_EVERY - 1:
+            _native.check("judge", W.judge_step(stream))
+
+    for i in range(max(3, args.warmup)):
         with torch.cuda.stream(stream):
             flush.zero_()
-        _native.check("evaluate", W.device_step(stream))
+        step(i)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -443,20 +529,18 @@ def run_ours(args):
     step_ms, kern_ms = [], []
     launches = 0
     t_wall0 = time.perf_counter()
-    for _ in range(args.steps):
+    for i in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record(stream)
-        _native.check("evaluate", W.device_step(stream))
+        step(i)
         e.record(stream)
         e.synchronize()
         step_ms.append(s.elapsed_time(e))
-        if not W.graph:
-            km = np.zeros(1, np.float32)
-            _native.check("last_kernel_ms", lib.calchem_xc_last_kernel_ms(W.gid, _native.ptr(km)))
-            kern_ms.append(float(km[0]))
         launches += lib.calchem_xc_last_launch_count(W.gid)
+        if judged and i % JUDGE_EVERY == JUDGE_EVERY - 1:
+            launches += W.judge_launches()
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall0
     if dist:
@@ -466,17 +550,28 @@ def run_ours(args):
     _native.check("device status", lib.calchem_xc_last_status(W.gid))
     res_dev = W.dres.cpu().numpy()
     ms = statistics.mean(step_ms)
-    if not kern_ms:  # graph replays: time the kernel outside the graph
-        for _ in range(3):
+    # the build alone and the judge alone, each on the device (the judge's time is that of one check)
+    build_ms, judge_ms = [], []
+    for _ in range(5):
+        for which in ("build", "judge") if judged else ("build",):
             with torch.cuda.stream(stream):
                 flush.zero_()
-            _native.check("evaluate", W.device_step(stream, direct=True))
-            km = np.zeros(1, np.float32)
-            _native.check("last_kernel_ms", lib.calchem_xc_last_kernel_ms(W.gid, _native.ptr(km)))
-            kern_ms.append(float(km[0]))
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            _native.check(which, W.device_step(stream) if which == "build" else W.judge_step(stream))
+            e.record(stream)
+            e.synchronize()
+            (build_ms if which == "build" else judge_ms).append(s.elapsed_time(e))
+    for _ in range(3):  # graph replays: time the quadrature kernel outside the graph
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        _native.check("evaluate", W.device_step(stream, direct=True))
+        km = np.zeros(1, np.float32)
+        _native.check("last_kernel_ms", lib.calchem_xc_last_kernel_ms(W.gid, _native.ptr(km)))
+        kern_ms.append(float(km[0]))
     kms = statistics.mean(kern_ms)
     ms = max_over_ranks(dist, ms, dev)
-    # ---- e2e through the host-buffer C ABI call (copies inside the timed region)
+    # ---- e2e through the host-buffer C ABI calls (copies inside the timed region)
     e2e = []
     host = None
     for i in range(args.warmup + args.steps):
@@ -485,6 +580,8 @@ def run_ours(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         host = W.host_step()
+        if judged and i % JUDGE_EVERY == JUDGE_EVERY - 1:
+            W.host_judge()
         if i >= args.warmup:
             e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = statistics.mean(e2e)
@@ -493,7 +590,7 @@ def run_ours(args):
     if W.plain is not None:
         ef, nf, Vf = W.host_step(prec=0, plain=True)
 
-        def timed(step, reps=3):
+        def timed(fn, reps=3):
             ts = []
             for _ in range(reps):
                 with torch.cuda.stream(stream):
@@ -501,32 +598,32 @@ def run_ours(args):
                 torch.cuda.synchronize()
                 s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 s.record(stream)
-                _native.check("evaluate", step())
+                _native.check("evaluate", fn())
                 e.record(stream)
                 e.synchronize()
                 ts.append(s.elapsed_time(e))
             return statistics.mean(ts)
 
-        fts = [timed(lambda: W.device_step(stream, prec=0, plain=True))]
+        fts = timed(lambda: W.device_step(stream, prec=0, plain=True))
         # the gains one at a time: FP64 on the timed build's own grid and batches, and (learned grid)
         # the timed precision on the Fine grid with CalChem's batching
         W.grid_info["fp64_same_plan_ms"] = round(timed(lambda: W.device_step(stream, prec=0)), 4)
-        if "grid_points_pruned" in W.grid_info:
+        if judged:
             W.grid_info["mixed_on_fine_grid_reference_batching_ms"] = round(timed(
                 lambda: W.device_step(stream, prec=W.prec, plain=True)), 4)
         dexc = host[0] - ef
-        ref_fp64 = {"fp64_plain_ms": round(statistics.mean(fts), 4),
-                    "speedup_vs_fp64_plain": round(statistics.mean(fts) / ms, 3),
+        ref_fp64 = {"fp64_plain_ms": round(fts, 4),
+                    "speedup_vs_fp64_plain": round(fts / ms, 3),
                     "dExc_vs_fp64": float(dexc[np.argmax(np.abs(dexc))]),
                     "dNelec_vs_fp64": float(np.max(np.abs(host[1] - nf))),
                     "max_abs_dV_vs_fp64": float(max(np.max(np.abs(a - b)) for a, b in zip(host[2], Vf)))}
         if W.n_mols > 1:
             ref_fp64["dExc_vs_fp64_is"] = "largest |dExc| over the molecules"
     if W.prec == 1:
-        # the AO cache (per-batch AO values, gradients and packed operand, kept across evaluations as
-        # CalChem's engine keeps its AO cache across SCF iterations): its size, the first build
-        # (which fills it) and a build with it off
+        # the AO cache: its size, the first build (which fills it) and a build with it off
         W.grid_info["ao_cache_bytes"] = W.obj.ao_cache_bytes()
+        if judged:
+            W.grid_info["judge_ao_cache_bytes"] = int(sum(j.ao_cache_bytes() for j in W.judge))
         W.grid_info["first_build_wall_ms"] = round(first_ms, 4)  # host call: workspace and cache allocation, fill
         W.obj.set_ao_cache(False)
         nts = []
@@ -547,14 +644,16 @@ def run_ours(args):
     else:
         tc_peak = fp64_peak_tflops(torch, dev)
         peak_note = "FP64 pipe: cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in the measured peaks)"
-    # the committed captures are of the default (learned-grid) headline build
-    traffic = NCU_TRAFFIC_BYTES.get(prec_name) if (W.name == "octane_b3lyp" and
-                                                   "grid_points_pruned" in W.grid_info) else None
+    traffic = NCU_TRAFFIC_BYTES.get((W.name, prec_name)) if judged else None
     nspin = 2 if W.kind == "uks" else 1
     # algorithmic bytes per build: D_sub gathered and V_sub scattered per batch and spin (8 B each per
     # AO pair), the points (x, y, z, w), and D in and V out once
     bytes_alg = nspin * 16.0 * W.sum_m2 + 32.0 * W.n_points + nspin * 16.0 * W.nn
     h2d, d2h = W.io_bytes()
+    if judged:
+        jh, jd = W.judge_io_bytes()
+        h2d += jh / JUDGE_EVERY
+        d2h += jd / JUDGE_EVERY
     line = {
         "metric": METRIC, "value": round(ms, 4), "unit": "ms", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
@@ -564,23 +663,26 @@ def run_ours(args):
         "config": {"workload": W.description, "name": W.name, "precision": prec_name, **W.grid_info, "n_ao": W.n_ao(),
                    "molecules": W.n_mols, "grid_points": W.n_points, "batches": W.n_batches, "max_m": W.max_m,
                    "l2": "flushed before every timed step (256 MiB write)",
-                   "graph": "CUDA-graph replay per step" if W.graph else "direct launches",
+                   "graph": "CUDA-graph replay of the build per step" if W.graph else "direct launches",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
-        "grid_points_per_s": round(W.n_points / (ms * 1e-3), 1),
+        "build_ms": round(statistics.mean(build_ms), 4),
+        "grid_points_per_s": round(W.n_points / (statistics.mean(build_ms) * 1e-3), 1),
         "median_ms_per_step": round(statistics.median(step_ms), 4),
         "exc": float(res_dev[0]), "nelec": float(res_dev[1]),
         "roofline": roofline(W.flops, bytes_alg, kms, tc_peak, peak_note, traffic, "vxc quadrature kernel",
                              f"{'8' if W.kind == 'uks' else '4'}*sum(m^2 n) = {W.flops:.4e} flop; "
                              f"{16 * nspin}*sum(m^2) + 32 N + {16 * nspin} n^2 = {bytes_alg:.4e} B per launch"),
-        "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches,
         "wall_s_timed": round(t_wall, 3),
         "clocks": clk,
     }
+    if judged:
+        line["judge_ms"] = round(statistics.mean(judge_ms), 4)
+        line["judge_ms_per_iteration"] = round(statistics.mean(judge_ms) / JUDGE_EVERY, 4)
     line.update(ref_fp64)
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline and W.name == "octane_b3lyp":
-        D = W.mats[0]
-        cms, threads, sample, _, _ = cpu_reference_run(W.basis, W.mol, D, 3, 1, budget_s=25.0)
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline and W.name in RKS_WORKLOADS:
+        cms, threads, sample = cpu_reference_run(W.name, 3, 1, budget_s=20.0, fine_xyzw=W.fine_xyzw)
         line["cpu_baseline"] = {"value": round(cms, 3), "unit": "ms", "cores": threads, "kind": "port",
                                 "sample": sample}
     if rank == 0:
@@ -624,7 +726,7 @@ def run_gradient(args):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     prec = "fp64" if args.precision == "fp64" else "mixed"
-    mol, basis, D = build_inputs()
+    mol, basis, D = build_inputs("octane_b3lyp")
     grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
     eng = RksVxcEngine(basis, grid)
     eng.set_profiling(True)
@@ -673,7 +775,7 @@ def run_gradient(args):
         "vs_baseline": None,
         "dtype": "f64" if prec == "fp64" else "bf16x4 fixed-point split contractions, df32 AO/forces/weights, f64 functional",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD + "; XC nuclear gradient at P_alpha = D / 2", "name": args.workload,
+        "config": {"workload": RKS_WORKLOADS["octane_b3lyp"][3] + "; XC nuclear gradient at P_alpha = D / 2", "name": args.workload,
                    "precision": prec, "grid_points": len(grid), "batches": n_batches, "max_m": max_m,
                    "atoms": len(mol.z), "l2": "flushed before every timed step (256 MiB write)"},
         "roofline": roofline(flops, bytes_alg, kms, tc_peak, peak_note, None, "gradient kernels + split + reduce",
@@ -714,7 +816,7 @@ def run_fxc(args):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     prec = "fp64" if args.precision == "fp64" else "mixed"
-    mol, basis, D = build_inputs()
+    mol, basis, D = build_inputs("octane_b3lyp")
     grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
     ker = FxcKernel(basis, grid, "b3lyp", D, precision=prec)
     rng = np.random.default_rng(SEED)
@@ -746,7 +848,7 @@ def run_fxc(args):
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "bf16x4 fixed-point / bf16x3 split contractions",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD + f"; TD-DFT kernel contraction of {FXC_TRIALS} seeded symmetric trial "
+        "config": {"workload": RKS_WORKLOADS["octane_b3lyp"][3] + f"; TD-DFT kernel contraction of {FXC_TRIALS} seeded symmetric trial "
                                           "matrices (singlet) at the ground-state density",
                    "name": args.workload, "precision": prec, "grid_points": len(grid), "trials": FXC_TRIALS,
                    "l2": "flushed before every timed step (256 MiB write)", "timing": "host wall clock of the "

@@ -92,6 +92,11 @@ struct Entry {
   long long* d_ao_cache_off = nullptr;
   int* d_ao_cache_ok = nullptr;
   size_t ao_cache_bytes = 0;
+  // per-atom share sums (calchem_xc_set_point_atoms): planned point indices grouped by host atom
+  int n_share_atoms = 0;
+  int* d_atom_pts = nullptr;
+  int* d_atom_off = nullptr;
+  double* d_atom_out = nullptr;     // 2 per atom (host-buffer calls)
   std::vector<int> h_host;          // host atom of every uploaded point (reference-layout uploads)
   std::vector<int> h_orig;          // caller's index of every uploaded point (empty: identity)
   int n_orig = 0;                   // points the caller passed (calchem_xc_upload_points*)
@@ -100,7 +105,8 @@ struct Entry {
     void* ptrs[] = {d_shells, d_prims, d_comps, d_prim_f, d_comp_f, d_shell_cf, d_pts,  d_batches, d_cand,  d_cand_loc, d_bao,   d_order,
                     d_P,      d_Pb,    d_V,     d_Vb,   d_rg,      d_red,   d_res,      d_counter, d_slab,
                     d_mixed_ws, d_mixed_slab, d_mol_n, d_mol_off, d_mol_ao_off, d_mol_boff, d_pt_out,
-                    d_fxc, d_fxc_m, d_fxc_v, d_ao_cache, d_ao_cache_off, d_ao_cache_ok};
+                    d_fxc, d_fxc_m, d_fxc_v, d_ao_cache, d_ao_cache_off, d_ao_cache_ok, d_atom_pts, d_atom_off,
+                    d_atom_out};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (graph) cudaGraphExecDestroy(graph);
@@ -486,12 +492,14 @@ void ao_cache_decide(Entry& e) {
   e.ao_cache_state = 2;
 }
 
+// shares_only (closed shell, with point_out): the per-point shares, Exc and Nelec without the Vxc
+// contraction; Va is not touched.
 int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, const double* Pb, double* Va,
                  double* Vb, const double* wv, double* rho_out, double* result, cudaStream_t st,
-                 double* point_out = nullptr) {
+                 double* point_out = nullptr, bool shares_only = false) {
   const size_t nn = (size_t)e.nn_total;
   int launches = 0;
-  if (mode != kModeRho) {
+  if (mode != kModeRho && !shares_only) {
     if (cudaMemsetAsync(Va, 0, nn * sizeof(double), st) != cudaSuccess) return -5;
     if (mode == kModeUks && cudaMemsetAsync(Vb, 0, nn * sizeof(double), st) != cudaSuccess) return -5;
   }
@@ -509,6 +517,7 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
   A.counter = e.d_counter;
   A.max_m = e.max_m;
   A.point_out = point_out;
+  A.shares_only = shares_only ? 1 : 0;
   const DevGrid G = dev_grid(e);
   cudaError_t err;
   const bool prof = e.profiling && e.ev0 && e.ev1;
@@ -553,8 +562,11 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
         cudaSuccess)
       return -5;
     const int from_upper = precision == CALCHEM_XC_MIXED ? 1 : 0;
-    if (launch_mirror(Va, e.max_n, e.d_mol_n, e.d_mol_off, e.n_mols, from_upper, st) != cudaSuccess) return -5;
-    launches += 2;
+    ++launches;
+    if (!shares_only) {
+      if (launch_mirror(Va, e.max_n, e.d_mol_n, e.d_mol_off, e.n_mols, from_upper, st) != cudaSuccess) return -5;
+      ++launches;
+    }
     if (mode == kModeUks) {
       if (launch_mirror(Vb, e.max_n, e.d_mol_n, e.d_mol_off, e.n_mols, from_upper, st) != cudaSuccess) return -5;
       ++launches;
@@ -1383,6 +1395,102 @@ int calchem_xc_evaluate_uks_device(uint64_t grid_id, int xc_code, int precision,
   if (int rc0 = ensure_ws(*e)) return rc0;
   return enqueue_eval(*e, kModeUks, xc_code, precision, d_pa, d_pb, d_va, d_vb, nullptr, nullptr, d_result,
                       (cudaStream_t)stream);
+}
+
+int calchem_xc_set_point_atoms(uint64_t grid_id, const int* h_host_atom, int n_points, int n_atoms) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_host_atom || n_points <= 0 || n_atoms <= 0) return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e || e->n_mols != 1) return -2;
+  const int n_caller = e->h_orig.empty() ? e->n_pts : e->n_orig;
+  if (n_points != n_caller) return -2;
+  for (int k = 0; k < n_points; ++k)
+    if (h_host_atom[k] < 0 || h_host_atom[k] >= n_atoms) return -1;
+  // planned point k came from the caller's point h_orig[k] (identity without a plan); counting sort
+  // by atom keeps the planned order within each atom
+  std::vector<int> off(n_atoms + 1, 0), pts(e->n_pts);
+  auto atom_of = [&](int k) { return h_host_atom[e->h_orig.empty() ? k : e->h_orig[k]]; };
+  for (int k = 0; k < e->n_pts; ++k) ++off[atom_of(k) + 1];
+  for (int a = 0; a < n_atoms; ++a) off[a + 1] += off[a];
+  std::vector<int> fill(off.begin(), off.end() - 1);
+  for (int k = 0; k < e->n_pts; ++k) pts[fill[atom_of(k)]++] = k;
+  for (int* p : {e->d_atom_pts, e->d_atom_off}) if (p) cudaFree(p);
+  if (e->d_atom_out) cudaFree(e->d_atom_out);
+  e->d_atom_pts = e->d_atom_off = nullptr;
+  e->d_atom_out = nullptr;
+  e->n_share_atoms = 0;
+  if (!dalloc(&e->d_atom_pts, pts.size()) || !dalloc(&e->d_atom_off, off.size()) ||
+      !dalloc(&e->d_atom_out, 2 * (size_t)n_atoms)) {
+    cudaGetLastError();
+    return -4;
+  }
+  if (cudaMemcpy(e->d_atom_pts, pts.data(), pts.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(e->d_atom_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+    return -5;
+  e->n_share_atoms = n_atoms;
+  return 0;
+}
+
+namespace {
+// Per-point shares (no Vxc) and their per-atom sums, enqueued on st.
+int enqueue_atom_shares(Entry& e, int xc_code, int precision, const double* d_total, double* d_result,
+                        double* d_atom_out, cudaStream_t st) {
+  if (int rc0 = ensure_ws(e)) return rc0;
+  const size_t np2 = 2 * (size_t)e.n_pts;
+  if (!e.d_pt_out && !dalloc(&e.d_pt_out, np2)) {
+    cudaGetLastError();
+    return -4;
+  }
+  if (cudaMemsetAsync(e.d_pt_out, 0, np2 * sizeof(double), st) != cudaSuccess) return -5;
+  int rc = enqueue_eval(e, kModeRks, xc_code, precision, d_total, nullptr, nullptr, nullptr, nullptr, nullptr,
+                        d_result, st, e.d_pt_out, true);
+  if (rc) return rc;
+  if (launch_atom_shares(e.d_pt_out, e.d_atom_pts, e.d_atom_off, e.n_share_atoms, d_atom_out, st) != cudaSuccess)
+    return -5;
+  e.last_launches += 1;
+  return 0;
+}
+}  // namespace
+
+int calchem_xc_evaluate_rks_atoms(uint64_t grid_id, int xc_code, int precision, const double* h_d_total,
+                                  double* exc_out, double* nelec_out, double* h_atom_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!h_d_total || !exc_out || !nelec_out || !h_atom_out || !valid_xc(xc_code)) return -1;
+  if (!valid_prec(precision, kModeRks)) return -1;
+  if (!device_ok()) return -3;
+  Entry* e = find(grid_id);
+  if (!e || e->n_mols != 1 || e->n_share_atoms <= 0) return -2;
+  if (!e->has_w) return -1;
+  if (int rc0 = ensure_ws(*e)) return rc0;
+  const size_t nn = (size_t)e->nn_total;
+  std::memcpy(e->h_stage, h_d_total, nn * sizeof(double));
+  if (cudaMemcpyAsync(e->d_P, e->h_stage, nn * sizeof(double), cudaMemcpyHostToDevice, e->stream) != cudaSuccess)
+    return -5;
+  int rc = enqueue_atom_shares(*e, xc_code, precision, e->d_P, e->d_res, e->d_atom_out, e->stream);
+  if (rc) return rc;
+  double* h_res = e->h_stage + 2 * nn;
+  int* h_status = reinterpret_cast<int*>(h_res + 4);
+  if (cudaMemcpyAsync(h_res, e->d_res, 2 * sizeof(double), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
+      cudaMemcpyAsync(h_status, e->d_counter + 2, sizeof(int), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
+      cudaMemcpyAsync(h_atom_out, e->d_atom_out, 2 * (size_t)e->n_share_atoms * sizeof(double), cudaMemcpyDeviceToHost,
+                      e->stream) != cudaSuccess ||
+      cudaStreamSynchronize(e->stream) != cudaSuccess)
+    return -5;
+  if (*h_status != 0) return -7;
+  *exc_out = h_res[0];
+  *nelec_out = h_res[1];
+  return 0;
+}
+
+int calchem_xc_evaluate_rks_atoms_device(uint64_t grid_id, int xc_code, int precision, const double* d_total,
+                                         double* d_result, double* d_atom_out, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_total || !d_result || !d_atom_out || !valid_xc(xc_code) || !valid_prec(precision, kModeRks)) return -1;
+  Entry* e = find(grid_id);
+  if (!e || e->n_mols != 1 || e->n_share_atoms <= 0) return -2;
+  if (!e->has_w) return -1;
+  return enqueue_atom_shares(*e, xc_code, precision, d_total, d_result, d_atom_out, (cudaStream_t)stream);
 }
 
 int calchem_xc_fxc_prepare(uint64_t grid_id, int xc_code, const double* h_d_total) {

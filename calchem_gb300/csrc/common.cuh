@@ -84,6 +84,9 @@ struct EvalArgs {
   // point_out[2 g + 1] = w_g (v_rho rho + v_gamma |grad rho|^2), the point's share of Exc and of
   // tr(D Vxc).  Points below the density floor are not written (the caller zeroes the buffer).
   double* point_out;
+  // With point_out in the closed-shell mode: nonzero skips the Vxc contraction (the per-point shares,
+  // Exc and Nelec only; V is neither read nor written).
+  int shares_only;
   // kModeFxc: n_trials matrices at Pa + b n^2, results at Va + b n^2; per-point kernel coefficients
   // fxc_coef[11 g ..] = (g_s x, y, z, singlet k_rr, k_rg, k_gg, u_iso, triplet k_rr, k_rg, k_gg, u_iso).
   int n_trials;

@@ -18,6 +18,9 @@ cudaError_t launch_reduce(const double* part, int n_batches, double* out, int n_
 cudaError_t launch_mirror(double* V, int max_n, const int* mol_n, const long long* mol_off, int n_mols, int from_upper,
                           cudaStream_t st);
 cudaError_t launch_mirror(double* V, int n, int from_upper, cudaStream_t st);
+// Per-atom (Exc, tr(D Vxc)) shares: out[2 a ..] = sums of point_out over atom a's points.
+cudaError_t launch_atom_shares(const double* point_out, const int* atom_pts, const int* atom_off, int n_atoms,
+                               double* out, cudaStream_t st);
 // Tensor-core form (vxc_mixed.cu)
 int mixed_supported(int mode);
 size_t mixed_slab_doubles(int max_m);

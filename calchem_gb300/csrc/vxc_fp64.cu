@@ -395,7 +395,7 @@ __global__ void __launch_bounds__(kThreads, 1) vxc_fp64_kernel(DevGrid G, EvalAr
         A.batch_red[3 * (size_t)b + 2] = nbs;
       }
     }
-    if (A.mode != kModeRho) {
+    if (A.mode != kModeRho && !A.shares_only) {
       build_z(bd, slab, m_pad, 4, S, 0);
       __syncthreads();
       accumulate_v(G, bd, slab, m_pad, 4, A.Va, S);
@@ -442,6 +442,36 @@ __global__ void __launch_bounds__(256) reduce_batches_kernel(const double* __res
     out[0] = s[0][0];
     if (n_out == 2) out[1] = s[1][0] + s[2][0];
     else { out[1] = s[1][0]; out[2] = s[2][0]; }
+  }
+}
+
+// Per-atom sums of the per-point shares (point_out[2 g], point_out[2 g + 1]): one CTA per atom over
+// its points atom_pts[atom_off[a] .. atom_off[a + 1]) (planned point indices, ascending), strided
+// partial sums and a fixed tree, so the result does not depend on scheduling.
+__global__ void __launch_bounds__(256) atom_shares_kernel(const double* __restrict__ point_out,
+                                                          const int* __restrict__ atom_pts,
+                                                          const int* __restrict__ atom_off, double* __restrict__ out) {
+  __shared__ double s[2][256];
+  const int t = threadIdx.x, a = blockIdx.x;
+  double e = 0, v = 0;
+  for (int k = atom_off[a] + t; k < atom_off[a + 1]; k += 256) {
+    const int g = atom_pts[k];
+    e += point_out[2 * (size_t)g];
+    v += point_out[2 * (size_t)g + 1];
+  }
+  s[0][t] = e;
+  s[1][t] = v;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (t < o) {
+      s[0][t] += s[0][t + o];
+      s[1][t] += s[1][t + o];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    out[2 * (size_t)a] = s[0][0];
+    out[2 * (size_t)a + 1] = s[1][0];
   }
 }
 
@@ -500,6 +530,12 @@ cudaError_t launch_mirror(double* V, int max_n, const int* mol_n, const long lon
 
 cudaError_t launch_mirror(double* V, int n, int from_upper, cudaStream_t st) {
   return launch_mirror(V, n, nullptr, nullptr, 1, from_upper, st);
+}
+
+cudaError_t launch_atom_shares(const double* point_out, const int* atom_pts, const int* atom_off, int n_atoms,
+                               double* out, cudaStream_t st) {
+  atom_shares_kernel<<<n_atoms, 256, 0, st>>>(point_out, atom_pts, atom_off, out);
+  return cudaGetLastError();
 }
 
 }  // namespace cxc

@@ -659,6 +659,9 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
         A.batch_red[3 * (size_t)b + 2] = nbs;
       }
     }
+    // per-point shares only: no GEMM2 and no V update (cta_sum's barrier follows the last reads of
+    // the stage and of coef, so the next batch may reuse them)
+    if (A.shares_only) continue;
 
     // (F)+(G) per spin: image tiles Phi^T / Z^T, then lower tile pairs of W.  Rows [m, 128 n_ib) of
     // the tiles are left as they are: a W entry depends on its own row of A and of B only, and the

@@ -334,13 +334,85 @@ def choose_levels(net, mol, tol_atom, margin=0.5) -> np.ndarray:
     return out
 
 
+class ShareEngine:
+    """A resident upload of a set of grid points with their host atoms, evaluated for per-atom shares
+    of Exc and tr(D Vxc) without the Vxc contraction (calchem_xc_set_point_atoms,
+    calchem_xc_evaluate_rks_atoms[_device]).  The points stay on the device, with the tensor-core
+    form's AO cache, across evaluations."""
+
+    def __init__(self, basis, grid, n_atoms):
+        from .vxc import _upload_points
+        lib = _native.load()
+        self.n_atoms = int(n_atoms)
+        self.n_points = len(grid)
+        self.grid_id = _upload_points(basis, grid)
+        host = np.ascontiguousarray(grid.host_atom, dtype=np.int32)
+        _native.check("calchem_xc_set_point_atoms",
+                      lib.calchem_xc_set_point_atoms(self.grid_id, _native.ptr(host), len(host), self.n_atoms))
+
+    def shares(self, D, func, precision="mixed"):
+        """(E_A, T_A) per atom from a host density."""
+        from .vxc import _xc_code, _PRECISION
+        lib = _native.load()
+        P = np.ascontiguousarray(D, dtype=np.float64)
+        out = np.zeros(2 * self.n_atoms)
+        exc, ne = np.zeros(1), np.zeros(1)
+        _native.check("calchem_xc_evaluate_rks_atoms", lib.calchem_xc_evaluate_rks_atoms(
+            self.grid_id, _xc_code(func), _PRECISION[precision], _native.ptr(P), _native.ptr(exc), _native.ptr(ne),
+            _native.ptr(out)))
+        return out[0::2].copy(), out[1::2].copy()
+
+    def enqueue(self, d_total, d_result, d_atom_out, stream, func, precision="mixed"):
+        """Device-buffer form (addresses; d_atom_out holds 2 n_atoms doubles), enqueued on stream."""
+        from .vxc import _xc_code, _PRECISION
+        return _native.load().calchem_xc_evaluate_rks_atoms_device(
+            self.grid_id, _xc_code(func), _PRECISION[precision], d_total, d_result, d_atom_out, stream)
+
+    def set_profiling(self, enable=True):
+        _native.check("calchem_xc_set_profiling", _native.load().calchem_xc_set_profiling(self.grid_id, int(enable)))
+
+    def ao_cache_bytes(self) -> int:
+        import ctypes
+        out = (ctypes.c_size_t * 1)()
+        _native.check("calchem_xc_set_ao_cache", _native.load().calchem_xc_set_ao_cache(self.grid_id, -1, out))
+        return int(out[0])
+
+    def last_kernel_ms(self):
+        import ctypes
+        ms = (ctypes.c_float * 1)()
+        _native.check("calchem_xc_last_kernel_ms", _native.load().calchem_xc_last_kernel_ms(self.grid_id, ms))
+        return float(ms[0])
+
+    def close(self):
+        if self.grid_id:
+            _native.load().calchem_cuda_vxc_release(self.grid_id)
+            self.grid_id = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _subgrid(grid, keep):
+    return MolecularGrid(grid.xyzw[keep], grid.raw_weight[keep], grid.host_atom[keep], grid.level)
+
+
 class LearnedGrid:
     """A molecule's MLP-pruned grid with the Fine grid as fallback and judge.
 
     ``tol`` bounds the total (per molecule) Exc and tr(D Vxc) quadrature error against the Fine grid;
     every atom is held to tol / n_atoms.  ``check(D, func)`` is the periodic full-grid check: it
     compares every atom's shares on the pruned and Fine grids for the density D and reverts the
-    atoms that exceed their tolerance to Fine (rebuilding the grid)."""
+    atoms that exceed their tolerance to Fine (rebuilding the grid).
+
+    Becke partitioning makes an atom's share depend on its own points only, and an atom kept at the
+    Fine level has the same points on both grids, so the judge evaluates just the pruned atoms'
+    points: their Fine points and their pruned points, two resident uploads (``judge_engines``) kept
+    with their AO caches between checks and rebuilt only when an atom reverts.  The shares need no
+    Vxc contraction, and the check runs in the tensor-core form by default (its per-atom share error,
+    ~1e-10 Eh, is far below the per-atom tolerance)."""
 
     def __init__(self, mol, basis, net=None, tol=5e-7, margin=0.5):
         self.mol = mol
@@ -350,6 +422,7 @@ class LearnedGrid:
         self.levels = choose_levels(self.net, mol, self.tol_atom, margin)
         self.grid = grid_for_levels(mol, self.levels)
         self._fine = None
+        self._judge = None
         self.reverted = []
 
     @property
@@ -358,14 +431,50 @@ class LearnedGrid:
             self._fine = grid_for_levels(self.mol, [FINE] * len(self.mol.atoms))
         return self._fine
 
-    def check(self, D, func):
-        """Full-grid check; returns the atoms reverted to Fine (the grid is rebuilt if any)."""
-        E0, T0 = atom_shares(self.mol, self.basis, self.fine_grid, func, D)
-        E, T = atom_shares(self.mol, self.basis, self.grid, func, D)
+    def pruned_atoms(self):
+        return np.nonzero(self.levels != FINE)[0]
+
+    def judge_engines(self):
+        """(Fine-grid points of the pruned atoms, pruned-grid points of the same atoms) as resident
+        ShareEngines; None when no atom is pruned."""
+        atoms = self.pruned_atoms()
+        if len(atoms) == 0:
+            return None
+        if self._judge is None:
+            n = len(self.mol.atoms)
+            fine = _subgrid(self.fine_grid, np.isin(self.fine_grid.host_atom, atoms))
+            pruned = _subgrid(self.grid, np.isin(self.grid.host_atom, atoms))
+            self._judge = (ShareEngine(self.basis, fine, n), ShareEngine(self.basis, pruned, n))
+        return self._judge
+
+    def judge_points(self):
+        """Points the judge evaluates (Fine and pruned uploads together)."""
+        j = self.judge_engines()
+        return 0 if j is None else j[0].n_points + j[1].n_points
+
+    def _close_judge(self):
+        if self._judge is not None:
+            for e in self._judge:
+                e.close()
+            self._judge = None
+
+    def check(self, D, func, precision="mixed"):
+        """Full-grid check; returns (atoms reverted to Fine, per-atom errors).  The grid and the judge
+        uploads are rebuilt if any atom reverts."""
+        n = len(self.mol.atoms)
+        judge = self.judge_engines()
+        if judge is None:
+            return [], np.zeros(n)
+        E0, T0 = judge[0].shares(D, func, precision)
+        E, T = judge[1].shares(D, func, precision)
         err = np.maximum(np.abs(E - E0), np.abs(T - T0))
         bad = [int(a) for a in np.nonzero((err > self.tol_atom) & (self.levels != FINE))[0]]
         if bad:
             self.levels[bad] = FINE
             self.grid = grid_for_levels(self.mol, self.levels)
             self.reverted.extend(bad)
+            self._close_judge()
         return bad, err
+
+    def close(self):
+        self._close_judge()

@@ -25,6 +25,12 @@
 #include <omp.h>
 #endif
 
+namespace orc {
+// cpu_gemm.cpp: the register-blocked FMA product of the timed CPU baseline.
+void gemm_acc(int M, int N, int K, const double* A, long ars, long acs, const double* B, long ldb, double* C,
+              long ldc);
+}  // namespace orc
+
 namespace {
 
 constexpr double kPi = 3.14159265358979323846;          // std::f64::consts::PI
@@ -1437,8 +1443,10 @@ RksEngine* rks_engine_create(const Basis& bs, const std::vector<GridPoint>& pts,
   return eng;
 }
 
+// blocked: the two contractions by the register-blocked FMA product of cpu_gemm.cpp (the timed CPU
+// baseline, as CalChem runs faer's GEMM) instead of the checker's plain loops; same sums, other order.
 void rks_engine_evaluate(const RksEngine& eng, const double* P, int func, int threads, double* exc, double* nelec,
-                         double* V, int batch_begin, int batch_end) {
+                         double* V, int batch_begin, int batch_end, bool blocked) {
   const Basis& bs = *eng.bs;
   const int n = bs.n_ao;
   if (!eng.cached) {
@@ -1462,7 +1470,7 @@ void rks_engine_evaluate(const RksEngine& eng, const double* P, int func, int th
   for (int c = 0; c < nchunks; ++c) {
     std::vector<double>& vl = vloc[c];
     vl.assign((size_t)n * n, 0.0);
-    std::vector<double> psub, t, z, vsub;
+    std::vector<double> psub, t, z, vsub, phit;
     double rho[kBatch], gx[kBatch], gy[kBatch], gz[kBatch], wv[kBatch], ux[kBatch], uy[kBatch], uz[kBatch];
     const int b0 = batch_begin + c * clen, b1 = std::min(batch_end, b0 + clen);
     for (int bi = b0; bi < b1; ++bi) {
@@ -1474,13 +1482,17 @@ void rks_engine_evaluate(const RksEngine& eng, const double* P, int func, int th
         for (int j = 0; j < m; ++j) psub[(size_t)i * m + j] = P[(size_t)cb.ao[i] * n + cb.ao[j]];
       // T = P_sub * Phi (gemm_nn_into, calchem-tensor/src/lib.rs:114-124)
       t.assign((size_t)m * b, 0.0);
-      for (int i = 0; i < m; ++i)
-        for (int k = 0; k < m; ++k) {
-          const double pik = psub[(size_t)i * m + k];
-          const double* prow = &cb.phi[(size_t)k * b];
-          double* trow = &t[(size_t)i * b];
-          for (int g = 0; g < b; ++g) trow[g] += pik * prow[g];
-        }
+      if (blocked) {
+        orc::gemm_acc(m, b, m, psub.data(), m, 1, cb.phi.data(), b, t.data(), b);
+      } else {
+        for (int i = 0; i < m; ++i)
+          for (int k = 0; k < m; ++k) {
+            const double pik = psub[(size_t)i * m + k];
+            const double* prow = &cb.phi[(size_t)k * b];
+            double* trow = &t[(size_t)i * b];
+            for (int g = 0; g < b; ++g) trow[g] += pik * prow[g];
+          }
+      }
       for (int g = 0; g < b; ++g) rho[g] = gx[g] = gy[g] = gz[g] = 0.0;
       for (int i = 0; i < m; ++i)
         for (int g = 0; g < b; ++g) {
@@ -1516,14 +1528,21 @@ void rks_engine_evaluate(const RksEngine& eng, const double* P, int func, int th
         }
       // V_sub = Z * Phi^T (gemm_nt_into, calchem-tensor/src/lib.rs:126-135)
       vsub.assign((size_t)m * m, 0.0);
-      for (int i = 0; i < m; ++i)
-        for (int j = 0; j < m; ++j) {
-          const double* zr = &z[(size_t)i * b];
-          const double* pr = &cb.phi[(size_t)j * b];
-          double s = 0;
-          for (int g = 0; g < b; ++g) s += zr[g] * pr[g];
-          vsub[(size_t)i * m + j] = s;
-        }
+      if (blocked) {
+        phit.resize((size_t)b * m);  // Phi^T, b x m, so that the product streams rows of both operands
+        for (int i = 0; i < m; ++i)
+          for (int g = 0; g < b; ++g) phit[(size_t)g * m + i] = cb.phi[(size_t)i * b + g];
+        orc::gemm_acc(m, m, b, z.data(), b, 1, phit.data(), m, vsub.data(), m);
+      } else {
+        for (int i = 0; i < m; ++i)
+          for (int j = 0; j < m; ++j) {
+            const double* zr = &z[(size_t)i * b];
+            const double* pr = &cb.phi[(size_t)j * b];
+            double s = 0;
+            for (int g = 0; g < b; ++g) s += zr[g] * pr[g];
+            vsub[(size_t)i * m + j] = s;
+          }
+      }
       for (int i = 0; i < m; ++i) {
         double* orow = &vl[(size_t)cb.ao[i] * n];
         for (int j = 0; j <= i; ++j) orow[cb.ao[j]] += vsub[(size_t)i * m + j] + vsub[(size_t)j * m + i];
@@ -1908,9 +1927,9 @@ int orc_rks_engine_is_cached(void* e) { return static_cast<RksEngine*>(e)->cache
 double orc_rks_engine_cache_bytes(void* e) { return static_cast<RksEngine*>(e)->cache_bytes; }
 int orc_rks_engine_n_batches(void* e) { return (int)static_cast<RksEngine*>(e)->batches.size(); }
 void orc_rks_engine_evaluate(void* e, const double* P, int func, int threads, double* exc, double* nelec, double* V,
-                             int batch_begin, int batch_end) {
+                             int batch_begin, int batch_end, int blocked) {
   rks_engine_evaluate(*static_cast<RksEngine*>(e), P, func, threads > 0 ? threads : n_threads(), exc, nelec, V,
-                      batch_begin, batch_end);
+                      batch_begin, batch_end, blocked != 0);
 }
 void orc_rks_engine_free(void* e) { delete static_cast<RksEngine*>(e); }
 

@@ -43,7 +43,7 @@ _SIGS = {
     "orc_rks_engine_is_cached": (_I, [_P]),
     "orc_rks_engine_cache_bytes": (_D, [_P]),
     "orc_rks_engine_n_batches": (_I, [_P]),
-    "orc_rks_engine_evaluate": (None, [_P, _P, _I, _I, _P, _P, _P, _I, _I]),
+    "orc_rks_engine_evaluate": (None, [_P, _P, _I, _I, _P, _P, _P, _I, _I, _I]),
     "orc_rks_engine_free": (None, [_P]),
     "orc_overlap": (None, [_P, _P]),
     "orc_max_threads": (_I, []),
@@ -254,14 +254,16 @@ class RksEngine:
         self.cache_bytes = lib().orc_rks_engine_cache_bytes(self.h)
         self.n_batches = lib().orc_rks_engine_n_batches(self.h)
 
-    def evaluate(self, P, func, threads=0, batch_range=(-1, -1)):
+    def evaluate(self, P, func, threads=0, batch_range=(-1, -1), blocked=False):
+        """blocked: the two contractions by the register-blocked FMA product (cpu_gemm.cpp), as the
+        reference runs them through faer; the default plain loops are the checker's."""
         P = np.ascontiguousarray(P, np.float64)
         n = self.basis.n_ao
         V = np.zeros((n, n))
         e = np.zeros(1)
         ne = np.zeros(1)
         lib().orc_rks_engine_evaluate(self.h, _p(P), xc_code(func), int(threads), _p(e), _p(ne), _p(V),
-                                      int(batch_range[0]), int(batch_range[1]))
+                                      int(batch_range[0]), int(batch_range[1]), int(bool(blocked)))
         return float(e[0]), float(ne[0]), V
 
     def __del__(self):
