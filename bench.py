@@ -336,6 +336,7 @@ class _Work:
                 grid_fine = grid
             self.plain = RksVxcEngine(basis, grid_fine, batching="reference")
             self.obj = RksVxcEngine(basis, grid)
+            self.grid_obj = grid
             self.n_points = len(grid)
         elif name == "c54h18_pbe0_uks":
             mol, basis, func, (Pa, Pb) = workloads.build_workload("c54h18_pbe0_uks", SEED)
@@ -343,6 +344,7 @@ class _Work:
             self.kind, self.func, self.xc = "uks", "pbe0", 5
             self.obj = UksVxcEngine(basis, grid)
             self.plain = UksVxcEngine(basis, grid, batching="reference")
+            self.basis_obj, self.grid_obj = basis, grid
             self.mats = [Pa, Pb]
             self.n_points = len(grid)
             na, nb = mol.n_alpha_beta()
@@ -392,6 +394,29 @@ class _Work:
     @property
     def gid(self):
         return self.obj.grid_id
+
+    def tune(self):
+        """The autotuner's tile choice for this workload (timed on its first tensor-core evaluation,
+        or taken from the cache), applied to the build and the judge uploads before the capture."""
+        from calchem_gb300 import autotune
+        if self.prec != 1:
+            return None
+        if self.kind == "group":
+            self.obj.evaluate_rks(self.func, self.mats)
+            sig = autotune.signature(self.obj._tile_src[0], self.obj._tile_src[1], self.func, "mixed",
+                                     self.obj._tile_src[2])
+        elif self.kind == "uks":
+            self.obj.evaluate(self.basis_obj, self.grid_obj, self.func, *self.mats, precision="mixed")
+            sig = autotune.signature(self.basis_obj, self.grid_obj, self.func, "mixed", "uks")
+        else:
+            self.obj.evaluate(self.basis, self.grid_obj, self.func, self.mats[0], precision="mixed")
+            sig = autotune.signature(self.basis, self.grid_obj, self.func, "mixed", "rks")
+        if self.judge is not None:
+            for j in self.judge:
+                j.set_tile(self.obj.tile)
+        rec = autotune._load().get(sig + "|tile", {})
+        return {"tile_n": self.obj.tile, "ctas_per_sm": 1 if self.obj.tile == 128 else 2,
+                "autotuned": True, "kernel_ms_by_tile": rec.get("ms")}
 
     def n_ao(self):
         return int(np.sqrt(self.nn)) if self.kind != "group" else int(self.obj.sizes.max())
@@ -500,12 +525,15 @@ def run_ours(args):
     lib = W.lib
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    W.enable_profiling()
     torch.cuda.synchronize()
     t_first = time.perf_counter()
     W.host_step()  # allocates the workspace (and fills the AO cache) outside the capture
     torch.cuda.synchronize()
     first_ms = (time.perf_counter() - t_first) * 1e3
+    tile = W.tune()  # the tile is chosen before the capture, which keeps it
+    if tile:
+        W.grid_info["tile"] = tile
+    W.enable_profiling()
     W.capture()
     torch.cuda.synchronize()
     judged = W.judge is not None

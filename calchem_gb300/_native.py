@@ -48,6 +48,8 @@ SIGNATURES = {
     "calchem_xc_plan_stats": (_I, [_U64, _P, _P, _P, _P]),
     "calchem_xc_evaluate_rks": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
     "calchem_xc_evaluate_rks_points": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
+    "calchem_xc_set_tile": (_I, [_U64, _I]),
+    "calchem_xc_get_tile": (_I, [_U64]),
     "calchem_xc_set_point_atoms": (_I, [_U64, _P, _I, _I]),
     "calchem_xc_evaluate_rks_atoms": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
     "calchem_xc_evaluate_rks_atoms_device": (_I, [_U64, _I, _I, _P, _P, _P, _P]),

@@ -72,7 +72,8 @@ struct Entry {
   void* d_mixed_ws = nullptr;  // split copies of the density for the tensor-core path
   size_t mixed_slab_stride = 0;
   double* d_mixed_slab = nullptr;
-  int mixed_ctas = 0;
+  int mixed_ctas = 0;               // tensor-core CTAs the workspace has slabs for
+  int tile_n = 64;                  // tensor-core GEMM1 N chunk (calchem_xc_set_tile)
   double* h_stage = nullptr;  // pinned: 2 n^2 + 4 doubles
   cudaStream_t stream = nullptr;
   int last_launches = 0;
@@ -296,7 +297,7 @@ int upload_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_pri
   const int per_sm = 1;  // FP64 kernel: 202 registers x 256 threads -> one resident CTA per SM
   const int n_ctas = std::max(1, std::min(nb, g_sm_count * per_sm));
   const size_t slab_stride = (size_t)kPlanes * m_pad * kBlockPts;
-  const int mixed_ctas = std::max(1, std::min(nb, g_sm_count * mixed_ctas_per_sm()));
+  const int mixed_ctas = std::max(1, std::min(nb, g_sm_count * mixed_ctas_per_sm(64)));
   const size_t mixed_stride = mixed_slab_doubles(hp.max_m);
   size_t total = 0;
   total += (size_t)n_shells * sizeof(AoShellGpu) + (size_t)n_prims * sizeof(AoPrimGpu) +
@@ -492,6 +493,11 @@ void ao_cache_decide(Entry& e) {
   e.ao_cache_state = 2;
 }
 
+// Tensor-core CTAs to launch for the grid's tile (never more than the workspace has slabs for).
+int mixed_launch_ctas(const Entry& e) {
+  return std::max(1, std::min(e.mixed_ctas, g_sm_count * mixed_ctas_per_sm(e.tile_n)));
+}
+
 // shares_only (closed shell, with point_out): the per-point shares, Exc and Nelec without the Vxc
 // contraction; Va is not touched.
 int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, const double* Pb, double* Va,
@@ -545,8 +551,9 @@ int enqueue_eval(Entry& e, int mode, int xc, int precision, const double* Pa, co
       A.ao_cache_off = e.d_ao_cache_off;
       A.ao_cache_ok = e.d_ao_cache_ok;
     }
+    A.tile_n = e.tile_n;
     if (prof) cudaEventRecord(e.ev0, st);
-    err = launch_mixed(G, A, e.mixed_ctas, st);
+    err = launch_mixed(G, A, mixed_launch_ctas(e), st);
     if (prof) cudaEventRecord(e.ev1, st);
   } else {
     A.slab = e.d_slab;
@@ -637,7 +644,8 @@ int enqueue_fxc_mixed(Entry& e, int triplet, const double* d_m, int n_trials, do
       A.ao_cache_off = e.d_ao_cache_off;
       A.ao_cache_ok = e.d_ao_cache_ok;
     }
-    if (launch_mixed(G, A, e.mixed_ctas, st) != cudaSuccess) return -5;
+    A.tile_n = e.tile_n;
+    if (launch_mixed(G, A, mixed_launch_ctas(e), st) != cudaSuccess) return -5;
     if (launch_mirror(v, e.n_ao, 1, st) != cudaSuccess) return -5;
   }
   e.last_launches = 3 * n_trials;
@@ -1397,6 +1405,21 @@ int calchem_xc_evaluate_uks_device(uint64_t grid_id, int xc_code, int precision,
                       (cudaStream_t)stream);
 }
 
+int calchem_xc_set_tile(uint64_t grid_id, int tile_n) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (tile_n != 64 && tile_n != 128) return -1;
+  Entry* e = find(grid_id);
+  if (!e) return -2;
+  e->tile_n = tile_n;
+  return 0;
+}
+
+int calchem_xc_get_tile(uint64_t grid_id) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Entry* e = find(grid_id);
+  return e ? e->tile_n : -2;
+}
+
 int calchem_xc_set_point_atoms(uint64_t grid_id, const int* h_host_atom, int n_points, int n_atoms) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!h_host_atom || n_points <= 0 || n_atoms <= 0) return -1;
@@ -1671,7 +1694,7 @@ int calchem_xc_group_create(const uint64_t* member_ids, int n_members, uint64_t 
   const int m_pad = (max_m + 63) / 64 * 64;
   g->n_ctas = std::max(1, std::min(g->n_batches, g_sm_count));
   g->slab_stride = (size_t)kPlanes * m_pad * kBlockPts;
-  g->mixed_ctas = std::max(1, std::min(g->n_batches, g_sm_count * mixed_ctas_per_sm()));
+  g->mixed_ctas = std::max(1, std::min(g->n_batches, g_sm_count * mixed_ctas_per_sm(64)));
   g->mixed_slab_stride = mixed_slab_doubles(max_m);
   size_t total = (size_t)n_shells * sizeof(AoShellGpu) + (size_t)n_prims * (sizeof(AoPrimGpu) + sizeof(float4)) +
                  (size_t)n_comps * (sizeof(AoCompGpu) + sizeof(float2)) + (size_t)n_shells * 3 * sizeof(float2) +

@@ -87,6 +87,8 @@ struct EvalArgs {
   // With point_out in the closed-shell mode: nonzero skips the Vxc contraction (the per-point shares,
   // Exc and Nelec only; V is neither read nor written).
   int shares_only;
+  // Tensor-core form: GEMM1 N chunk, 64 (two CTAs per SM) or 128 (one CTA per SM, 512 TMEM columns).
+  int tile_n;
   // kModeFxc: n_trials matrices at Pa + b n^2, results at Va + b n^2; per-point kernel coefficients
   // fxc_coef[11 g ..] = (g_s x, y, z, singlet k_rr, k_rg, k_gg, u_iso, triplet k_rr, k_rg, k_gg, u_iso).
   int n_trials;

@@ -24,7 +24,7 @@ cudaError_t launch_atom_shares(const double* point_out, const int* atom_pts, con
 // Tensor-core form (vxc_mixed.cu)
 int mixed_supported(int mode);
 size_t mixed_slab_doubles(int max_m);
-int mixed_ctas_per_sm();
+int mixed_ctas_per_sm(int tile_n);
 int mixed_max_m();
 cudaError_t launch_closed_shell_points(int xc, int precision, int n, const double* rho, const double* gam,
                                        double* out, cudaStream_t st);

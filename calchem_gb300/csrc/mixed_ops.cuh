@@ -65,13 +65,15 @@ __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint4 v) {
                : "memory");
 }
 
-// GEMM1 B operand for K block kb and N chunk [nc, nc + 64): D[nu][mu] 2^-f_nu pieces hi / mid / lo
-// / lo2 at stage + 64 KB + q * 8 KB (64 rows x 64 K, 128-byte swizzle), gathered from the packed
+// GEMM1 B operand for K block kb and N chunk [nc, nc + N): D[nu][mu] 2^-f_nu pieces hi / mid / lo
+// / lo2 at stage + 64 KB + q * N * 128 (N rows x 64 K, 128-byte swizzle), gathered from the packed
 // fixed-point density (x = hi | mid << 16, y = lo | lo2 << 16).
+template <int N = kNc>
 static __device__ void gather_b(unsigned char* stage, const uint2* __restrict__ Dp, const int* s_ao, int n, int m, int kb,
                          int nc) {
+  constexpr uint32_t kPiece = N * 128;
   const uint32_t sbase = smem_addr(stage) + 65536;
-  for (int e = threadIdx.x; e < kNc * 8; e += kThreads) {
+  for (int e = threadIdx.x; e < N * 8; e += kThreads) {
     const int c = e & 7, r = e >> 3;
     const int nu = nc + r;
     const int mu0 = kb * 64 + c * 8;
@@ -90,9 +92,9 @@ static __device__ void gather_b(unsigned char* stage, const uint2* __restrict__ 
     }
     const uint32_t off = sw128(r, c);
     st_shared_v4(sbase + off, make_uint4(hw[0], hw[1], hw[2], hw[3]));
-    st_shared_v4(sbase + 8192 + off, make_uint4(mw[0], mw[1], mw[2], mw[3]));
-    st_shared_v4(sbase + 16384 + off, make_uint4(lw[0], lw[1], lw[2], lw[3]));
-    st_shared_v4(sbase + 24576 + off, make_uint4(qw[0], qw[1], qw[2], qw[3]));
+    st_shared_v4(sbase + kPiece + off, make_uint4(mw[0], mw[1], mw[2], mw[3]));
+    st_shared_v4(sbase + 2 * kPiece + off, make_uint4(lw[0], lw[1], lw[2], lw[3]));
+    st_shared_v4(sbase + 3 * kPiece + off, make_uint4(qw[0], qw[1], qw[2], qw[3]));
   }
 }
 

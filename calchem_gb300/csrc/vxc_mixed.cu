@@ -59,24 +59,38 @@ constexpr int kMT = kThreads;         // threads per CTA (two CTAs per SM)
 constexpr int kGroups = kMT / 128;    // thread groups of 128 (one thread per point in each)
 constexpr int kMaxMixedM = 2048;      // AOs per batch held in shared memory
 constexpr uint32_t kWaitLimit = 1u << 26;
-constexpr uint32_t kTmemCols = 256;
 constexpr int kRing = 4;              // epilogue bulk-copy buffers in the stage
 constexpr int kRingBytes = 24576;     // one 8-row step: 4 x 4 KB FP32 + 4 x 2 KB BF16
-constexpr int kStageBytes = 98304;    // operand staging area: GEMM1 A 64 KB + B 32 KB; GEMM2 6 x 16 KB
-constexpr int kOffCoef = kStageBytes;                    // float [8][128]
-constexpr int kOffAo = kOffCoef + 8 * 128 * 4;           // int [kMaxMixedM]
-constexpr int kOffRed = kOffAo + kMaxMixedM * 4;         // double [3][kMT / 32]
-constexpr int kOffEg = kOffRed + 3 * (kMT / 32) * 8;     // int [128]: per-point power-of-two scale
-constexpr int kOffTab = kOffEg + 128 * 4;                // df32 [64]: 2^(-j/64)
-constexpr int kOffFx = kOffTab + 64 * 8;                 // int [kNc]: row exponents of the chunk's AOs
-constexpr int kOffMisc = kOffFx + kNc * 4;               // mbarriers, tmem slot, batch
-constexpr int kSmemBytes = kOffMisc + 96 + 1024;         // + alignment slack
+constexpr int kMaxTileN = 128;        // largest GEMM1 N chunk
+
+// Shared-memory and TMEM layout of the kernel for GEMM1 N chunk kN (AOs per TMEM accumulator):
+//   kN = 64:  256 TMEM columns (hh, hm+mh, the 2^-16/2^-24 class, running sum: 64 each) and a 96 KB
+//             operand stage (GEMM1 A 64 KB + B 32 KB), so that two CTAs share an SM;
+//   kN = 128: all 512 TMEM columns of the SM and a 128 KB stage (A 64 KB + B 64 KB), one CTA per SM:
+//             half the GEMM1 rounds and half the reloads of the A operand per batch.
+// GEMM2 needs 6 x 16 KB of the stage and 256 TMEM columns in both.
+template <int kN>
+struct MixCfg {
+  static_assert(kN == 64 || kN == 128, "GEMM1 N chunk of 64 or 128 AOs");
+  static constexpr uint32_t kTmemCols = 4 * kN;
+  static constexpr int kCtas = kN == 64 ? 2 : 1;                // resident CTAs per SM
+  static constexpr int kStageBytes = 65536 + kN * 512;          // GEMM1 A 64 KB + B kN x 64 x 4 pieces
+  static constexpr int kOffCoef = kStageBytes;                  // float [8][128]
+  static constexpr int kOffAo = kOffCoef + 8 * 128 * 4;         // int [kMaxMixedM]
+  static constexpr int kOffRed = kOffAo + kMaxMixedM * 4;       // double [3][kMT / 32]
+  static constexpr int kOffEg = kOffRed + 3 * (kMT / 32) * 8;   // int [128]: per-point power-of-two scale
+  static constexpr int kOffTab = kOffEg + 128 * 4;              // df32 [64]: 2^(-j/64)
+  static constexpr int kOffFx = kOffTab + 64 * 8;               // int [kN]: row exponents of the chunk's AOs
+  static constexpr int kOffMisc = kOffFx + kMaxTileN * 4;       // mbarriers, tmem slot, batch
+  static constexpr int kSmemBytes = kOffMisc + 96 + 1024;       // + alignment slack
+  static_assert(kRing * kRingBytes <= kStageBytes, "the epilogue ring lives in the stage");
+  static_assert(6 * 16384 <= kStageBytes, "GEMM2's six image tiles live in the stage");
+  static_assert(kCtas * (kSmemBytes + 1024) <= 233472, "the resident CTAs must fit in one SM's shared memory");
+};
 // dens [kGroups][4][128] doubles (8 KB) lives in the stage at +64 KB while the stage is idle
 constexpr int kOffDensInStage = 65536;
-static_assert(kRing * kRingBytes <= kStageBytes, "the epilogue ring lives in the stage");
 static_assert(24 + 8 * kRing + 8 <= 64, "misc area holds the barriers, the TMEM slot, the batch index and the planes' base");
 static_assert(64 + 8 * kRing <= 96, "the ring's release barriers follow at +64");
-static_assert(2 * (kSmemBytes + 1024) <= 233472, "two CTAs must fit in one SM's shared memory");
 
 // (A) AO values and gradients in double-float.  Planes p = 0..3 (phi, d/dx, d/dy, d/dz) hold the
 // FP32 hi parts at planes + p * P and the lo parts, rounded to BF16 (lo <= ulp(hi) / 2, so hi + lo
@@ -262,9 +276,14 @@ __device__ __forceinline__ double cta_sum(double v, double* red_row) {
 }  // namespace
 
 // kCache: the grid has an AO cache (EvalArgs::ao_cache); the instantiation without it keeps the
-// batch's planes in the CTA's slab at fixed addresses.
-template <bool kCache>
-__global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A) {
+// batch's planes in the CTA's slab at fixed addresses.  kN: GEMM1 N chunk (MixCfg).
+template <bool kCache, int kN>
+__global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGrid G, EvalArgs A) {
+  using Cfg = MixCfg<kN>;
+  constexpr int kOffCoef = Cfg::kOffCoef, kOffAo = Cfg::kOffAo, kOffRed = Cfg::kOffRed, kOffEg = Cfg::kOffEg;
+  constexpr int kOffTab = Cfg::kOffTab, kOffFx = Cfg::kOffFx, kOffMisc = Cfg::kOffMisc;
+  constexpr uint32_t kTmemCols = Cfg::kTmemCols;
+  constexpr int kNc = kN;  // GEMM1 N chunk of this instantiation
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* stage = base;
@@ -308,9 +327,9 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-  // TMEM: GEMM1 uses four 64-column accumulators (hh, hm+mh, hl+mm+lh, running sum); GEMM2, which
+  // TMEM: GEMM1 uses four kN-column accumulators (hh, hm+mh, hl+mm+lh, running sum); GEMM2, which
   // runs after GEMM1 is finished, uses 128 columns for its hh products and 128 for its corrections.
-  const uint32_t tH = tmem, tC1 = tmem + 64, tC2 = tmem + 128, tS = tmem + 192;
+  const uint32_t tH = tmem, tC1 = tmem + kN, tC2 = tmem + 2 * kN, tS = tmem + 3 * kN;
   const uint32_t tW = tmem, tWc = tmem + 128;
   uint32_t phase = 0, tphase = 0;
   uint32_t ring_uses[kRing] = {0, 0, 0, 0};  // uses of each buffer (its fill and release phases alike)
@@ -436,15 +455,16 @@ __global__ void __launch_bounds__(kMT, 2) vxc_mixed_kernel(DevGrid G, EvalArgs A
                             16384, tbar, pol_keep);
             tma_busy = true;
           }
-          gather_b(stage, Dhl, s_ao, n, m, kb, nc);
+          gather_b<kN>(stage, Dhl, s_ao, n, m, kb, nc);
           fence_proxy_async_smem();
           if (!wait_tma()) { failed = true; break; }
           if (tid == 0) {
             tc_fence_after();
             const uint64_t ah = sdesc_sw128(sb), am = sdesc_sw128(sb + 16384), al = sdesc_sw128(sb + 32768);
             const uint64_t aq = sdesc_sw128(sb + 49152);
-            const uint64_t bh = sdesc_sw128(sb + 65536), bm = sdesc_sw128(sb + 73728), bl = sdesc_sw128(sb + 81920);
-            const uint64_t bq = sdesc_sw128(sb + 90112);
+            // B pieces: kN rows of 128 bytes each, one after the other from +64 KB
+            const uint64_t bh = sdesc_sw128(sb + 65536), bm = sdesc_sw128(sb + 65536 + kN * 128);
+            const uint64_t bl = sdesc_sw128(sb + 65536 + 2 * kN * 128), bq = sdesc_sw128(sb + 65536 + 3 * kN * 128);
             const bool group_start = (kb & 15) == 0;
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks) {
@@ -909,28 +929,44 @@ size_t mixed_slab_doubles(int max_m) {
                         6 * sizeof(__nv_bfloat16)) / sizeof(double);
 }
 
-int mixed_ctas_per_sm() { return 2; }
+int mixed_ctas_per_sm(int tile_n) { return tile_n == 128 ? MixCfg<128>::kCtas : MixCfg<64>::kCtas; }
 
 int mixed_max_m() { return kMaxMixedM; }
 
 cudaError_t mixed_set_attributes() {
   static bool attr = false;
   if (attr) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(vxc_mixed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  cudaError_t e = cudaFuncSetAttribute(vxc_mixed_kernel<false, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       MixCfg<64>::kSmemBytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(vxc_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    e = cudaFuncSetAttribute(vxc_mixed_kernel<true, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             MixCfg<64>::kSmemBytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(vxc_mixed_kernel<false, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             MixCfg<128>::kSmemBytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(vxc_mixed_kernel<true, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             MixCfg<128>::kSmemBytes);
   if (e == cudaSuccess) attr = true;
   return e;
 }
 
+// n_ctas: the CTAs to launch (the caller sizes them by mixed_ctas_per_sm(A.tile_n)).
 cudaError_t launch_mixed(const DevGrid& G, const EvalArgs& A, int n_ctas, cudaStream_t st) {
   if (A.max_m > kMaxMixedM) return cudaErrorInvalidValue;
   const cudaError_t e = mixed_set_attributes();
   if (e != cudaSuccess) return e;
-  if (A.ao_cache)
-    vxc_mixed_kernel<true><<<n_ctas, kMT, kSmemBytes, st>>>(G, A);
-  else
-    vxc_mixed_kernel<false><<<n_ctas, kMT, kSmemBytes, st>>>(G, A);
+  if (A.tile_n == 128) {
+    if (A.ao_cache)
+      vxc_mixed_kernel<true, 128><<<n_ctas, kMT, MixCfg<128>::kSmemBytes, st>>>(G, A);
+    else
+      vxc_mixed_kernel<false, 128><<<n_ctas, kMT, MixCfg<128>::kSmemBytes, st>>>(G, A);
+  } else {
+    if (A.ao_cache)
+      vxc_mixed_kernel<true, 64><<<n_ctas, kMT, MixCfg<64>::kSmemBytes, st>>>(G, A);
+    else
+      vxc_mixed_kernel<false, 64><<<n_ctas, kMT, MixCfg<64>::kSmemBytes, st>>>(G, A);
+  }
   return cudaGetLastError();
 }
 

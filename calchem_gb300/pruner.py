@@ -371,6 +371,10 @@ class ShareEngine:
     def set_profiling(self, enable=True):
         _native.check("calchem_xc_set_profiling", _native.load().calchem_xc_set_profiling(self.grid_id, int(enable)))
 
+    def set_tile(self, tile_n):
+        """The tensor-core GEMM1 tile (64 or 128, calchem_xc_set_tile); results do not depend on it."""
+        _native.check("calchem_xc_set_tile", _native.load().calchem_xc_set_tile(self.grid_id, int(tile_n)))
+
     def ao_cache_bytes(self) -> int:
         import ctypes
         out = (ctypes.c_size_t * 1)()

@@ -198,14 +198,53 @@ def plan_points(basis, xyzw, batch_pts: int = 128, batching: str = "spatial") ->
             "sum_m2n": float(s2[0]), "max_m": int(mm[0])}
 
 
-class _EngineBase:
+class _TileMixin:
+    """The tensor-core form's GEMM1 tile (calchem_xc_set_tile): 64 or 128, or "auto" to take the
+    autotuner's choice for the workload, measured at the first tensor-core evaluation (and cached)."""
+
+    def _init_tile(self, tile, basis, grid, spin):
+        self._tile_src = (basis, grid, spin)
+        self.tile = None
+        if tile != "auto":
+            self.set_tile(int(tile))
+
+    def set_tile(self, tile_n: int):
+        _native.check("calchem_xc_set_tile", _native.load().calchem_xc_set_tile(self.grid_id, int(tile_n)))
+        self.tile = int(tile_n)
+
+    def _tune_tile(self, func, run):
+        """Picks the tile on the first tensor-core evaluation: every tile is timed on this workload (or
+        the cached choice for its signature is taken)."""
+        from . import autotune
+        basis, grid, spin = self._tile_src
+        key = autotune.signature(basis, grid, func, "mixed", spin)
+        lib = _native.load()
+
+        def measure():
+            _native.check("calchem_xc_set_profiling", lib.calchem_xc_set_profiling(self.grid_id, 1))
+            try:
+                return autotune.time_tiles(self, run)
+            finally:
+                _native.check("calchem_xc_set_profiling", lib.calchem_xc_set_profiling(self.grid_id,
+                                                                                      int(self._profiling)))
+        self.set_tile(autotune.choose_tile(key, measure))
+
+    def last_kernel_ms(self) -> float:
+        """Duration of the quadrature kernel of the last evaluate (profiling enabled)."""
+        ms = (ctypes.c_float * 1)()
+        _native.check("calchem_xc_last_kernel_ms", _native.load().calchem_xc_last_kernel_ms(self.grid_id, ms))
+        return float(ms[0])
+
+
+class _EngineBase(_TileMixin):
     """batch_pts: points per batch (16..128; the reference's 128 by default), or "auto" to take
     the autotuner's choice for this workload (tuned on first use, then cached).  batching:
     "spatial" (compact batches, the default) or "reference" (CalChem's chunks of consecutive
-    points); the results agree up to summation order."""
+    points); the results agree up to summation order.  tile: the tensor-core GEMM1 tile, 64, 128 or
+    "auto" (the default: tuned at the first tensor-core evaluation; results do not depend on it)."""
 
     def __init__(self, basis, grid, use_gpu=True, precision="fp64", batch_pts=128, func="b3lyp",
-                 batching="spatial"):
+                 batching="spatial", tile="auto"):
         if not use_gpu:
             raise NotImplementedError("calchem_gb300 evaluates Vxc on the GPU only; there is no CPU engine")
         self.n_ao = basis.n_ao
@@ -214,26 +253,27 @@ class _EngineBase:
         self.gpu_fallback_invocations = 0
         self.grid_id = 0
         self.last_nelec = None
+        self._profiling = False
+        spin = "uks" if isinstance(self, UksVxcEngine) else "rks"
         if batch_pts == "auto":
             from . import autotune
-            batch_pts = autotune.choose_batch_pts(basis, grid, func, precision,
-                                                  spin="uks" if isinstance(self, UksVxcEngine) else "rks")
+            plan = autotune.choose_plan(basis, grid, func, precision, spin=spin)
+            batch_pts = plan["batch_pts"]
+            if tile == "auto" and precision == "mixed":
+                tile = plan["tile_n"]
         self.batch_pts = int(batch_pts)
         self.batching = batching
         self.grid_id = _upload_points(basis, grid, self.batch_pts, batching)
+        self._init_tile(tile, basis, grid, spin)
 
     @classmethod
-    def new_with_gpu(cls, basis, grid, use_gpu=True, precision="fp64", batch_pts=128, batching="spatial"):
-        return cls(basis, grid, use_gpu, precision, batch_pts, batching=batching)
+    def new_with_gpu(cls, basis, grid, use_gpu=True, precision="fp64", batch_pts=128, batching="spatial",
+                     tile="auto"):
+        return cls(basis, grid, use_gpu, precision, batch_pts, batching=batching, tile=tile)
 
     def set_profiling(self, enable: bool = True):
         _native.check("calchem_xc_set_profiling", _native.load().calchem_xc_set_profiling(self.grid_id, int(enable)))
-
-    def last_kernel_ms(self) -> float:
-        """Duration of the quadrature kernel of the last evaluate (profiling enabled)."""
-        ms = (ctypes.c_float * 1)()
-        _native.check("calchem_xc_last_kernel_ms", _native.load().calchem_xc_last_kernel_ms(self.grid_id, ms))
-        return float(ms[0])
+        self._profiling = bool(enable)
 
     def telemetry(self):
         """(gpu_kernel_invocations, gpu_fallback_invocations) as in vxc.rs:420-425."""
@@ -308,9 +348,12 @@ class RksVxcEngine(_EngineBase):
         exc = np.zeros(1)
         ne = np.zeros(1)
         prec = self.precision if precision is None else _PRECISION[precision]
-        _native.check("calchem_xc_evaluate_rks", lib.calchem_xc_evaluate_rks(
+        run = lambda: _native.check("calchem_xc_evaluate_rks", lib.calchem_xc_evaluate_rks(
             self.grid_id, _xc_code(func), prec, _native.ptr(P), _native.ptr(exc), _native.ptr(ne),
             _native.ptr(V)))
+        if prec == MIXED and self.tile is None:
+            self._tune_tile(func, run)
+        run()
         self.gpu_kernel_invocations += self.last_launch_count()
         self.last_nelec = float(ne[0])
         return float(exc[0]), V
@@ -328,9 +371,12 @@ class UksVxcEngine(_EngineBase):
         exc = np.zeros(1)
         ne = np.zeros(2)
         prec = self.precision if precision is None else _PRECISION[precision]
-        _native.check("calchem_xc_evaluate_uks", lib.calchem_xc_evaluate_uks(
+        run = lambda: _native.check("calchem_xc_evaluate_uks", lib.calchem_xc_evaluate_uks(
             self.grid_id, _xc_code(func), prec, _native.ptr(Pa), _native.ptr(Pb), _native.ptr(exc),
             _native.ptr(ne), _native.ptr(Va), _native.ptr(Vb)))
+        if prec == MIXED and self.tile is None:
+            self._tune_tile(func, run)
+        run()
         self.gpu_kernel_invocations += self.last_launch_count()
         self.last_nelec = (float(ne[0]), float(ne[1]))
         return float(exc[0]), Va, Vb
@@ -381,7 +427,14 @@ def xc_nuclear_gradient(mol, basis, grid, func, pa, pb, precision="fp64"):
     return xc_nuclear_gradient_with_gpu(mol, basis, grid, func, pa, pb, True, precision)[0]
 
 
-class VxcGroup:
+class _GroupGrid:
+    """Point count of a group's members together (the autotuner's workload signature)."""
+
+    def __init__(self, n):
+        self.xyzw = np.empty((n, 0))
+
+
+class VxcGroup(_TileMixin):
     """Many molecules, one persistent kernel launch per evaluation (calchem_xc_group_create).
 
     ``members`` is a sequence of (basis, grid) pairs.  Every member's grid is batched as a single
@@ -391,10 +444,11 @@ class VxcGroup:
     vector whose member blocks start at ``offsets`` (device and graph paths).
     """
 
-    def __init__(self, members, precision="fp64", batch_pts=128, batching="spatial"):
+    def __init__(self, members, precision="fp64", batch_pts=128, batching="spatial", tile="auto"):
         lib = _native.load()
         self.precision = _PRECISION[precision]
         self.grid_id = 0
+        self._profiling = False
         ids = []
         try:
             for basis, grid in members:
@@ -416,6 +470,13 @@ class VxcGroup:
         _native.check("calchem_xc_group_layout", lib.calchem_xc_group_layout(
             self.grid_id, _native.ptr(nm), _native.ptr(self.sizes), _native.ptr(self.offsets)))
         self.packed_size = int(np.sum(self.sizes.astype(np.int64) ** 2))
+        # the tile is tuned on the whole group (its members' first basis names the signature)
+        self._init_tile(tile, members[0][0], _GroupGrid(sum(len(g.xyzw) for _, g in members)),
+                        f"group{self.n_mols}")
+
+    def set_profiling(self, enable: bool = True):
+        _native.check("calchem_xc_set_profiling", _native.load().calchem_xc_set_profiling(self.grid_id, int(enable)))
+        self._profiling = bool(enable)
 
     def pack(self, mats) -> np.ndarray:
         if len(mats) != self.n_mols:
@@ -461,8 +522,11 @@ class VxcGroup:
         exc = np.zeros(self.n_mols)
         ne = np.zeros(self.n_mols)
         prec = self.precision if precision is None else _PRECISION[precision]
-        _native.check("calchem_xc_evaluate_rks", lib.calchem_xc_evaluate_rks(
+        run = lambda: _native.check("calchem_xc_evaluate_rks", lib.calchem_xc_evaluate_rks(
             self.grid_id, _xc_code(func), prec, _native.ptr(P), _native.ptr(exc), _native.ptr(ne), _native.ptr(V)))
+        if prec == MIXED and self.tile is None:
+            self._tune_tile(func, run)
+        run()
         return exc, ne, self.unpack(V)
 
     def evaluate_uks(self, func, pas, pbs, precision=None):
@@ -475,9 +539,12 @@ class VxcGroup:
         exc = np.zeros(self.n_mols)
         ne = np.zeros(2 * self.n_mols)
         prec = self.precision if precision is None else _PRECISION[precision]
-        _native.check("calchem_xc_evaluate_uks", lib.calchem_xc_evaluate_uks(
+        run = lambda: _native.check("calchem_xc_evaluate_uks", lib.calchem_xc_evaluate_uks(
             self.grid_id, _xc_code(func), prec, _native.ptr(Pa), _native.ptr(Pb), _native.ptr(exc), _native.ptr(ne),
             _native.ptr(Va), _native.ptr(Vb)))
+        if prec == MIXED and self.tile is None:
+            self._tune_tile(func, run)
+        run()
         return exc, ne.reshape(self.n_mols, 2), self.unpack(Va), self.unpack(Vb)
 
     def capture_rks(self, func, d_total: int, d_result: int, d_v: int, precision=None):

@@ -245,6 +245,15 @@ int calchem_xc_evaluate_rks(uint64_t grid_id, int xc_code, int precision, const 
 int calchem_xc_evaluate_rks_points(uint64_t grid_id, int xc_code, int precision, const double* h_d_total,
                                    double* exc_out, double* nelec_out, double* h_point_out);
 
+/* The tensor-core form's GEMM1 tile (no counterpart in the reference; chosen by the autotuner):
+ * tile_n = 64 AOs per TMEM accumulator with two CTAs per SM (the default), or 128 with one CTA per SM
+ * and all 512 TMEM columns (half the GEMM1 rounds and operand reloads per batch, no second CTA to
+ * overlap with).  Results are identical up to the order of the Vxc atomics.  calchem_xc_set_tile
+ * returns -1 for another value, -2 for an unknown id; calchem_xc_get_tile returns the tile or -2.  A
+ * captured graph keeps the tile it was captured with. */
+int calchem_xc_set_tile(uint64_t grid_id, int tile_n);
+int calchem_xc_get_tile(uint64_t grid_id);
+
 /* Per-atom quadrature shares for the learned grid's periodic full-grid judge (no counterpart in the
  * reference).  calchem_xc_set_point_atoms gives the host atom (0 .. n_atoms - 1) of every point the
  * caller uploaded, in its order (n_points = the uploaded count); the library groups the planned points
