@@ -51,8 +51,8 @@ SIGNATURES = {
     "calchem_xc_set_tile": (_I, [_U64, _I]),
     "calchem_xc_get_tile": (_I, [_U64]),
     "calchem_xc_set_point_atoms": (_I, [_U64, _P, _I, _I]),
-    "calchem_xc_evaluate_rks_atoms": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
-    "calchem_xc_evaluate_rks_atoms_device": (_I, [_U64, _I, _I, _P, _P, _P, _P]),
+    "calchem_xc_evaluate_rks_atoms": (_I, [_U64, _I, _I, _P, _P, _P, _P, _P]),
+    "calchem_xc_evaluate_rks_atoms_device": (_I, [_U64, _I, _I, _P, _P, _P, _P, _P]),
     "calchem_xc_eval_closed_shell": (_I, [_I, _I, _I, _P, _P, _P]),
     "calchem_xc_set_ao_cache": (_I, [_U64, _I, _P]),
     "calchem_xc_fxc_contract_ex": (_I, [_U64, _I, _I, _P, _I, _P]),

@@ -1456,8 +1456,9 @@ int calchem_xc_set_point_atoms(uint64_t grid_id, const int* h_host_atom, int n_p
 }
 
 namespace {
-// Per-point shares (no Vxc) and their per-atom sums, enqueued on st.
-int enqueue_atom_shares(Entry& e, int xc_code, int precision, const double* d_total, double* d_result,
+// Per-point shares and their per-atom sums, enqueued on st; with d_v the full build (Vxc into d_v)
+// as well, without it the shares alone (no Vxc contraction).
+int enqueue_atom_shares(Entry& e, int xc_code, int precision, const double* d_total, double* d_result, double* d_v,
                         double* d_atom_out, cudaStream_t st) {
   if (int rc0 = ensure_ws(e)) return rc0;
   const size_t np2 = 2 * (size_t)e.n_pts;
@@ -1466,8 +1467,8 @@ int enqueue_atom_shares(Entry& e, int xc_code, int precision, const double* d_to
     return -4;
   }
   if (cudaMemsetAsync(e.d_pt_out, 0, np2 * sizeof(double), st) != cudaSuccess) return -5;
-  int rc = enqueue_eval(e, kModeRks, xc_code, precision, d_total, nullptr, nullptr, nullptr, nullptr, nullptr,
-                        d_result, st, e.d_pt_out, true);
+  int rc = enqueue_eval(e, kModeRks, xc_code, precision, d_total, nullptr, d_v, nullptr, nullptr, nullptr, d_result,
+                        st, e.d_pt_out, d_v == nullptr);
   if (rc) return rc;
   if (launch_atom_shares(e.d_pt_out, e.d_atom_pts, e.d_atom_off, e.n_share_atoms, d_atom_out, st) != cudaSuccess)
     return -5;
@@ -1477,7 +1478,7 @@ int enqueue_atom_shares(Entry& e, int xc_code, int precision, const double* d_to
 }  // namespace
 
 int calchem_xc_evaluate_rks_atoms(uint64_t grid_id, int xc_code, int precision, const double* h_d_total,
-                                  double* exc_out, double* nelec_out, double* h_atom_out) {
+                                  double* exc_out, double* nelec_out, double* h_atom_out, double* h_v_out) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!h_d_total || !exc_out || !nelec_out || !h_atom_out || !valid_xc(xc_code)) return -1;
   if (!valid_prec(precision, kModeRks)) return -1;
@@ -1490,10 +1491,14 @@ int calchem_xc_evaluate_rks_atoms(uint64_t grid_id, int xc_code, int precision, 
   std::memcpy(e->h_stage, h_d_total, nn * sizeof(double));
   if (cudaMemcpyAsync(e->d_P, e->h_stage, nn * sizeof(double), cudaMemcpyHostToDevice, e->stream) != cudaSuccess)
     return -5;
-  int rc = enqueue_atom_shares(*e, xc_code, precision, e->d_P, e->d_res, e->d_atom_out, e->stream);
+  int rc = enqueue_atom_shares(*e, xc_code, precision, e->d_P, e->d_res, h_v_out ? e->d_V : nullptr, e->d_atom_out,
+                               e->stream);
   if (rc) return rc;
   double* h_res = e->h_stage + 2 * nn;
   int* h_status = reinterpret_cast<int*>(h_res + 4);
+  if (h_v_out && cudaMemcpyAsync(e->h_stage, e->d_V, nn * sizeof(double), cudaMemcpyDeviceToHost, e->stream) !=
+                     cudaSuccess)
+    return -5;
   if (cudaMemcpyAsync(h_res, e->d_res, 2 * sizeof(double), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
       cudaMemcpyAsync(h_status, e->d_counter + 2, sizeof(int), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
       cudaMemcpyAsync(h_atom_out, e->d_atom_out, 2 * (size_t)e->n_share_atoms * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1503,17 +1508,18 @@ int calchem_xc_evaluate_rks_atoms(uint64_t grid_id, int xc_code, int precision, 
   if (*h_status != 0) return -7;
   *exc_out = h_res[0];
   *nelec_out = h_res[1];
+  if (h_v_out) std::memcpy(h_v_out, e->h_stage, nn * sizeof(double));
   return 0;
 }
 
 int calchem_xc_evaluate_rks_atoms_device(uint64_t grid_id, int xc_code, int precision, const double* d_total,
-                                         double* d_result, double* d_atom_out, void* stream) {
+                                         double* d_result, double* d_v, double* d_atom_out, void* stream) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!d_total || !d_result || !d_atom_out || !valid_xc(xc_code) || !valid_prec(precision, kModeRks)) return -1;
   Entry* e = find(grid_id);
   if (!e || e->n_mols != 1 || e->n_share_atoms <= 0) return -2;
   if (!e->has_w) return -1;
-  return enqueue_atom_shares(*e, xc_code, precision, d_total, d_result, d_atom_out, (cudaStream_t)stream);
+  return enqueue_atom_shares(*e, xc_code, precision, d_total, d_result, d_v, d_atom_out, (cudaStream_t)stream);
 }
 
 int calchem_xc_fxc_prepare(uint64_t grid_id, int xc_code, const double* h_d_total) {

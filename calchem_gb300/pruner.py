@@ -359,14 +359,14 @@ class ShareEngine:
         exc, ne = np.zeros(1), np.zeros(1)
         _native.check("calchem_xc_evaluate_rks_atoms", lib.calchem_xc_evaluate_rks_atoms(
             self.grid_id, _xc_code(func), _PRECISION[precision], _native.ptr(P), _native.ptr(exc), _native.ptr(ne),
-            _native.ptr(out)))
+            _native.ptr(out), None))
         return out[0::2].copy(), out[1::2].copy()
 
     def enqueue(self, d_total, d_result, d_atom_out, stream, func, precision="mixed"):
         """Device-buffer form (addresses; d_atom_out holds 2 n_atoms doubles), enqueued on stream."""
         from .vxc import _xc_code, _PRECISION
         return _native.load().calchem_xc_evaluate_rks_atoms_device(
-            self.grid_id, _xc_code(func), _PRECISION[precision], d_total, d_result, d_atom_out, stream)
+            self.grid_id, _xc_code(func), _PRECISION[precision], d_total, d_result, None, d_atom_out, stream)
 
     def set_profiling(self, enable=True):
         _native.check("calchem_xc_set_profiling", _native.load().calchem_xc_set_profiling(self.grid_id, int(enable)))
@@ -414,9 +414,12 @@ class LearnedGrid:
     Becke partitioning makes an atom's share depend on its own points only, and an atom kept at the
     Fine level has the same points on both grids, so the judge evaluates just the pruned atoms'
     points: their Fine points and their pruned points, two resident uploads (``judge_engines``) kept
-    with their AO caches between checks and rebuilt only when an atom reverts.  The shares need no
-    Vxc contraction, and the check runs in the tensor-core form by default (its per-atom share error,
-    ~1e-10 Eh, is far below the per-atom tolerance)."""
+    with their AO caches between checks and rebuilt only when an atom reverts.  The pruned grid's
+    shares can come from the iteration's own build instead (``pruned_shares``, from
+    ``RksVxcEngine.evaluate_with_shares``), which leaves only the Fine points to evaluate.  The shares
+    need no Vxc contraction, and the check runs in the tensor-core form by default (the difference
+    it judges is within ~2e-10 Eh of the FP64 form's on water clusters and octane, against per-atom
+    tolerances of ~3e-9 and above)."""
 
     def __init__(self, mol, basis, net=None, tol=5e-7, margin=0.5):
         self.mol = mol
@@ -438,39 +441,58 @@ class LearnedGrid:
     def pruned_atoms(self):
         return np.nonzero(self.levels != FINE)[0]
 
-    def judge_engines(self):
-        """(Fine-grid points of the pruned atoms, pruned-grid points of the same atoms) as resident
-        ShareEngines; None when no atom is pruned."""
+    def fine_judge(self):
+        """The Fine-grid points of the pruned atoms as a resident ShareEngine; None when no atom is
+        pruned."""
         atoms = self.pruned_atoms()
         if len(atoms) == 0:
             return None
         if self._judge is None:
-            n = len(self.mol.atoms)
+            self._judge = [None, None]
+        if self._judge[0] is None:
             fine = _subgrid(self.fine_grid, np.isin(self.fine_grid.host_atom, atoms))
-            pruned = _subgrid(self.grid, np.isin(self.grid.host_atom, atoms))
-            self._judge = (ShareEngine(self.basis, fine, n), ShareEngine(self.basis, pruned, n))
-        return self._judge
+            self._judge[0] = ShareEngine(self.basis, fine, len(self.mol.atoms))
+        return self._judge[0]
 
-    def judge_points(self):
-        """Points the judge evaluates (Fine and pruned uploads together)."""
-        j = self.judge_engines()
-        return 0 if j is None else j[0].n_points + j[1].n_points
+    def judge_engines(self):
+        """(Fine-grid points of the pruned atoms, pruned-grid points of the same atoms) as resident
+        ShareEngines; None when no atom is pruned."""
+        if self.fine_judge() is None:
+            return None
+        if self._judge[1] is None:
+            pruned = _subgrid(self.grid, np.isin(self.grid.host_atom, self.pruned_atoms()))
+            self._judge[1] = ShareEngine(self.basis, pruned, len(self.mol.atoms))
+        return tuple(self._judge)
+
+    def judge_points(self, with_pruned=True):
+        """Points the judge evaluates (the Fine upload, and the pruned one unless the build supplies
+        the pruned shares)."""
+        j = self.fine_judge()
+        if j is None:
+            return 0
+        return j.n_points + (self.judge_engines()[1].n_points if with_pruned else 0)
 
     def _close_judge(self):
         if self._judge is not None:
             for e in self._judge:
-                e.close()
+                if e is not None:
+                    e.close()
             self._judge = None
 
-    def check(self, D, func, precision="mixed"):
-        """Full-grid check; returns (atoms reverted to Fine, per-atom errors).  The grid and the judge
-        uploads are rebuilt if any atom reverts."""
+    def check(self, D, func, precision="mixed", pruned_shares=None):
+        """Full-grid check; returns (atoms reverted to Fine, per-atom errors).  pruned_shares: the
+        pruned grid's per-atom (E_A, T_A) from the iteration's own build (all atoms; only the pruned
+        ones are read), in place of evaluating them here.  The grid and the judge uploads are rebuilt
+        if any atom reverts."""
         n = len(self.mol.atoms)
-        judge = self.judge_engines()
+        judge = self.fine_judge()
         if judge is None:
             return [], np.zeros(n)
-        E0, T0 = judge[0].shares(D, func, precision)
-        E, T = judge[1].shares(D, func, precision)
+        E0, T0 = judge.shares(D, func, precision)
+        if pruned_shares is None:
+            E, T = self.judge_engines()[1].shares(D, func, precision)
+        else:
+            E, T = (np.asarray(x, dtype=np.float64) for x in pruned_shares)
         err = np.maximum(np.abs(E - E0), np.abs(T - T0))
         bad = [int(a) for a in np.nonzero((err > self.tol_atom) & (self.levels != FINE))[0]]
         if bad:

@@ -68,6 +68,57 @@ def eri_tensor(basis) -> np.ndarray:
     return eri
 
 
+class _JK:
+    """Coulomb and exchange matrices J_pq = sum_rs (pq|rs) D_rs and K_pq = sum_rs (pr|qs) D_rs from the
+    dense ERI tensor: numpy contractions, or (device given) two matrix-vector products on the GPU with
+    the tensor resident in device memory (large bases, where the host contractions would dominate)."""
+
+    def __init__(self, eri, device=None):
+        self.n = eri.shape[0]
+        self.eri = eri
+        self.dev = device
+        if device is not None:
+            import torch
+            t = torch.from_numpy(eri).to(device)
+            n2 = self.n * self.n
+            self.Jm = t.view(n2, n2)
+            self.Km = t.permute(0, 2, 1, 3).reshape(n2, n2)  # (pq|rs) -> [(p,q), (r,s)] of (pr|qs)
+
+    def _apply(self, M, D, spec):
+        if self.dev is None:
+            return np.einsum(spec, self.eri, D, optimize=True)
+        import torch
+        d = torch.from_numpy(np.ascontiguousarray(D, dtype=np.float64).ravel()).to(self.dev)
+        return (M @ d).view(self.n, self.n).cpu().numpy()
+
+    def J(self, D):
+        return self._apply(getattr(self, "Jm", None), D, "pqrs,rs->pq")
+
+    def K(self, D):
+        return self._apply(getattr(self, "Km", None), D, "prqs,rs->pq")
+
+
+def integrals(mol, basis):
+    """The SCF's integrals once per geometry: {"S", "T", "V", "eri"} (pass to rks / uks as ints)."""
+    S, T, V = core_matrices(basis, mol)
+    return {"S": S, "T": T, "V": V, "eri": eri_tensor(basis)}
+
+
+def _jk_device(eri, jk):
+    if jk == "host":
+        return None
+    if jk not in ("auto", "gpu"):
+        raise ValueError("jk must be 'auto', 'host' or 'gpu'")
+    try:
+        import torch
+        ok = torch.cuda.is_available()
+    except ImportError:
+        ok = False
+    if jk == "gpu" and not ok:
+        raise RuntimeError("jk='gpu' needs a CUDA device")
+    return torch.device("cuda", torch.cuda.current_device()) if ok and (jk == "gpu" or eri.nbytes > (1 << 30)) else None
+
+
 class _Diis:
     def __init__(self, size=8):
         self.size = size
@@ -111,6 +162,8 @@ class ScfResult:
     grid_points: int = 0
     energies: list = field(default_factory=list)
     reverted_atoms: list = field(default_factory=list)
+    first_exc: float = 0.0            # Exc of the first iteration (at the core-Hamiltonian guess density)
+    first_density: np.ndarray = None  # total density of the first iteration
 
 
 def _orthogonaliser(S):
@@ -134,14 +187,24 @@ def _grid_and_engine(mol, basis, func, level, precision, learned, tol, spin):
     else:
         lg = None
         grid = MolecularGrid.build_for_basis(mol, basis, level)
-    cls = RksVxcEngine if spin == "rks" else UksVxcEngine
-    return lg, grid, cls(basis, grid, precision=precision)
+    return lg, grid, _engine(mol, basis, grid, precision, spin, learned)
 
 
-def _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter, e_tol, g_tol, spin):
-    S, T, Vn = core_matrices(basis, mol)
+def _engine(mol, basis, grid, precision, spin, learned):
+    if spin == "uks":
+        return UksVxcEngine(basis, grid, precision=precision)
+    eng = RksVxcEngine(basis, grid, precision=precision)
+    if learned:  # the judge takes the pruned grid's per-atom shares from the build
+        eng.set_point_atoms(grid.host_atom, len(mol.atoms))
+    return eng
+
+
+def _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter, e_tol, g_tol, spin, ints=None,
+         jk="auto"):
+    ints = integrals(mol, basis) if ints is None else ints
+    S, T, Vn, eri = ints["S"], ints["T"], ints["V"], ints["eri"]
     H = T + Vn
-    eri = eri_tensor(basis)
+    jk_op = _JK(eri, _jk_device(eri, jk))
     X = _orthogonaliser(S)
     ax = exact_exchange_fraction(func)
     e_nuc = nuclear_repulsion(mol)
@@ -158,21 +221,33 @@ def _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter
     exc = 0.0
     it = 0
     for it in range(1, max_iter + 1):
-        if lg is not None and judge_every and it % judge_every == 0:
-            bad, _ = lg.check(Da + Db, func) if spin == "rks" else lg.check(Da + Db, func)
+        judge_now = lg is not None and judge_every and it % judge_every == 0
+        if judge_now and spin == "uks":
+            bad, _ = lg.check(Da + Db, func, precision=precision)
             if bad:
                 reverted.extend(bad)
                 eng.close()
                 grid = lg.grid
-                eng = (RksVxcEngine if spin == "rks" else UksVxcEngine)(basis, grid, precision=precision)
+                eng = _engine(mol, basis, grid, precision, spin, True)
         Dt = Da + Db
-        J = np.einsum("pqrs,rs->pq", eri, Dt, optimize=True)
-        Ka = np.einsum("prqs,rs->pq", eri, Da, optimize=True)
-        Kb = np.einsum("prqs,rs->pq", eri, Db, optimize=True)
+        J = jk_op.J(Dt)
+        Ka = jk_op.K(Da) if ax != 0.0 else np.zeros_like(Dt)
+        Kb = Ka if spin == "rks" else (jk_op.K(Db) if ax != 0.0 else Ka)
         if func is None:
             exc, Va, Vb = 0.0, 0.0, 0.0
         elif spin == "rks":
-            exc, Va = eng.evaluate(basis, grid, func, Dt)
+            if judge_now:
+                # the periodic full-grid check, with the pruned grid's shares from this build
+                exc, Va, E, T = eng.evaluate_with_shares(basis, grid, func, Dt)
+                bad, _ = lg.check(Dt, func, precision=precision, pruned_shares=(E, T))
+                if bad:
+                    reverted.extend(bad)
+                    eng.close()
+                    grid = lg.grid
+                    eng = _engine(mol, basis, grid, precision, spin, True)
+                    exc, Va = eng.evaluate(basis, grid, func, Dt)
+            else:
+                exc, Va = eng.evaluate(basis, grid, func, Dt)
             Vb = Va
         else:
             exc, Va, Vb = eng.evaluate(basis, grid, func, Da, Db)
@@ -180,6 +255,8 @@ def _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter
         Fb = H + J - ax * Kb + Vb
         e = (np.sum(Dt * H) + 0.5 * np.sum(Dt * J) - 0.5 * ax * (np.sum(Da * Ka) + np.sum(Db * Kb)) + exc + e_nuc)
         energies.append(float(e))
+        if it == 1:
+            first = (float(exc), Dt.copy())
         errs = (X.T @ (Fa @ Da @ S - S @ Da @ Fa) @ X, X.T @ (Fb @ Db @ S - S @ Db @ Fb) @ X)
         g = max(float(np.max(np.abs(errs[0]))), float(np.max(np.abs(errs[1]))))
         if e_old is not None and abs(e - e_old) < e_tol and g < g_tol:
@@ -203,21 +280,27 @@ def _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter
         s2 = float(sz * (sz + 1) + n_b - np.sum(ov * ov) - sz * (sz + 1))
     if eng is not None:
         eng.close()
+    if lg is not None:
+        lg.close()
     dens = (Da + Db,) if spin == "rks" else (Da, Db)
     return ScfResult(energies[-1], converged, it, e_orb, dens, float(exc), e_nuc, s2,
-                     0 if grid is None else len(grid), energies, reverted)
+                     0 if grid is None else len(grid), energies, reverted, first_exc=first[0], first_density=first[1])
 
 
 def rks(mol, basis, func="b3lyp", level=GridLevel.FINE, precision="fp64", learned=False, tol=5e-7, judge_every=5,
-        max_iter=128, e_tol=1e-10, g_tol=1e-7):
-    """Restricted Kohn-Sham (restricted Hartree-Fock for func=None) to tight convergence."""
-    return _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter, e_tol, g_tol, "rks")
+        max_iter=128, e_tol=1e-10, g_tol=1e-7, ints=None, jk="auto"):
+    """Restricted Kohn-Sham (restricted Hartree-Fock for func=None) to tight convergence.  ints: the
+    integrals() of this geometry, to share them between runs; jk: "auto" (J and K on the GPU for dense
+    ERI tensors over 1 GiB), "host" or "gpu"."""
+    return _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter, e_tol, g_tol, "rks",
+                ints, jk)
 
 
 def uks(mol, basis, func="b3lyp", level=GridLevel.FINE, precision="fp64", learned=False, tol=5e-7, judge_every=5,
-        max_iter=128, e_tol=1e-10, g_tol=1e-7):
+        max_iter=128, e_tol=1e-10, g_tol=1e-7, ints=None, jk="auto"):
     """Unrestricted Kohn-Sham (unrestricted Hartree-Fock for func=None)."""
-    return _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter, e_tol, g_tol, "uks")
+    return _run(mol, basis, func, level, precision, learned, tol, judge_every, max_iter, e_tol, g_tol, "uks",
+                ints, jk)
 
 
 def rhf(mol, basis, **kw):

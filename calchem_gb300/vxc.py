@@ -359,6 +359,35 @@ class RksVxcEngine(_EngineBase):
         return float(exc[0]), V
 
 
+    def set_point_atoms(self, host_atom, n_atoms):
+        """Host atom of every grid point (the grid's order), for evaluate_with_shares."""
+        host = np.ascontiguousarray(host_atom, dtype=np.int32)
+        _native.check("calchem_xc_set_point_atoms", _native.load().calchem_xc_set_point_atoms(
+            self.grid_id, _native.ptr(host), len(host), int(n_atoms)))
+        self._share_atoms = int(n_atoms)
+
+    def evaluate_with_shares(self, basis, grid, func, density_total, precision=None):
+        """evaluate() plus every atom's share of Exc and of tr(D Vxc) from the same build
+        (calchem_xc_evaluate_rks_atoms): (Exc, Vxc, E_A, T_A).  set_point_atoms must come first."""
+        lib = _native.load()
+        n_at = getattr(self, "_share_atoms", 0)
+        if n_at <= 0:
+            raise ValueError("set_point_atoms first")
+        P = _as_matrix(density_total, self.n_ao)
+        V = np.zeros((self.n_ao, self.n_ao), dtype=np.float64)
+        out = np.zeros(2 * n_at)
+        exc, ne = np.zeros(1), np.zeros(1)
+        prec = self.precision if precision is None else _PRECISION[precision]
+        if prec == MIXED and self.tile is None:
+            self.evaluate(basis, grid, func, density_total, precision)  # tunes the tile
+        _native.check("calchem_xc_evaluate_rks_atoms", lib.calchem_xc_evaluate_rks_atoms(
+            self.grid_id, _xc_code(func), prec, _native.ptr(P), _native.ptr(exc), _native.ptr(ne), _native.ptr(out),
+            _native.ptr(V)))
+        self.gpu_kernel_invocations += self.last_launch_count()
+        self.last_nelec = float(ne[0])
+        return float(exc[0]), V, out[0::2].copy(), out[1::2].copy()
+
+
 class UksVxcEngine(_EngineBase):
     """Open-shell engine: evaluate(basis, grid, func, Pa, Pb) -> (Exc, Va, Vb) (vxc.rs:1662-1669)."""
 

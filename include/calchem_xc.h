@@ -258,16 +258,19 @@ int calchem_xc_get_tile(uint64_t grid_id);
  * reference).  calchem_xc_set_point_atoms gives the host atom (0 .. n_atoms - 1) of every point the
  * caller uploaded, in its order (n_points = the uploaded count); the library groups the planned points
  * by atom once.  calchem_xc_evaluate_rks_atoms then evaluates the closed-shell per-point shares of
- * calchem_xc_evaluate_rks_points WITHOUT the Vxc contraction and sums them per atom on the device in
- * a fixed order: atom_out[2 a] = sum of w f over atom a's points (its share of Exc), atom_out[2 a + 1]
- * = its share of tr(D Vxc); exc_out / nelec_out as calchem_xc_evaluate_rks.  The _device variant takes
- * device buffers (d_result: Exc, Nelec; d_atom_out: 2 n_atoms) and enqueues on `stream`.  Returns -2
- * for an unknown id, a group, a point count that differs from the upload, or (evaluate) no atoms set. */
+ * calchem_xc_evaluate_rks_points and sums them per atom on the device in a fixed order: atom_out[2 a] =
+ * sum of w f over atom a's points (its share of Exc), atom_out[2 a + 1] = its share of tr(D Vxc);
+ * exc_out / nelec_out as calchem_xc_evaluate_rks.  With h_v_out = NULL it skips the Vxc contraction
+ * (the shares alone); with h_v_out it is the full build as well (Vxc as calchem_xc_evaluate_rks), so
+ * an SCF iteration that runs the judge gets the pruned grid's shares from its own build.  The
+ * _device variant takes device buffers (d_result: Exc, Nelec; d_v: n x n or NULL; d_atom_out: 2
+ * n_atoms) and enqueues on `stream`.  Returns -2 for an unknown id, a group, a point count that
+ * differs from the upload, or (evaluate) no atoms set. */
 int calchem_xc_set_point_atoms(uint64_t grid_id, const int* h_host_atom, int n_points, int n_atoms);
 int calchem_xc_evaluate_rks_atoms(uint64_t grid_id, int xc_code, int precision, const double* h_d_total,
-                                  double* exc_out, double* nelec_out, double* h_atom_out);
+                                  double* exc_out, double* nelec_out, double* h_atom_out, double* h_v_out);
 int calchem_xc_evaluate_rks_atoms_device(uint64_t grid_id, int xc_code, int precision, const double* d_total,
-                                         double* d_result, double* d_atom_out, void* stream);
+                                         double* d_result, double* d_v, double* d_atom_out, void* stream);
 
 /* The closed-shell point functional on the device (eval_xc_spin, crates/calchem-dft/src/xc.rs:159-175,
  * at rho_a = rho_b = h_rho[i], gamma_aa = gamma_ab = gamma_bb = h_gamma[i]): h_out[3 i ..] =

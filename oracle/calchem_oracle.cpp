@@ -1386,6 +1386,7 @@ struct RksEngine {
   std::vector<GridPoint> pts;
   bool cached = false;
   double cache_bytes = 0;
+  double work = 0;  // sum over batches of m_b^2 n_b (the two contractions' size)
   std::vector<CachedBatch> batches;
 };
 
@@ -1407,6 +1408,7 @@ RksEngine* rks_engine_create(const Basis& bs, const std::vector<GridPoint>& pts,
     int m = 0;
     for (int s : cand[b]) m += bs.shells[s].ncomp();
     total += (double)m * (double)pidx[b].size() * 4.0 * 8.0;
+    eng->work += (double)m * (double)m * (double)pidx[b].size();
   }
   eng->cache_bytes = total;
   if (total > cap_bytes) return eng;  // the engine then runs evaluate_vxc_rks (vxc.rs:802-804)
@@ -1926,6 +1928,7 @@ void* orc_rks_engine_create(void* bp, void* gp, double cap_bytes, int threads) {
 int orc_rks_engine_is_cached(void* e) { return static_cast<RksEngine*>(e)->cached ? 1 : 0; }
 double orc_rks_engine_cache_bytes(void* e) { return static_cast<RksEngine*>(e)->cache_bytes; }
 int orc_rks_engine_n_batches(void* e) { return (int)static_cast<RksEngine*>(e)->batches.size(); }
+double orc_rks_engine_work(void* e) { return static_cast<RksEngine*>(e)->work; }
 void orc_rks_engine_evaluate(void* e, const double* P, int func, int threads, double* exc, double* nelec, double* V,
                              int batch_begin, int batch_end, int blocked) {
   rks_engine_evaluate(*static_cast<RksEngine*>(e), P, func, threads > 0 ? threads : n_threads(), exc, nelec, V,

@@ -43,6 +43,7 @@ _SIGS = {
     "orc_rks_engine_is_cached": (_I, [_P]),
     "orc_rks_engine_cache_bytes": (_D, [_P]),
     "orc_rks_engine_n_batches": (_I, [_P]),
+    "orc_rks_engine_work": (_D, [_P]),
     "orc_rks_engine_evaluate": (None, [_P, _P, _I, _I, _P, _P, _P, _I, _I, _I]),
     "orc_rks_engine_free": (None, [_P]),
     "orc_overlap": (None, [_P, _P]),
@@ -253,6 +254,7 @@ class RksEngine:
         self.cached = bool(lib().orc_rks_engine_is_cached(self.h))
         self.cache_bytes = lib().orc_rks_engine_cache_bytes(self.h)
         self.n_batches = lib().orc_rks_engine_n_batches(self.h)
+        self.work = lib().orc_rks_engine_work(self.h)  # sum over CalChem's batches of m_b^2 n_b
 
     def evaluate(self, P, func, threads=0, batch_range=(-1, -1), blocked=False):
         """blocked: the two contractions by the register-blocked FMA product (cpu_gemm.cpp), as the

@@ -8,7 +8,7 @@ import time
 import numpy as np
 import pytest
 
-from calchem_gb300 import BasisSet, GridLevel, MolecularGrid, RksVxcEngine, UksVxcEngine, pruner, workloads
+from calchem_gb300 import BasisSet, GridLevel, MolecularGrid, RksVxcEngine, UksVxcEngine, VxcGroup, pruner, workloads
 
 pytestmark = pytest.mark.gpu
 
@@ -64,3 +64,46 @@ def test_water61_learned_grid_mixed_against_fp64_fine(lib):
     assert abs(e - e_ref) < EXC_TOL
     ref.close()
     eng.close()
+
+
+def test_water_clusters_64_group_graph_mixed_against_fp64(lib):
+    """The 64-cluster batched workload at full size (PBE / 6-31G(d), Fine grid): one group, one
+    persistent launch per build, the autotuned tile, a CUDA-graph replay; every molecule within
+    |dExc| <= 1e-6 Eh of the FP64 form, and the replay equal to the host call."""
+    torch = pytest.importorskip("torch")
+    sizes = workloads.cluster_batch_sizes()
+    members, dens = [], []
+    for i, k in enumerate(sizes):
+        mol = workloads.water_cluster(k, 1000 + i)
+        basis = BasisSet.from_name("6-31g(d)", mol)
+        grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
+        members.append((basis, grid))
+        dens.append(workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, 7 + i))
+    fp64 = VxcGroup(members, precision="fp64")
+    e64, n64, V64 = fp64.evaluate_rks("pbe", dens)
+    fp64.close()
+    grp = VxcGroup(members, precision="mixed")
+    t0 = time.perf_counter()
+    em, nm, Vm = grp.evaluate_rks("pbe", dens)  # tunes the tile on the first evaluation
+    t = time.perf_counter() - t0
+    assert grp.tile in (64, 128)
+    print(f"\n64 clusters ({sum(sizes)} waters, {sum(len(g) for _, g in members)} points): tile {grp.tile}, "
+          f"first mixed call {t * 1e3:.0f} ms, max |dExc| {np.max(np.abs(em - e64)):.2e}")
+    assert np.max(np.abs(em - e64)) <= EXC_TOL
+    assert np.max(np.abs(nm - n64)) < 1e-6
+    assert max(float(np.max(np.abs(a - b))) for a, b in zip(Vm, V64)) < 2e-6
+    # one graph replay of the whole build on device buffers
+    dev = torch.device("cuda")
+    dP = torch.from_numpy(grp.pack(dens)).to(dev)
+    dV = torch.zeros(grp.packed_size, dtype=torch.float64, device=dev)
+    dres = torch.zeros(3 * grp.n_mols + 1, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    grp.capture_rks("pbe", dP.data_ptr(), dres.data_ptr(), dV.data_ptr())
+    grp.replay(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert grp.status() == 0
+    res = dres.cpu().numpy()
+    assert np.array_equal(res[0:2 * grp.n_mols:2], em)
+    Vg = grp.unpack(dV.cpu().numpy())
+    assert max(float(np.max(np.abs(a - b))) for a, b in zip(Vg, Vm)) < 1e-12
+    grp.close()

@@ -78,6 +78,38 @@ def test_device_atom_sums_match_the_per_point_shares(lib, precision, tol):
     eng.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_build_with_shares_matches_the_build_and_the_share_engine(lib, precision):
+    """evaluate_with_shares: the same Exc, Nelec and Vxc as evaluate, and the same per-atom shares as a
+    shares-only evaluation of the same points; the judge gives the same verdict with them."""
+    mol = workloads.water_cluster(4, 6)
+    basis = BasisSet.from_name("6-31g(d)", mol)
+    D = workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, 9)
+    lg = pruner.LearnedGrid(mol, basis, tol=5e-7)
+    n = len(mol.atoms)
+    eng = RksVxcEngine(basis, lg.grid, precision=precision)
+    eng.set_point_atoms(lg.grid.host_atom, n)
+    e0, V0 = eng.evaluate(basis, lg.grid, "b3lyp", D)
+    n0 = eng.last_nelec
+    e1, V1, E, T = eng.evaluate_with_shares(basis, lg.grid, "b3lyp", D)
+    assert e1 == e0 and eng.last_nelec == n0
+    assert np.max(np.abs(V1 - V0)) < 1e-12
+    assert abs(E.sum() - e1) < 1e-10
+    share = pruner.ShareEngine(basis, lg.grid, n)
+    Es, Ts = share.shares(D, "b3lyp", precision)
+    assert np.max(np.abs(E - Es)) < 1e-12 and np.max(np.abs(T - Ts)) < 1e-12
+    share.close()
+    bad_a, err_a = lg.check(D, "b3lyp", precision=precision)
+    lg2 = pruner.LearnedGrid(mol, basis, tol=5e-7)
+    bad_b, err_b = lg2.check(D, "b3lyp", precision=precision, pruned_shares=(E, T))
+    at = lg2.pruned_atoms()
+    assert bad_a == bad_b
+    assert np.max(np.abs(err_a[at] - err_b[at])) < 1e-12
+    eng.close()
+    lg.close()
+    lg2.close()
+
+
 def test_level_errors_shrink_towards_fine(lib):
     mol = workloads.water_cluster(2, 3)
     basis = BasisSet.from_name("6-31g(d)", mol)

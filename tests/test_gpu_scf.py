@@ -61,3 +61,29 @@ def test_mixed_learned_scf_energy_matches_fp64_fine(lib):
           f"dE {fast.total_energy_hartree - ref.total_energy_hartree:.2e}")
     assert fast.grid_points < ref.grid_points
     assert abs(fast.total_energy_hartree - ref.total_energy_hartree) < 1e-6
+
+
+def test_octane_mixed_learned_scf_energy_matches_fp64_fine(lib, oracle):
+    """The spec accuracy criterion on the C8H18 benchmark molecule (B3LYP / 6-31G(d,p), 210 AOs,
+    33 doubly occupied orbitals): the converged SCF energy with the tensor-core build on the learned
+    grid (judge every 5 iterations) within 1e-6 Eh of the FP64 Fine-grid SCF; and the FP64 Fine
+    SCF's first-iteration Exc (core-Hamiltonian guess density) against the oracle's CalChem
+    restatement on the same grid."""
+    mol = workloads.octane()
+    basis = BasisSet.from_name("6-31g(d,p)", mol)
+    ints = scf.integrals(mol, basis)
+    ref = scf.rks(mol, basis, "b3lyp", GridLevel.FINE, precision="fp64", ints=ints, e_tol=1e-9, g_tol=1e-6)
+    fast = scf.rks(mol, basis, "b3lyp", precision="mixed", learned=True, tol=5e-7, ints=ints, e_tol=1e-9,
+                   g_tol=1e-6)
+    assert ref.converged and fast.converged
+    print(f"\nC8H18 B3LYP/6-31G(d,p): FP64 Fine {ref.total_energy_hartree:.10f} ({ref.grid_points} points, "
+          f"{ref.iterations} iterations), mixed learned {fast.total_energy_hartree:.10f} ({fast.grid_points} "
+          f"points, {fast.iterations} iterations, reverted {len(fast.reverted_atoms)}), "
+          f"dE {fast.total_energy_hartree - ref.total_energy_hartree:.2e}")
+    assert fast.grid_points < ref.grid_points
+    assert abs(fast.total_energy_hartree - ref.total_energy_hartree) < 1e-6
+    from calchem_gb300 import MolecularGrid
+    grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
+    ob = oracle.Basis.from_name("6-31g(d,p)", [a.symbol for a in mol.atoms], mol.coords_bohr)
+    e_or, _, _ = oracle.RksEngine(ob, oracle.Grid.from_points(grid.xyzw)).evaluate(ref.first_density, "b3lyp")
+    assert abs(ref.first_exc - e_or) < 1e-9
