@@ -55,6 +55,10 @@ RKS_WORKLOADS = {
                       "(H2O)61 water cluster, 183 atoms (rigid waters, 1 g/cm^3, O-O >= 2.6 A, PCG64 seed 61), "
                       "B3LYP (VWN_RPA), 6-31G(d) Cartesian 1159 AOs, CalChem Fine grid (99 radial shells, pruned "
                       "Lebedev, Becke) as judge, seeded S-orthonormal D (244 occ, seed 7)"),
+    "water12_b3lyp": (("water_cluster", (12, 12)), "6-31g(d)", "b3lyp",
+                      "(H2O)12 water cluster (rigid waters, 1 g/cm^3, O-O >= 2.6 A, PCG64 seed 12), B3LYP (VWN_RPA), "
+                      "6-31G(d) Cartesian 228 AOs, CalChem Fine grid as judge, seeded S-orthonormal D (seed 7); "
+                      "the profiling stand-in for the 61-water build (a few GB on the device)"),
     "octane_b3lyp": (("octane", ()), "6-31g(d,p)", "b3lyp",
                      "C8H18 all-trans, B3LYP (VWN_RPA), 6-31G(d,p) Cartesian 210 AOs, CalChem Fine grid "
                      "(99 radial shells, pruned Lebedev, Becke) as judge, seeded S-orthonormal D (33 occ, seed 7)"),
@@ -74,9 +78,13 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", default="learned", choices=["learned", "fine"],
                     help="learned: the MLP-pruned grid with the periodic Fine-grid judge (RKS workloads)")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="profiling case for ncu: the learned-grid build of an RKS workload on a fresh engine, "
+                         "twice (the first fills the AO cache), tile 64, no judge, tuning, graph or baselines; "
+                         "capture the second launch of the quadrature kernel")
     ap.add_argument("--workload", default="water61_b3lyp",
-                    choices=["water61_b3lyp", "octane_b3lyp", "c54h18_pbe0_uks", "water_clusters_pbe",
-                             "octane_b3lyp_gradient", "octane_b3lyp_fxc"],
+                    choices=["water61_b3lyp", "water12_b3lyp", "octane_b3lyp", "c54h18_pbe0_uks",
+                             "water_clusters_pbe", "octane_b3lyp_gradient", "octane_b3lyp_fxc"],
                     help="water61_b3lyp is the headline; octane_b3lyp, the UKS flake and the 64-cluster batched "
                          "launch report the same line; octane_b3lyp_gradient times the XC nuclear gradient and "
                          "octane_b3lyp_fxc the TD-DFT kernel contraction (each its own metric)")
@@ -956,8 +964,34 @@ def run_fxc(args):
     return 0
 
 
+def run_profile_case(args):
+    """Two builds of the workload's learned-grid engine (tensor-core form unless --precision fp64); the
+    second reads the AO cache, as every timed build does.  Prints the kernel times."""
+    from calchem_gb300 import RksVxcEngine, pruner
+
+    mol, basis, D = build_inputs(args.workload)
+    _, _, func, _ = rks_molecule(args.workload)
+    lg = pruner.LearnedGrid(mol, basis, tol=PRUNE_TOL)
+    prec = "fp64" if args.precision == "fp64" else "mixed"
+    eng = RksVxcEngine(basis, lg.grid, precision=prec, tile=64)
+    eng.set_profiling(True)
+    ms = []
+    for _ in range(2):
+        eng.evaluate(basis, lg.grid, func, D)
+        ms.append(eng.last_kernel_ms())
+    n_batches, sum_m2n, sum_m2, max_m = eng.plan_stats()
+    print(json.dumps({"profile_case": args.workload, "precision": prec, "grid_points": len(lg.grid),
+                      "batches": n_batches, "sum_m2n": sum_m2n, "sum_m2": sum_m2, "max_m": max_m,
+                      "ao_cache_bytes": eng.ao_cache_bytes(), "kernel_ms": ms}), flush=True)
+    eng.close()
+    lg.close()
+    return 0
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "octane_b3lyp_gradient":
