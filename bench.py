@@ -64,8 +64,11 @@ RKS_WORKLOADS = {
                      "(99 radial shells, pruned Lebedev, Becke) as judge, seeded S-orthonormal D (33 occ, seed 7)"),
 }
 # DRAM bytes (read + write) per launch of the quadrature kernel from one ncu capture of the workload's
-# timed build (profiles/); absent until a capture exists for the workload and precision.
-NCU_TRAFFIC_BYTES = {("octane_b3lyp", "fp64"): 1.746e9, ("octane_b3lyp", "mixed"): 2.656e9}
+# timed build (profiles/); absent until a capture exists for the workload and precision.  The 61-water
+# build is too large for a full capture: its figure is the 12-water capture (2.006 GB, 1.599 GB of AO
+# cache) scaled by the AO-cache bytes (14.138 GB), the data that traffic grows with.
+NCU_TRAFFIC_BYTES = {("octane_b3lyp", "fp64"): 1.746e9, ("octane_b3lyp", "mixed"): 2.597e9,
+                     ("water12_b3lyp", "mixed"): 2.006e9, ("water61_b3lyp", "mixed"): 17.74e9}
 
 
 def parse():
