@@ -339,6 +339,7 @@ class _Work:
     def __init__(self, name, torch, dev, prec_name, grid_kind="fine"):
         from calchem_gb300 import (BasisSet, GridLevel, MolecularGrid, RksVxcEngine, UksVxcEngine, VxcGroup,
                                    _native, pruner, workloads)
+        from calchem_gb300.vxc import default_ao_floor
         self.name = name
         self.torch = torch
         self.dev = dev
@@ -383,7 +384,10 @@ class _Work:
             else:
                 grid_fine = grid
             self.plain = RksVxcEngine(basis, grid_fine, batching="reference")
-            self.obj = RksVxcEngine(basis, grid)
+            # the timed engine's plan: the tensor-core form's value screen (vxc.MIXED_AO_FLOOR)
+            self.ao_floor = default_ao_floor(prec_name)
+            self.obj = RksVxcEngine(basis, grid, ao_floor=self.ao_floor)
+            self.grid_info["ao_floor"] = self.ao_floor
             if self.lg is not None:
                 self.obj.set_point_atoms(grid.host_atom, len(mol.atoms))
             self.grid_obj = grid
@@ -392,7 +396,8 @@ class _Work:
             mol, basis, func, (Pa, Pb) = workloads.build_workload("c54h18_pbe0_uks", SEED)
             grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
             self.kind, self.func, self.xc = "uks", "pbe0", 5
-            self.obj = UksVxcEngine(basis, grid)
+            self.obj = UksVxcEngine(basis, grid, ao_floor=default_ao_floor(prec_name))
+            self.grid_info["ao_floor"] = default_ao_floor(prec_name)
             self.plain = UksVxcEngine(basis, grid, batching="reference")
             self.basis_obj, self.grid_obj = basis, grid
             self.mats = [Pa, Pb]
@@ -414,6 +419,7 @@ class _Work:
             self.cluster_xyzw = [g.xyzw for _, g in members]
             self.kind, self.func, self.xc = "group", "pbe", 2
             self.obj = VxcGroup(members, precision=prec_name)
+            self.grid_info["ao_floor"] = self.obj.ao_floor
             self.plain = VxcGroup(members, precision="fp64", batching="reference")
             self.mats = dens
             self.n_points = sum(len(g) for _, g in members)

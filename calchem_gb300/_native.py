@@ -43,6 +43,7 @@ SIGNATURES = {
     "calchem_xc_upload_points": (_I, [_P, _I, _P, _I, _P, _I, _P, _I, _I, _U64, _SZ]),
     "calchem_xc_upload_points_ex": (_I, [_P, _I, _P, _I, _P, _I, _P, _I, _I, _I, _U64, _SZ]),
     "calchem_xc_upload_points_spatial": (_I, [_P, _I, _P, _I, _P, _I, _P, _I, _I, _I, _U64, _SZ]),
+    "calchem_xc_upload_points_screened": (_I, [_P, _I, _P, _I, _P, _I, _P, _I, _I, _I, _U64, _SZ, ctypes.c_double]),
     "calchem_xc_plan_points": (_I, [_P, _I, _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I]),
     "calchem_xc_set_weights": (_I, [_U64, _P, _I]),
     "calchem_xc_plan_stats": (_I, [_U64, _P, _P, _P, _P]),

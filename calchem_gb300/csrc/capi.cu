@@ -1098,18 +1098,21 @@ int calchem_xc_grid_release(uint64_t grid_handle) {
 
 static int upload_points_impl(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,
                               const AoCompGpu* h_comps, int n_comps, const double* h_xyzw, int n_pts, int n_ao,
-                              int batch_pts, uint64_t grid_id, size_t memory_limit_bytes, bool spatial) {
+                              int batch_pts, uint64_t grid_id, size_t memory_limit_bytes, bool spatial,
+                              double ao_floor = kZeroFloor) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!h_shells || !h_prims || !h_comps || !h_xyzw || n_shells <= 0 || n_prims <= 0 || n_comps <= 0 || n_pts <= 0 ||
-      n_ao <= 0 || grid_id == 0 || batch_pts < 16 || batch_pts > kBlockPts)
+      n_ao <= 0 || grid_id == 0 || batch_pts < 16 || batch_pts > kBlockPts || !(ao_floor >= kZeroFloor) ||
+      !(ao_floor <= 1e-6))
     return -1;
   if (g_grids.count(grid_id)) return -2;
   for (int s = 0; s < n_shells; ++s)
     if (!(h_shells[s].r2_cutoff >= 0.0)) return -1;
   Plan plan;
-  if (spatial)
-    plan_batches_spatial(h_shells, n_shells, h_xyzw, n_pts, plan, batch_pts);
-  else
+  if (spatial) {
+    const ValueScreen vs{h_prims, h_comps, n_prims, n_comps, ao_floor};
+    plan_batches_spatial(h_shells, n_shells, h_xyzw, n_pts, plan, batch_pts, &vs);
+  } else
     plan_batches(h_shells, n_shells, h_xyzw, n_pts, plan, batch_pts);
   if (plan.pts.empty()) return -1;
   const int rc = upload_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, plan.pts.data(),
@@ -1174,6 +1177,14 @@ int calchem_xc_upload_points_spatial(const AoShellGpu* h_shells, int n_shells, c
                                      size_t memory_limit_bytes) {
   return upload_points_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, h_xyzw, n_pts, n_ao, batch_pts,
                             grid_id, memory_limit_bytes, true);
+}
+
+int calchem_xc_upload_points_screened(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims,
+                                      int n_prims, const AoCompGpu* h_comps, int n_comps, const double* h_xyzw,
+                                      int n_pts, int n_ao, int batch_pts, uint64_t grid_id,
+                                      size_t memory_limit_bytes, double ao_floor) {
+  return upload_points_impl(h_shells, n_shells, h_prims, n_prims, h_comps, n_comps, h_xyzw, n_pts, n_ao, batch_pts,
+                            grid_id, memory_limit_bytes, true, ao_floor);
 }
 
 int calchem_xc_upload_points(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims, int n_prims,

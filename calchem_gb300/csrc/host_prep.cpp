@@ -436,8 +436,45 @@ void becke_tables(int n, const int* z, const double* xyz, std::vector<double>& i
 // With `reach`, only those with r^2 <= r2_cutoff (1 + 1e-6) at one point at least are kept: the
 // others give exact zeros at every point of the batch (the kernels test r^2 > r2_cutoff per point;
 // the margin covers their FP32 form of that test).
+// Whether a bound on |phi| and |grad phi| of one of shell s's components reaches `floor` at one of the
+// points at least.  With R0 = sum_p w_p exp(-a_p r^2), R1 = -2 sum_p a_p w_p exp(-a_p r^2), l the
+// shell's angular momentum and S the largest component scale: |x^i y^j z^k| <= r^l, so
+// |phi| <= S r^l sum |w_p| e_p and |d phi / dq| <= S (l r^(l-1) sum |w_p| e_p + 2 r^(l+1) sum a_p |w_p| e_p).
+static bool shell_reaches_value(const AoShellGpu& sh, const AoPrimGpu* prims, const AoCompGpu* comps,
+                                const double* xyzw, const int* idx, int n, double floor) {
+  const int l = sh.n_funcs == 1 ? 0 : sh.n_funcs == 3 ? 1 : sh.n_funcs == 6 ? 2 : 3;
+  double smax = 0.0;
+  for (int c = 0; c < sh.n_funcs; ++c) smax = std::max(smax, std::fabs(comps[sh.comp_start + c].scale));
+  for (int k = 0; k < n; ++k) {
+    const double* p = xyzw + 4 * (size_t)idx[k];
+    const double px = p[0] - sh.center[0], py = p[1] - sh.center[1], pz = p[2] - sh.center[2];
+    const double r2 = px * px + py * py + pz * pz;
+    double e0 = 0.0, e1 = 0.0;
+    for (int q = 0; q < sh.n_prims; ++q) {
+      const AoPrimGpu& pr = prims[sh.prim_start + q];
+      const double e = std::fabs(pr.weighted_norm) * std::exp(-pr.exponent * r2);
+      e0 += e;
+      e1 += pr.exponent * e;
+    }
+    const double r = std::sqrt(r2);
+    const double rl = l == 0 ? 1.0 : (l == 1 ? r : (l == 2 ? r2 : r2 * r));
+    const double rl1 = l == 0 ? 0.0 : (l == 1 ? 1.0 : (l == 2 ? r : r2));  // r^(l-1)
+    const double b0 = smax * rl * e0;
+    const double b1 = smax * (l * rl1 * e0 + 2.0 * rl * r * e1);
+    if (b0 >= floor || b1 >= floor) return true;
+  }
+  return false;
+}
+
+// valid: the shell's primitive and component ranges lie in the arrays (the upload rejects them
+// otherwise, so the bound is not needed then).
+static bool shell_ranges_ok(const AoShellGpu& sh, int n_prims, int n_comps) {
+  return sh.n_prims >= 1 && sh.prim_start >= 0 && sh.prim_start + sh.n_prims <= n_prims && sh.n_funcs >= 1 &&
+         sh.n_funcs <= 10 && sh.comp_start >= 0 && sh.comp_start + sh.n_funcs <= n_comps;
+}
+
 static void batch_candidates(const AoShellGpu* shells, int n_shells, const double* xyzw, const int* idx, int n,
-                             bool reach, std::vector<int>& out) {
+                             bool reach, std::vector<int>& out, const ValueScreen* vs = nullptr) {
   out.clear();
   double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
   for (int k = 0; k < n; ++k) {
@@ -464,13 +501,16 @@ static void batch_candidates(const AoShellGpu* shells, int n_shells, const doubl
         hit = px * px + py * py + pz * pz <= lim;
       }
       if (!hit) continue;
+      if (vs && shell_ranges_ok(shells[s], vs->n_prims, vs->n_comps) &&
+          !shell_reaches_value(shells[s], vs->prims, vs->comps, xyzw, idx, n, vs->floor))
+        continue;
     }
     out.push_back(s);
   }
 }
 
 int plan_batches_spatial(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan,
-                         int batch_pts) {
+                         int batch_pts, const ValueScreen* vs) {
   plan = Plan();
   std::vector<int> order;
   order.reserve(n_pts);
@@ -513,7 +553,7 @@ int plan_batches_spatial(const AoShellGpu* shells, int n_shells, const double* x
 #pragma omp parallel for schedule(dynamic, 16)
   for (int b = 0; b < nb; ++b)
     batch_candidates(shells, n_shells, xyzw, order.data() + leaves[b].first, leaves[b].second - leaves[b].first,
-                     true, cand[b]);
+                     true, cand[b], vs);
   plan.cand_offsets.push_back(0);
   for (int b = 0; b < nb; ++b) {
     if (cand[b].empty()) continue;  // no AO reaches these points: they contribute nothing

@@ -59,10 +59,24 @@ struct Plan {
 // Chunks of batch_pts consecutive points (kPlanBatch = 128 in the reference, vxc.rs:96).
 int plan_batches(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan,
                  int batch_pts = kPlanBatch);
+// Value screen of the compact plan: a candidate shell is dropped from a batch when a bound on every
+// component's |phi| and |grad phi| stays below `floor` at all of the batch's points.  With floor
+// kZeroFloor (1e-17) the dropped shells are exactly zero at those points in every form of the
+// quadrature (the reference zeroes components whose value and gradient are all <= 1e-16,
+// ao_grid.rs:182-230), so results change only by the order of additions of zeros; a larger floor is
+// an approximation that the caller chooses.
+constexpr double kZeroFloor = 1e-17;
+struct ValueScreen {
+  const AoPrimGpu* prims;
+  const AoCompGpu* comps;
+  int n_prims, n_comps;
+  double floor;
+};
 // Spatially compact batches: the kept points ordered by recursive bisection (leaves of batch_pts
 // points), then chunked; candidates by the reference's rule, narrowed to the shells that reach at
-// least one point of the batch.  Every point sees the same nonzero AOs as under plan_batches.
+// least one point of the batch (and, with vs, whose values reach vs->floor there).  Every point sees
+// the same nonzero AOs as under plan_batches.
 int plan_batches_spatial(const AoShellGpu* shells, int n_shells, const double* xyzw, int n_pts, Plan& plan,
-                         int batch_pts = kPlanBatch);
+                         int batch_pts = kPlanBatch, const ValueScreen* vs = nullptr);
 
 }  // namespace cxc

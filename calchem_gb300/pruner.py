@@ -340,12 +340,12 @@ class ShareEngine:
     calchem_xc_evaluate_rks_atoms[_device]).  The points stay on the device, with the tensor-core
     form's AO cache, across evaluations."""
 
-    def __init__(self, basis, grid, n_atoms):
+    def __init__(self, basis, grid, n_atoms, ao_floor=None):
         from .vxc import _upload_points
         lib = _native.load()
         self.n_atoms = int(n_atoms)
         self.n_points = len(grid)
-        self.grid_id = _upload_points(basis, grid)
+        self.grid_id = _upload_points(basis, grid, ao_floor=ao_floor)
         host = np.ascontiguousarray(grid.host_atom, dtype=np.int32)
         _native.check("calchem_xc_set_point_atoms",
                       lib.calchem_xc_set_point_atoms(self.grid_id, _native.ptr(host), len(host), self.n_atoms))
@@ -421,9 +421,13 @@ class LearnedGrid:
     it judges is within ~2e-10 Eh of the FP64 form's on water clusters and octane, against per-atom
     tolerances of ~3e-9 and above)."""
 
-    def __init__(self, mol, basis, net=None, tol=5e-7, margin=0.5):
+    def __init__(self, mol, basis, net=None, tol=5e-7, margin=0.5, ao_floor="auto"):
+        """ao_floor: the value screen of the judge's uploads ("auto": the tensor-core engines' floor,
+        so that the judge's shares and a tensor-core build's shares come from the same plan rule)."""
+        from .vxc import MIXED_AO_FLOOR
         self.mol = mol
         self.basis = basis
+        self.ao_floor = MIXED_AO_FLOOR if ao_floor == "auto" else ao_floor
         self.net = Network.load() if net is None else net
         self.tol_atom = tol / len(mol.atoms)
         self.levels = choose_levels(self.net, mol, self.tol_atom, margin)
@@ -451,7 +455,7 @@ class LearnedGrid:
             self._judge = [None, None]
         if self._judge[0] is None:
             fine = _subgrid(self.fine_grid, np.isin(self.fine_grid.host_atom, atoms))
-            self._judge[0] = ShareEngine(self.basis, fine, len(self.mol.atoms))
+            self._judge[0] = ShareEngine(self.basis, fine, len(self.mol.atoms), self.ao_floor)
         return self._judge[0]
 
     def judge_engines(self):
@@ -461,7 +465,7 @@ class LearnedGrid:
             return None
         if self._judge[1] is None:
             pruned = _subgrid(self.grid, np.isin(self.grid.host_atom, self.pruned_atoms()))
-            self._judge[1] = ShareEngine(self.basis, pruned, len(self.mol.atoms))
+            self._judge[1] = ShareEngine(self.basis, pruned, len(self.mol.atoms), self.ao_floor)
         return tuple(self._judge)
 
     def judge_points(self, with_pruned=True):

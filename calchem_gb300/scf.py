@@ -182,7 +182,8 @@ def _grid_and_engine(mol, basis, func, level, precision, learned, tol, spin):
         return None, None, None
     if learned:
         from . import pruner
-        lg = pruner.LearnedGrid(mol, basis, tol=tol)
+        from .vxc import default_ao_floor
+        lg = pruner.LearnedGrid(mol, basis, tol=tol, ao_floor=default_ao_floor(precision))
         grid = lg.grid
     else:
         lg = None

@@ -30,6 +30,19 @@ _ids = itertools.count(1 << 20)
 
 MAX_GPU_MEMORY_BYTES = 64 << 30
 
+# The tensor-core engines' value screen (calchem_xc_upload_points_screened): a shell is left out of a
+# compact batch when a bound on its components' values and gradients stays below this at every point
+# of the batch.  Those contributions are ~4 orders below the tensor-core form's own agreement with
+# FP64 on Vxc (~1e-6); on the 61-water cluster the screen halves sum m^2 n and moves Exc by < 1e-10 Eh.
+# The FP64 form keeps the exact screen (1e-17: only values the reference itself zeroes are left out).
+MIXED_AO_FLOOR = 1e-12
+
+
+def default_ao_floor(precision):
+    """The value screen an engine of this precision uploads with: MIXED_AO_FLOOR for the tensor-core
+    form, the exact screen (None) for FP64."""
+    return MIXED_AO_FLOOR if _PRECISION[precision] == MIXED else None
+
 
 def eval_closed_shell_gpu(func, rho_a, gamma, precision="fp64"):
     """The closed-shell point functional on the device: eval_xc_spin (xc.rs:159-175) at
@@ -150,10 +163,13 @@ class GpuVxcGrid:
 BATCHING = ("spatial", "reference")
 
 
-def _upload_points(basis, grid, batch_pts: int = 128, batching: str = "spatial") -> int:
+def _upload_points(basis, grid, batch_pts: int = 128, batching: str = "spatial", ao_floor=None) -> int:
     """Batches and uploads one molecule's grid; returns its grid id.  batching "spatial": compact
     batches (calchem_xc_upload_points_spatial); "reference": chunks of consecutive points as CalChem
-    forms them (calchem_xc_upload_points_ex).  The results agree up to summation order."""
+    forms them (calchem_xc_upload_points_ex).  The results agree up to summation order.  ao_floor
+    (compact batches only): drop a shell from a batch when a bound on its components' values and
+    gradients stays below this at every point of the batch (calchem_xc_upload_points_screened);
+    None is the exact screen (1e-17, below the reference's own 1e-16 cut)."""
     if batching not in BATCHING:
         raise ValueError(f"batching must be one of {BATCHING}")
     lib = _native.load()
@@ -162,10 +178,16 @@ def _upload_points(basis, grid, batch_pts: int = 128, batching: str = "spatial")
     if len(xyzw) == 0:
         raise ValueError("empty grid")
     gid = next(_ids)
+    args = (_native.ptr(sh), len(sh), _native.ptr(pr), len(pr), _native.ptr(co), len(co), _native.ptr(xyzw),
+            len(xyzw), basis.n_ao, int(batch_pts), gid, resolve_gpu_memory_limit())
+    if ao_floor is not None:
+        if batching != "spatial":
+            raise ValueError("ao_floor applies to compact (spatial) batches")
+        _native.check("calchem_xc_upload_points_screened", lib.calchem_xc_upload_points_screened(*args,
+                                                                                                float(ao_floor)))
+        return gid
     fn = "calchem_xc_upload_points_spatial" if batching == "spatial" else "calchem_xc_upload_points_ex"
-    _native.check(fn, getattr(lib, fn)(
-        _native.ptr(sh), len(sh), _native.ptr(pr), len(pr), _native.ptr(co), len(co), _native.ptr(xyzw),
-        len(xyzw), basis.n_ao, int(batch_pts), gid, resolve_gpu_memory_limit()))
+    _native.check(fn, getattr(lib, fn)(*args))
     return gid
 
 
@@ -241,10 +263,12 @@ class _EngineBase(_TileMixin):
     the autotuner's choice for this workload (tuned on first use, then cached).  batching:
     "spatial" (compact batches, the default) or "reference" (CalChem's chunks of consecutive
     points); the results agree up to summation order.  tile: the tensor-core GEMM1 tile, 64, 128 or
-    "auto" (the default: tuned at the first tensor-core evaluation; results do not depend on it)."""
+    "auto" (the default: tuned at the first tensor-core evaluation; results do not depend on it).
+    ao_floor: the compact plan's value screen ("auto": MIXED_AO_FLOOR for a tensor-core engine, the
+    exact screen for FP64; None: exact; a number: that floor)."""
 
     def __init__(self, basis, grid, use_gpu=True, precision="fp64", batch_pts=128, func="b3lyp",
-                 batching="spatial", tile="auto"):
+                 batching="spatial", tile="auto", ao_floor="auto"):
         if not use_gpu:
             raise NotImplementedError("calchem_gb300 evaluates Vxc on the GPU only; there is no CPU engine")
         self.n_ao = basis.n_ao
@@ -263,7 +287,10 @@ class _EngineBase(_TileMixin):
                 tile = plan["tile_n"]
         self.batch_pts = int(batch_pts)
         self.batching = batching
-        self.grid_id = _upload_points(basis, grid, self.batch_pts, batching)
+        if ao_floor == "auto":
+            ao_floor = default_ao_floor(precision) if batching == "spatial" else None
+        self.ao_floor = ao_floor
+        self.grid_id = _upload_points(basis, grid, self.batch_pts, batching, ao_floor)
         self._init_tile(tile, basis, grid, spin)
 
     @classmethod
@@ -473,15 +500,18 @@ class VxcGroup(_TileMixin):
     vector whose member blocks start at ``offsets`` (device and graph paths).
     """
 
-    def __init__(self, members, precision="fp64", batch_pts=128, batching="spatial", tile="auto"):
+    def __init__(self, members, precision="fp64", batch_pts=128, batching="spatial", tile="auto", ao_floor="auto"):
         lib = _native.load()
         self.precision = _PRECISION[precision]
         self.grid_id = 0
         self._profiling = False
+        if ao_floor == "auto":
+            ao_floor = default_ao_floor(precision) if batching == "spatial" else None
+        self.ao_floor = ao_floor
         ids = []
         try:
             for basis, grid in members:
-                ids.append(_upload_points(basis, grid, batch_pts, batching))
+                ids.append(_upload_points(basis, grid, batch_pts, batching, ao_floor))
             gid = next(_ids)
             arr = np.array(ids, dtype=np.uint64)
             _native.check("calchem_xc_group_create", lib.calchem_xc_group_create(

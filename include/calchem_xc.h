@@ -195,11 +195,24 @@ int calchem_xc_plan_points(const AoShellGpu* h_shells, int n_shells, const doubl
  * cut-off sphere holds at least one of its points.  A chunk of the reference's order spans whole
  * Lebedev spheres, so its candidates are nearly every shell; a compact batch has far fewer AOs.
  * Every point sees the same nonzero AO values as under the reference's batching, so the results are
- * the same up to summation order. */
+ * the same up to summation order.  A candidate shell is also dropped from a batch when a bound on all
+ * its components' |phi| and |grad phi| stays below 1e-17 at every point of the batch: those values are
+ * zeroed by the reference's own screen (<= 1e-16, ao_grid.rs:182-230), so the results do not change.
+ * (calchem_xc_plan_points, which has no primitives, does not apply this bound.) */
 int calchem_xc_upload_points_spatial(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims,
                                      int n_prims, const AoCompGpu* h_comps, int n_comps, const double* h_xyzw,
                                      int n_pts, int n_ao, int batch_pts, uint64_t grid_id,
                                      size_t memory_limit_bytes);
+
+/* As calchem_xc_upload_points_spatial with the value screen's floor chosen by the caller (no
+ * counterpart in the reference): shells whose bound stays below ao_floor at every point of a batch are
+ * left out of it.  ao_floor = 1e-17 is the exact screen above; larger floors (up to 1e-6) drop AO
+ * contributions up to that size, an approximation traded for fewer AOs per batch.  -1 for ao_floor
+ * outside [1e-17, 1e-6]. */
+int calchem_xc_upload_points_screened(const AoShellGpu* h_shells, int n_shells, const AoPrimGpu* h_prims,
+                                      int n_prims, const AoCompGpu* h_comps, int n_comps, const double* h_xyzw,
+                                      int n_pts, int n_ao, int batch_pts, uint64_t grid_id,
+                                      size_t memory_limit_bytes, double ao_floor);
 
 /* Attaches quadrature weights to a grid uploaded with calchem_cuda_vxc_upload_grid
  * (weights in the uploaded point order). */

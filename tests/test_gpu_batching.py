@@ -121,3 +121,39 @@ def test_spatial_batches_degenerate_grids(shape):
         tol_e, tol_v = (1e-11, 1e-12) if prec == "fp64" else (1e-7, 2e-6)
         assert abs(e_sp - e_ref) < tol_e * max(1.0, abs(e_ref))
         assert np.max(np.abs(V_sp - V_ref)) < tol_v
+
+
+@pytest.mark.gpu
+def test_value_screen_floor_changes_little_and_cuts_work(native_lib):
+    """The compact plan's value screen: the exact floor (1e-17, the default) leaves out only shells
+    the reference zeroes itself; the tensor-core engines' floor (1e-12) leaves out contributions below
+    it, which moves Exc by far less than the mixed form's own error and cuts sum m^2 n; floors outside
+    [1e-17, 1e-6] are rejected."""
+    from calchem_gb300.vxc import MIXED_AO_FLOOR
+    from calchem_gb300 import _native
+    mol = workloads.water_cluster(8, 5)
+    basis = BasisSet.from_name("6-31g(d)", mol)
+    grid = MolecularGrid.build_for_basis(mol, basis, GridLevel.FINE)
+    D = workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, 7)
+    ref = RksVxcEngine(basis, grid, batching="reference")
+    e_ref, V_ref = ref.evaluate(basis, grid, "b3lyp", D)
+    ref.close()
+    out = {}
+    for floor in (None, MIXED_AO_FLOOR):
+        for prec in ("fp64", "mixed"):
+            eng = RksVxcEngine(basis, grid, precision=prec, ao_floor=floor)
+            e, V = eng.evaluate(basis, grid, "b3lyp", D)
+            out[(floor, prec)] = (e, V, eng.plan_stats()[1])
+            eng.close()
+    e0, V0, w0 = out[(None, "fp64")]
+    assert abs(e0 - e_ref) < 1e-10 and np.max(np.abs(V0 - V_ref)) < 1e-12  # the exact screen
+    e1, V1, w1 = out[(MIXED_AO_FLOOR, "fp64")]
+    assert w1 < 0.9 * w0
+    assert abs(e1 - e0) < 1e-9 and np.max(np.abs(V1 - V0)) < 1e-9
+    em0, Vm0, _ = out[(None, "mixed")]
+    em1, Vm1, _ = out[(MIXED_AO_FLOOR, "mixed")]
+    assert abs(em1 - em0) < 1e-9 and np.max(np.abs(Vm1 - Vm0)) < 1e-8
+    assert RksVxcEngine(basis, grid, precision="mixed").ao_floor == MIXED_AO_FLOOR
+    for bad in (1e-18, 1e-5):
+        with pytest.raises(_native.CalchemXcError):
+            RksVxcEngine(basis, grid, ao_floor=bad)
