@@ -65,10 +65,10 @@ RKS_WORKLOADS = {
 }
 # DRAM bytes (read + write) per launch of the quadrature kernel from one ncu capture of the workload's
 # timed build (profiles/); absent until a capture exists for the workload and precision.  The 61-water
-# build is too large for a full capture: its figure is the 12-water capture (2.006 GB, 1.599 GB of AO
-# cache) scaled by the AO-cache bytes (14.138 GB), the data that traffic grows with.
-NCU_TRAFFIC_BYTES = {("octane_b3lyp", "fp64"): 1.746e9, ("octane_b3lyp", "mixed"): 2.597e9,
-                     ("water12_b3lyp", "mixed"): 2.006e9, ("water61_b3lyp", "mixed"): 17.74e9}
+# build is too large for a full capture: its figure is the 12-water capture (1.267 GB, 1.325 GB of AO
+# cache) scaled by the AO-cache bytes (10.074 GB), the data that traffic grows with.
+NCU_TRAFFIC_BYTES = {("octane_b3lyp", "mixed"): 1.951e9, ("water12_b3lyp", "mixed"): 1.267e9,
+                     ("water61_b3lyp", "mixed"): 9.63e9}
 
 
 def parse():
