@@ -35,18 +35,31 @@ __device__ __forceinline__ double dist_to(const double* __restrict__ xyz, int a,
 
 __device__ __forceinline__ double clamp1(double v) { return v < -1.0 ? -1.0 : (v > 1.0 ? 1.0 : v); }
 
+// Molecules with at most this many atoms keep every point-atom distance of pass 1 in a per-thread
+// array, which pass 2 reads instead of recomputing an FP64 square root per (active atom, atom) pair;
+// the values are the same, so the weights are too.
+constexpr int kBeckeDistCache = 256;
+
 __device__ double becke_weight(int n, const double* __restrict__ xyz, const double* __restrict__ inv_r,
                                const double* __restrict__ a_ij, int host, double x, double y, double z) {
   if (n <= 1) return 1.0;
+  double rd[kBeckeDistCache];
+  const bool cached = n <= kBeckeDistCache;
   const double r_host = dist_to(xyz, host, x, y, z);
   const size_t row_h = (size_t)host * n;
   double p_host = 1.0;
   int n_active = 0;
+  int b_done = 0;  // distances rd[0 .. b_done) are filled
   for (int b = 0; b < n; ++b) {
+    if (cached) {
+      rd[b] = b == host ? r_host : dist_to(xyz, b, x, y, z);
+      b_done = b + 1;
+    }
     if (b == host) continue;
     const double inv = inv_r[row_h + b];
     if (inv == 0.0) continue;
-    const double mu = clamp1((r_host - dist_to(xyz, b, x, y, z)) * inv);
+    const double r_b = cached ? rd[b] : dist_to(xyz, b, x, y, z);
+    const double mu = clamp1((r_host - r_b) * inv);
     const double nu = mu + a_ij[row_h + b] * (1.0 - mu * mu);
     const double s = step3(nu);
     p_host *= s;
@@ -54,12 +67,14 @@ __device__ double becke_weight(int n, const double* __restrict__ xyz, const doub
     if (1.0 - s > 1e-17) ++n_active;
   }
   if (n_active == 0) return 1.0;
+  if (cached)  // pass 1 ran to the end (it returns early only with p_host < 1e-20)
+    for (int b = b_done; b < n; ++b) rd[b] = dist_to(xyz, b, x, y, z);
   double sum_p = p_host;
   for (int a = 0; a < n; ++a) {
     if (a == host) continue;
     const double inv_ha = inv_r[row_h + a];
     if (inv_ha == 0.0) continue;
-    const double r_a = dist_to(xyz, a, x, y, z);
+    const double r_a = cached ? rd[a] : dist_to(xyz, a, x, y, z);
     const double mu_ha = clamp1((r_host - r_a) * inv_ha);
     const double s_ha = step3(mu_ha + a_ij[row_h + a] * (1.0 - mu_ha * mu_ha));
     if (!(1.0 - s_ha > 1e-17)) continue;
@@ -70,7 +85,7 @@ __device__ double becke_weight(int n, const double* __restrict__ xyz, const doub
       if (b == host || b == a) continue;
       const double inv = inv_r[row_a + b];
       if (inv == 0.0) continue;
-      const double mu = clamp1((r_a - dist_to(xyz, b, x, y, z)) * inv);
+      const double mu = clamp1((r_a - (cached ? rd[b] : dist_to(xyz, b, x, y, z))) * inv);
       p_a *= step3(mu + a_ij[row_a + b] * (1.0 - mu * mu));
       if (p_a < 1e-20) break;
     }
@@ -80,7 +95,8 @@ __device__ double becke_weight(int n, const double* __restrict__ xyz, const doub
 }
 
 // One CTA per radial shell: expand, weight, flag, count kept points.
-__global__ void __launch_bounds__(256) shell_points_kernel(GridBuildArgs a) {
+constexpr int kShellThreads = 256;
+__global__ void __launch_bounds__(kShellThreads) shell_points_kernel(GridBuildArgs a) {
   const int sh = blockIdx.x;
   const RadialShellDev rs = a.shells[sh];
   const double ax = a.xyz[3 * rs.atom], ay = a.xyz[3 * rs.atom + 1], az = a.xyz[3 * rs.atom + 2];
@@ -176,7 +192,7 @@ __global__ void __launch_bounds__(256) compact_kernel(GridBuildArgs a, const lon
 }  // namespace
 
 cudaError_t launch_grid_expand(const GridBuildArgs& a, int n_shells, cudaStream_t st) {
-  shell_points_kernel<<<n_shells, 256, 0, st>>>(a);
+  shell_points_kernel<<<n_shells, kShellThreads, 0, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -263,15 +263,23 @@ __device__ __forceinline__ size_t img_tile(int p, int ib, int kb2, int n_ib) {
   return (((size_t)p * n_ib + ib) * 2 + kb2) * 16384;
 }
 
-__device__ __forceinline__ double cta_sum(double v, double* red_row) {
+// Three CTA-wide sums with one barrier: warp shuffles, then thread 0 adds the warps' partials in
+// order (the results are valid in thread 0).
+__device__ __forceinline__ void cta_sum3(double (&v)[3], double (*red)[kMT / 32]) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) red_row[threadIdx.x >> 5] = v;
+  for (int q = 0; q < 3; ++q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v[q];
+  }
   __syncthreads();
-  double s = 0;
   if (threadIdx.x == 0)
-    for (int k = 0; k < kMT / 32; ++k) s += red_row[k];
-  return s;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      double s = 0;
+      for (int k = 0; k < kMT / 32; ++k) s += red[q][k];
+      v[q] = s;
+    }
 }
 
 }  // namespace
@@ -671,16 +679,15 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
     }
     __syncthreads();
     {
-      const double es = cta_sum(e_loc, red[0]);
-      const double nas = cta_sum(na_loc, red[1]);
-      const double nbs = cta_sum(nb_loc, red[2]);
+      double sums[3] = {e_loc, na_loc, nb_loc};
+      cta_sum3(sums, red);
       if (tid == 0) {
-        A.batch_red[3 * (size_t)b] = es;
-        A.batch_red[3 * (size_t)b + 1] = nas;
-        A.batch_red[3 * (size_t)b + 2] = nbs;
+        A.batch_red[3 * (size_t)b] = sums[0];
+        A.batch_red[3 * (size_t)b + 1] = sums[1];
+        A.batch_red[3 * (size_t)b + 2] = sums[2];
       }
     }
-    // per-point shares only: no GEMM2 and no V update (cta_sum's barrier follows the last reads of
+    // per-point shares only: no GEMM2 and no V update (cta_sum3's barrier follows the last reads of
     // the stage and of coef, so the next batch may reuse them)
     if (A.shares_only) continue;
 
