@@ -26,13 +26,28 @@ __device__ __forceinline__ void split3_bf16(float x, __nv_bfloat16& hi, __nv_bfl
   lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
 }
 
+__device__ __forceinline__ uint32_t bf162_bits(__nv_bfloat162 v) {
+  return (uint32_t)__bfloat16_as_ushort(v.x) | ((uint32_t)__bfloat16_as_ushort(v.y) << 16);
+}
+
+// split3_bf16 of eight values, two at a time (one paired conversion per piece): the same pieces,
+// packed in order (value 2k in the low half of word k)
 __device__ __forceinline__ void pack8x3(const float* v, uint4& hi, uint4& mid, uint4& lo) {
-  __nv_bfloat16 h[8], m[8], l[8];
+  uint32_t h[4], md[4], l[4];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) split3_bf16(v[k], h[k], m[k], l[k]);
-  hi = make_uint4(pack_bf16x2(h[0], h[1]), pack_bf16x2(h[2], h[3]), pack_bf16x2(h[4], h[5]), pack_bf16x2(h[6], h[7]));
-  mid = make_uint4(pack_bf16x2(m[0], m[1]), pack_bf16x2(m[2], m[3]), pack_bf16x2(m[4], m[5]), pack_bf16x2(m[6], m[7]));
-  lo = make_uint4(pack_bf16x2(l[0], l[1]), pack_bf16x2(l[2], l[3]), pack_bf16x2(l[4], l[5]), pack_bf16x2(l[6], l[7]));
+  for (int k = 0; k < 4; ++k) {
+    const float a = v[2 * k], b = v[2 * k + 1];
+    const __nv_bfloat162 h2 = __floats2bfloat162_rn(a, b);
+    const float ra = __fsub_rn(a, __low2float(h2)), rb = __fsub_rn(b, __high2float(h2));
+    const __nv_bfloat162 m2 = __floats2bfloat162_rn(ra, rb);
+    const __nv_bfloat162 l2 = __floats2bfloat162_rn(__fsub_rn(ra, __low2float(m2)), __fsub_rn(rb, __high2float(m2)));
+    h[k] = bf162_bits(h2);
+    md[k] = bf162_bits(m2);
+    l[k] = bf162_bits(l2);
+  }
+  hi = make_uint4(h[0], h[1], h[2], h[3]);
+  mid = make_uint4(md[0], md[1], md[2], md[3]);
+  lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
 // Fixed-point split of |x| < 1 (a double-float hi + lo) into four pieces that are multiples of

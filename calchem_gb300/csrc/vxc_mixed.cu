@@ -23,7 +23,8 @@
 //       i + j = 2 and 3) are at least 2^8 smaller and accumulate separately, over up to 16 K
 //       blocks; longer contractions are combined into a fourth accumulator;
 //   (D) epilogue: each thread owns one point (its TMEM lane); T = hh + corrections is kept as a
-//       double-float; the planes stream through a ring of shared-memory buffers by bulk copies (a
+//       double-float, times the density row's scale 2^f (the point's scale 2^e_g multiplies the
+//       finished sums); the planes stream through a ring of shared-memory buffers by bulk copies (a
 //       buffer is refilled once every warp has arrived on its release barrier) and rho,
 //       grad rho = 2 sum grad Phi T are compensated sums of double-float products;
 //   (E) the functional per point (double-float for the closed-shell codes 0-5 above 1e-12, FP64
@@ -92,6 +93,19 @@ struct MixCfg {
 constexpr int kOffDensInStage = 65536;
 static_assert(24 + 8 * kRing + 8 <= 64, "misc area holds the barriers, the TMEM slot, the batch index and the planes' base");
 static_assert(64 + 8 * kRing <= 96, "the ring's release barriers follow at +64");
+
+// 2^k as a float: exact for -149 <= k <= 127 (a normal number for k >= -126)
+__device__ __forceinline__ float pow2f(int k) {
+  return (k >= -126 && k <= 127) ? __int_as_float((k + 127) << 23) : ldexpf(1.f, k);
+}
+
+// (double)x for a normal float x, by moving its sign, exponent and mantissa fields: the same value
+// as the conversion, with integer instructions only
+__device__ __forceinline__ double normal_f32_to_f64(float x) {
+  const uint32_t u = __float_as_uint(x);
+  const uint32_t em = u & 0x7FFFFFFFu;
+  return __hiloint2double((int)((u & 0x80000000u) | ((em >> 3) + ((1023u - 127u) << 20))), (int)(em << 29));
+}
 
 // (A) AO values and gradients in double-float.  Planes p = 0..3 (phi, d/dx, d/dy, d/dz) hold the
 // FP32 hi parts at planes + p * P and the lo parts, rounded to BF16 (lo <= ulp(hi) / 2, so hi + lo
@@ -312,7 +326,7 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
   uint64_t* ring_free = reinterpret_cast<uint64_t*>(base + kOffMisc + 64);
   int* s_eg = reinterpret_cast<int*>(base + kOffEg);
   df32* s_tab = reinterpret_cast<df32*>(base + kOffTab);
-  int* s_fx = reinterpret_cast<int*>(base + kOffFx);
+  float* s_fs = reinterpret_cast<float*>(base + kOffFx);  // 2^f of the chunk's density rows
 
   const int tid = threadIdx.x, warp = tid >> 5;
   const int g = tid & 127, h = tid >> 7;
@@ -451,9 +465,9 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
       CompSum sr, sgx, sgy, sgz;
       const uint32_t idesc = idesc_bf16_f32(128, kNc);
       for (int nc = 0; nc < m && !failed; nc += kNc) {
-        // the density rows' power-of-two exponents for this chunk's AOs (read in the epilogue; the
+        // the density rows' power-of-two scales 2^f for this chunk's AOs (read in the epilogue; the
         // barriers of the K loop order the writes before it)
-        if (tid < kNc) s_fx[tid] = nc + tid < m ? fexp[s_ao[nc + tid]] : 0;
+        if (tid < kNc) s_fs[tid] = pow2f(nc + tid < m ? fexp[s_ao[nc + tid]] : 0);
         for (int kb = 0; kb < nkb; ++kb) {
           if (tid == 0) {  // A operand of this K block: four 16 KB tiles
             mbar_arrive_expect_tx(tbar, 65536);
@@ -558,7 +572,8 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
                 const int nu = nc + c0 + j;
                 if (ok && nu < m) {
                   df32 t = first_group ? two_sum(a[j], bb[j]) : df_add_f(two_sum(cc[j], a[j]), bb[j]);
-                  t = df_ldexp(t, eg + s_fx[c0 + j]);
+                  const float sc = s_fs[c0 + j];
+                  t = df32{t.hi * sc, t.lo * sc};
                   const int o = (4 * h + j) * 128 + g;  // row within the step, point g
                   acc_prod(sr, df32{buf[o], __bfloat162float(lbuf[o])}, t);
                   acc_prod(sgx, df32{buf[1024 + o], __bfloat162float(lbuf[1024 + o])}, t);
@@ -585,7 +600,9 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
           __syncthreads();
         }
       }
-      double acc[4] = {sr.value(), sgx.value(), sgy.value(), sgz.value()};
+      // the point's scale 2^e_g, applied to the sums (exact)
+      const double seg = ldexp(1.0, eg);
+      double acc[4] = {sr.value() * seg, sgx.value() * seg, sgy.value() * seg, sgz.value() * seg};
       if (failed) break;
       for (int k = 0; k < 4; ++k) dens[h][k][g] = acc[k];
       __syncthreads();
@@ -697,7 +714,7 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
     const uint32_t idesc2 = idesc_bf16_f32(128, 128);
     // 8 points (c16 * 8 ..) of AO row mu: Phi^T and Z^T, three BF16 pieces each
     const float* const planes = batch_planes();
-    auto image8 = [&](int s, int mu, int c16, uint4 (&p3)[3], uint4 (&z3)[3]) {
+    auto image8 = [&](const float (&cz)[4][8], int mu, int c16, uint4 (&p3)[3], uint4 (&z3)[3]) {
       const size_t o = (size_t)mu * 128 + c16 * 8;
       float ph[8], zz[8];
       // the hi planes' last use in the batch: streaming loads (first in line for eviction)
@@ -715,9 +732,7 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
       const float dzv[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        const int gg = c16 * 8 + k;
-        zz[k] = coef[4 * s][gg] * ph[k] + coef[4 * s + 1][gg] * dxv[k] + coef[4 * s + 2][gg] * dyv[k] +
-                coef[4 * s + 3][gg] * dzv[k];
+        zz[k] = cz[0][k] * ph[k] + cz[1][k] * dxv[k] + cz[2][k] * dyv[k] + cz[3][k] * dzv[k];
       }
       pack8x3(ph, p3[0], p3[1], p3[2]);
       pack8x3(zz, z3[0], z3[1], z3[2]);
@@ -760,7 +775,7 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
             if (j < m && (I != J || i >= j) && fabsf(wv[jj]) >= 1e-13f) {
               const int aj = s_ao[j];
               const int r = ai < aj ? ai : aj, c = ai < aj ? aj : ai;
-              atomicAdd(&V[(size_t)r * n + c], (double)wv[jj]);
+              atomicAdd(&V[(size_t)r * n + c], normal_f32_to_f64(wv[jj]));
             }
           }
         }
@@ -774,10 +789,15 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
         // one tile pair: the six image tiles of each 64-point K half are built in the stage and
         // consumed there (slots 0..2 Phi^T, 3..5 Z^T), with no global round trip
         for (int kb2 = 0; kb2 < 2 && !failed; ++kb2) {
+          float cz[4][8];  // this thread's 8 points (the same in every row)
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) cz[k][kk] = coef[4 * s + k][(kb2 * 8 + (tid & 7)) * 8 + kk];
           for (int e = tid; e < m * 8; e += kMT) {
             const int mu = e >> 3, cc = e & 7;
             uint4 p3[3], z3[3];
-            image8(s, mu, kb2 * 8 + cc, p3, z3);
+            image8(cz, mu, kb2 * 8 + cc, p3, z3);
             const uint32_t sw = sw128(mu, cc);
 #pragma unroll
             for (int t = 0; t < 3; ++t) {
@@ -799,10 +819,15 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
         drain(V, 0, 0);
         continue;
       }
+      float cz[4][8];  // this thread's 8 points (the same in every row)
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) cz[k][kk] = coef[4 * s + k][(tid & 15) * 8 + kk];
       for (int e = tid; e < m * 16; e += kMT) {
         const int mu = e >> 4, c16 = e & 15;
         uint4 p3[3], z3[3];
-        image8(s, mu, c16, p3, z3);
+        image8(cz, mu, c16, p3, z3);
         const int ib = mu >> 7, r = mu & 127, kb2 = c16 >> 3, cc = c16 & 7;
         const uint32_t sw = sw128(r, cc);
 #pragma unroll
