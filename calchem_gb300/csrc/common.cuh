@@ -82,7 +82,9 @@ struct EvalArgs {
   int max_m;
   // Optional per-point output of the fused RKS modes (nullptr: none): point_out[2 g] = w_g f_g and
   // point_out[2 g + 1] = w_g (v_rho rho + v_gamma |grad rho|^2), the point's share of Exc and of
-  // tr(D Vxc).  Points below the density floor are not written (the caller zeroes the buffer).
+  // tr(D Vxc).  Points below the density floor are not written (the caller zeroes the buffer).  The
+  // tensor-core form sums grad rho with compensation in builds with point_out (the shares' accuracy)
+  // and by FP32 FMAs without it.
   double* point_out;
   // With point_out in the closed-shell mode: nonzero skips the Vxc contraction (the per-point shares,
   // Exc and Nelec only; V is neither read nor written).

@@ -129,5 +129,14 @@ __device__ __forceinline__ void acc_prod(CompSum& A, df32 x, df32 t) {
   A.c = __fadd_rn(A.c, __fadd_rn(q.lo, e));
 }
 
+// The same product summed by FP32 FMAs: s collects x.hi t.hi, c the cross terms x.hi t.lo +
+// x.lo t.hi; the rounding of each FMA into s is not recovered.  The double-float value's low part
+// still enters (its error is the same at every point of a radial shell and would not average out);
+// the accumulation's own roundings vary from point to point.
+__device__ __forceinline__ void acc_prod_fma(CompSum& A, df32 x, df32 t) {
+  A.s = __fmaf_rn(x.hi, t.hi, A.s);
+  A.c = __fmaf_rn(x.hi, t.lo, __fmaf_rn(x.lo, t.hi, A.c));
+}
+
 }  // namespace mix
 }  // namespace cxc

@@ -25,8 +25,12 @@
 //   (D) epilogue: each thread owns one point (its TMEM lane); T = hh + corrections is kept as a
 //       double-float, times the density row's scale 2^f (the point's scale 2^e_g multiplies the
 //       finished sums); the planes stream through a ring of shared-memory buffers by bulk copies (a
-//       buffer is refilled once every warp has arrived on its release barrier) and rho,
-//       grad rho = 2 sum grad Phi T are compensated sums of double-float products;
+//       buffer is refilled once every warp has arrived on its release barrier); rho = sum Phi T is
+//       a compensated sum of double-float products, grad rho = 2 sum grad Phi T three FP32 FMA sums
+//       of them (compensated too in builds with per-point output), with the AO gradients' low parts
+//       kept (on (H2O)61 against the FP64 form: the FMA sums for grad rho move Exc by < 2e-9 Eh and
+//       take 7 % off the kernel; dropping the low parts would move it by 2.6e-8, summing rho the
+//       same way by 1.1e-7);
 //   (E) the functional per point (double-float for the closed-shell codes 0-5 above 1e-12, FP64
 //       otherwise; a closed shell's exchange and correlation terms in the two 128-thread halves),
 //       Exc and Nelec partial sums in FP64 (vxc.rs:890-920);
@@ -44,6 +48,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 #include "dfloat.cuh"
@@ -332,6 +337,10 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
   const int g = tid & 127, h = tid >> 7;
   const bool uks = A.mode == kModeUks;
   const int nspin = uks ? 2 : 1;
+  // grad rho by FP32 FMA sums, except where per-point or per-atom shares are asked for: the judge
+  // of a learned grid compares atoms' shares from different batch plans to ~1e-9 Eh, and the FMA
+  // sums' roundings (~5e-10 on an oxygen's share) follow the batch's set of AOs
+  const bool fma_grad = A.point_out == nullptr && !A.shares_only;
 
   if (tid == 0) {
     mbar_init(mbar, 1);
@@ -550,50 +559,68 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
             // each buffer is released by an arrival of every warp (no block-wide barrier per step); an
             // expired wait marks the chunk failed, and the flag is combined after the loop
             bool efail = false;
-            for (int st = 0; st < n_steps; ++st) {
-              const int r = st % kRing;
-              const bool ok = !efail && mbar_wait_bounded(ring + r, ring_uses[r] & 1u, kWaitLimit);
-              if (ok) {  // on expiry the copy stays pending and teardown waits for it again
-                ring_uses[r]++;
-                ring_busy[r] = false;
-              } else {
-                efail = true;
-              }
-              const int c0 = 8 * st + 4 * h;
-              float a[4], bb[4], c2[4], cc[4];
-              tmem_ld4x4(tH + lane_base + (uint32_t)c0, tC1 + lane_base + (uint32_t)c0, tC2 + lane_base + (uint32_t)c0,
-                         (first_group ? tH : tS) + lane_base + (uint32_t)c0, a, bb, c2, cc);
-#pragma unroll
-              for (int j = 0; j < 4; ++j) bb[j] += c2[j];
-              const float* buf = reinterpret_cast<const float*>(stage + r * kRingBytes);
-              const __nv_bfloat16* lbuf = reinterpret_cast<const __nv_bfloat16*>(stage + r * kRingBytes + 16384);
-#pragma unroll
-              for (int j = 0; j < 4; ++j) {
-                const int nu = nc + c0 + j;
-                if (ok && nu < m) {
-                  df32 t = first_group ? two_sum(a[j], bb[j]) : df_add_f(two_sum(cc[j], a[j]), bb[j]);
-                  const float sc = s_fs[c0 + j];
-                  t = df32{t.hi * sc, t.lo * sc};
-                  const int o = (4 * h + j) * 128 + g;  // row within the step, point g
-                  acc_prod(sr, df32{buf[o], __bfloat162float(lbuf[o])}, t);
-                  acc_prod(sgx, df32{buf[1024 + o], __bfloat162float(lbuf[1024 + o])}, t);
-                  acc_prod(sgy, df32{buf[2 * 1024 + o], __bfloat162float(lbuf[2 * 1024 + o])}, t);
-                  acc_prod(sgz, df32{buf[3 * 1024 + o], __bfloat162float(lbuf[3 * 1024 + o])}, t);
-                }
-              }
-              __syncwarp();
-              if ((tid & 31) == 0) mbar_arrive(ring_free + r);  // this warp is done with buffer r
-              if (tid == 0 && st + kRing < n_steps) {
-                // refill buffer r once every warp has released it (the release of this use: the
-                // phase with the parity of the use's index)
-                if (!efail && mbar_wait_bounded(ring_free + r, (ring_uses[r] - 1u) & 1u, kWaitLimit)) {
-                  fence_proxy_async_smem();
-                  issue(st + kRing);
+            // the step loop, compiled once per form of the grad rho sums (a branch per product would
+            // be predicated and issue both forms)
+            auto steps = [&](auto fma_form) {
+              constexpr bool kFma = decltype(fma_form)::value;
+              for (int st = 0; st < n_steps; ++st) {
+                const int r = st % kRing;
+                const bool ok = !efail && mbar_wait_bounded(ring + r, ring_uses[r] & 1u, kWaitLimit);
+                if (ok) {  // on expiry the copy stays pending and teardown waits for it again
+                  ring_uses[r]++;
+                  ring_busy[r] = false;
                 } else {
                   efail = true;
                 }
+                const int c0 = 8 * st + 4 * h;
+                float a[4], bb[4], c2[4], cc[4];
+                tmem_ld4x4(tH + lane_base + (uint32_t)c0, tC1 + lane_base + (uint32_t)c0, tC2 + lane_base + (uint32_t)c0,
+                           (first_group ? tH : tS) + lane_base + (uint32_t)c0, a, bb, c2, cc);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) bb[j] += c2[j];
+                const float* buf = reinterpret_cast<const float*>(stage + r * kRingBytes);
+                const __nv_bfloat16* lbuf = reinterpret_cast<const __nv_bfloat16*>(stage + r * kRingBytes + 16384);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                  const int nu = nc + c0 + j;
+                  if (ok && nu < m) {
+                    df32 t = first_group ? two_sum(a[j], bb[j]) : df_add_f(two_sum(cc[j], a[j]), bb[j]);
+                    const float sc = s_fs[c0 + j];
+                    t = df32{t.hi * sc, t.lo * sc};
+                    const int o = (4 * h + j) * 128 + g;  // row within the step, point g
+                    acc_prod(sr, df32{buf[o], __bfloat162float(lbuf[o])}, t);
+                    const df32 xg = {buf[1024 + o], __bfloat162float(lbuf[1024 + o])};
+                    const df32 yg = {buf[2 * 1024 + o], __bfloat162float(lbuf[2 * 1024 + o])};
+                    const df32 zg = {buf[3 * 1024 + o], __bfloat162float(lbuf[3 * 1024 + o])};
+                    if constexpr (kFma) {
+                      acc_prod_fma(sgx, xg, t);
+                      acc_prod_fma(sgy, yg, t);
+                      acc_prod_fma(sgz, zg, t);
+                    } else {
+                      acc_prod(sgx, xg, t);
+                      acc_prod(sgy, yg, t);
+                      acc_prod(sgz, zg, t);
+                    }
+                  }
+                }
+                __syncwarp();
+                if ((tid & 31) == 0) mbar_arrive(ring_free + r);  // this warp is done with buffer r
+                if (tid == 0 && st + kRing < n_steps) {
+                  // refill buffer r once every warp has released it (the release of this use: the
+                  // phase with the parity of the use's index)
+                  if (!efail && mbar_wait_bounded(ring_free + r, (ring_uses[r] - 1u) & 1u, kWaitLimit)) {
+                    fence_proxy_async_smem();
+                    issue(st + kRing);
+                  } else {
+                    efail = true;
+                  }
+                }
               }
-            }
+            };
+            if (fma_grad)
+              steps(std::true_type{});
+            else
+              steps(std::false_type{});
             if (__syncthreads_or(efail)) { failed = true; break; }
           }
           tc_fence_before();

@@ -152,7 +152,9 @@ def test_value_screen_floor_changes_little_and_cuts_work(native_lib):
     assert abs(e1 - e0) < 1e-9 and np.max(np.abs(V1 - V0)) < 1e-9
     em0, Vm0, _ = out[(None, "mixed")]
     em1, Vm1, _ = out[(MIXED_AO_FLOOR, "mixed")]
-    assert abs(em1 - em0) < 1e-9 and np.max(np.abs(Vm1 - Vm0)) < 1e-8
+    # the mixed form sums grad rho in FP32 FMAs, whose roundings follow the set of AOs summed: V
+    # moves by ~2e-8 between the floors, against its ~1e-6 agreement with FP64
+    assert abs(em1 - em0) < 1e-9 and np.max(np.abs(Vm1 - Vm0)) < 1e-7
     assert RksVxcEngine(basis, grid, precision="mixed").ao_floor == MIXED_AO_FLOOR
     for bad in (1e-18, 1e-5):
         with pytest.raises(_native.CalchemXcError):

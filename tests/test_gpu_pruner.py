@@ -80,8 +80,10 @@ def test_device_atom_sums_match_the_per_point_shares(lib, precision, tol):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_build_with_shares_matches_the_build_and_the_share_engine(lib, precision):
-    """evaluate_with_shares: the same Exc, Nelec and Vxc as evaluate, and the same per-atom shares as a
-    shares-only evaluation of the same points; the judge gives the same verdict with them."""
+    """evaluate_with_shares: the same Exc, Nelec and Vxc as evaluate (the tensor-core form: the same up
+    to the rounding of grad rho, which plain builds sum by FP32 FMAs and builds with shares with
+    compensation), and the same per-atom shares as a shares-only evaluation of the same points; the
+    judge gives the same verdict with them."""
     mol = workloads.water_cluster(4, 6)
     basis = BasisSet.from_name("6-31g(d)", mol)
     D = workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, 9)
@@ -92,8 +94,11 @@ def test_build_with_shares_matches_the_build_and_the_share_engine(lib, precision
     e0, V0 = eng.evaluate(basis, lg.grid, "b3lyp", D)
     n0 = eng.last_nelec
     e1, V1, E, T = eng.evaluate_with_shares(basis, lg.grid, "b3lyp", D)
-    assert e1 == e0 and eng.last_nelec == n0
-    assert np.max(np.abs(V1 - V0)) < 1e-12
+    assert eng.last_nelec == n0
+    if precision == "fp64":
+        assert e1 == e0 and np.max(np.abs(V1 - V0)) < 1e-12
+    else:
+        assert abs(e1 - e0) < 2e-9 and np.max(np.abs(V1 - V0)) < 1e-7
     assert abs(E.sum() - e1) < 1e-10
     share = pruner.ShareEngine(basis, lg.grid, n)
     Es, Ts = share.shares(D, "b3lyp", precision)
