@@ -186,6 +186,26 @@ __device__ __forceinline__ void tmem_ld4x4(uint32_t t0, uint32_t t1, uint32_t t2
   }
 }
 
+// Three 4-column loads (from three TMEM addresses of the thread's lane) completed by one wait.
+__device__ __forceinline__ void tmem_ld4x3(uint32_t t0, uint32_t t1, uint32_t t2, float* a, float* b, float* c) {
+  uint32_t r[12];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%12];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%4,%5,%6,%7}, [%13];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%8,%9,%10,%11}, [%14];\n\t"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11])
+      : "r"(t0), "r"(t1), "r"(t2)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    a[i] = __uint_as_float(r[i]);
+    b[i] = __uint_as_float(r[4 + i]);
+    c[i] = __uint_as_float(r[8 + i]);
+  }
+}
+
 // Each thread of the warp writes 16 consecutive FP32 columns of its TMEM lane.
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float* v) {
   asm volatile(

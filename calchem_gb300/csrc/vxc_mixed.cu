@@ -559,10 +559,10 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
             // each buffer is released by an arrival of every warp (no block-wide barrier per step); an
             // expired wait marks the chunk failed, and the flag is combined after the loop
             bool efail = false;
-            // the step loop, compiled once per form of the grad rho sums (a branch per product would
-            // be predicated and issue both forms)
-            auto steps = [&](auto fma_form) {
-              constexpr bool kFma = decltype(fma_form)::value;
+            // the step loop, compiled once per form of the grad rho sums and per K group kind (a branch
+            // per product would be predicated and issue both forms)
+            auto steps = [&](auto fma_form, auto first_form) {
+              constexpr bool kFma = decltype(fma_form)::value, kFirst = decltype(first_form)::value;
               for (int st = 0; st < n_steps; ++st) {
                 const int r = st % kRing;
                 const bool ok = !efail && mbar_wait_bounded(ring + r, ring_uses[r] & 1u, kWaitLimit);
@@ -573,9 +573,12 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
                   efail = true;
                 }
                 const int c0 = 8 * st + 4 * h;
+                const uint32_t tl = lane_base + (uint32_t)c0;
                 float a[4], bb[4], c2[4], cc[4];
-                tmem_ld4x4(tH + lane_base + (uint32_t)c0, tC1 + lane_base + (uint32_t)c0, tC2 + lane_base + (uint32_t)c0,
-                           (first_group ? tH : tS) + lane_base + (uint32_t)c0, a, bb, c2, cc);
+                if constexpr (kFirst)
+                  tmem_ld4x3(tH + tl, tC1 + tl, tC2 + tl, a, bb, c2);
+                else
+                  tmem_ld4x4(tH + tl, tC1 + tl, tC2 + tl, tS + tl, a, bb, c2, cc);
 #pragma unroll
                 for (int j = 0; j < 4; ++j) bb[j] += c2[j];
                 const float* buf = reinterpret_cast<const float*>(stage + r * kRingBytes);
@@ -584,7 +587,11 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
                 for (int j = 0; j < 4; ++j) {
                   const int nu = nc + c0 + j;
                   if (ok && nu < m) {
-                    df32 t = first_group ? two_sum(a[j], bb[j]) : df_add_f(two_sum(cc[j], a[j]), bb[j]);
+                    df32 t;
+                    if constexpr (kFirst)
+                      t = two_sum(a[j], bb[j]);
+                    else
+                      t = df_add_f(two_sum(cc[j], a[j]), bb[j]);
                     const float sc = s_fs[c0 + j];
                     t = df32{t.hi * sc, t.lo * sc};
                     const int o = (4 * h + j) * 128 + g;  // row within the step, point g
@@ -617,10 +624,17 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
                 }
               }
             };
-            if (fma_grad)
-              steps(std::true_type{});
-            else
-              steps(std::false_type{});
+            if (fma_grad) {
+              if (first_group)
+                steps(std::true_type{}, std::true_type{});
+              else
+                steps(std::true_type{}, std::false_type{});
+            } else {
+              if (first_group)
+                steps(std::false_type{}, std::true_type{});
+              else
+                steps(std::false_type{}, std::false_type{});
+            }
             if (__syncthreads_or(efail)) { failed = true; break; }
           }
           tc_fence_before();
