@@ -32,7 +32,7 @@
 //       take 7 % off the kernel; dropping the low parts would move it by 2.6e-8, summing rho the
 //       same way by 1.1e-7);
 //   (E) the functional per point (double-float for the closed-shell codes 0-5 above 1e-12, FP64
-//       otherwise; a closed shell's exchange and correlation terms in the two 128-thread halves),
+//       otherwise; a closed shell's two parts of xc_eval_cs_df in the two 128-thread halves),
 //       Exc and Nelec partial sums in FP64 (vxc.rs:890-920);
 //   (F) GEMM2  W = Z^T Phi + Phi^T Z  (Z = (w v_rho / 2) Phi + (w u) . grad Phi) on lower
 //       128 x 128 AO tile pairs, K = 64 points per step: Phi and Z split into three BF16 pieces
@@ -657,8 +657,9 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
     if (failed) break;
 
     // (E) functional, one thread per point (threads with h == 0).  The closed-shell functional is
-    // split between the halves: exchange terms in threads h == 0, correlation terms in threads
-    // h == 1 (passed through dens, idle until the image pass), summed as xc_eval_cs_fast sums them.
+    // split between the halves: part 0 of xc_eval_cs_df (exchange and VWN) in threads h == 0, part 1
+    // in threads h == 1 (passed through dens, idle until the image pass), summed as xc_eval_cs_fast
+    // sums them.
     XcCs xpart{0.0, 0.0, 0.0};
     if (!uks && A.mode != kModeFxc) {
       const double ra = spin_rho[0][0];

@@ -147,8 +147,9 @@ __device__ __forceinline__ void pw92_df(df32 rs, const df32* tab, df32& g, df32&
 }
 
 // xc_eval_cs for codes 0-5 (SVWN5, BLYP, PBE, B3LYP, B3LYP5, PBE0) at spin density r and
-// gamma_ss g, for r + r >= kDfRhoMin: part 0 the exchange terms (Slater, B88, PBE exchange), part 1
-// the correlation terms (VWN, LYP, PBE correlation); the functional is their sum.  tab: the
+// gamma_ss g, for r + r >= kDfRhoMin: part 0 the exchange terms (Slater, B88, PBE exchange) and VWN,
+// part 1 the other correlation terms (LYP, PBE correlation), which balances the two parts' work for
+// B3LYP; the functional is their sum.  tab: the
 // 2^(-j/64) table of df_exp_neg.
 __device__ __forceinline__ XcCsDf xc_eval_cs_df(int code, df32 r, df32 g, const df32* tab, int part) {
   using namespace dfo;
@@ -193,7 +194,7 @@ __device__ __forceinline__ XcCsDf xc_eval_cs_df(int code, df32 r, df32 g, const 
     o.vr += sc * (dfc((4.0 / 3.0) * kCsCxu) * rho13 * fx + exl * dfx * (dfc(-(8.0 / 3.0)) * s2 / rho));
     o.vg += sc * (2.f * (exl * dfx / den_s2));
   }
-  if (cpart && (code == 0 || code == 3 || code == 4)) {  // VWN5 / VWN_RPA, paramagnetic channel
+  if (xpart && (code == 0 || code == 3 || code == 4)) {  // VWN5 / VWN_RPA, paramagnetic channel (part 0)
     const df32 sc = code == 0 ? df32{1.f, 0.f} : dfc(0.19);
     const VwnDf ch = code == 3 ? vwn_df(kVwnRpaPara) : vwn_df(kVwn5Para);
     const df32 x = df_sqrt(dfc(kCsRsK) / rho13);

@@ -457,8 +457,8 @@ __global__ void __launch_bounds__(kGM, 2) xc_grad_mixed_kernel(DevGrid G, GradAr
     if (failed) break;
 
     // (C) functional, one thread per point: coef rows (w v_rho_a, w u_a, w v_rho_b, w u_b, f).  A
-    // closed shell's functional is split between the halves: exchange terms in threads h == 0,
-    // correlation terms in threads h == 1 (passed through dens), summed as xc_eval_cs_fast sums them.
+    // closed shell's functional is split between the halves: part 0 of xc_eval_cs_df in threads
+    // h == 0, part 1 in threads h == 1 (passed through dens), summed as xc_eval_cs_fast sums them.
     XcCs xpart{0.0, 0.0, 0.0};
     if (A.closed) {
       const double rpa = fmax(spin_rho[0][0], 0.0);
