@@ -799,7 +799,11 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
     // drain: lane = AO row i of tile I, this group's 64 columns of tile J
     auto drain = [&](double* V, int I, int J) {
       const int i = I + g;
+      const int row0 = I + 32 * (warp & 3);  // the warp's first row (its TMEM lanes)
       for (int c0 = h * 64; c0 < h * 64 + 64; c0 += 32) {
+        // a 32-column block none of whose entries the warp adds (columns beyond m, rows beyond m, or
+        // in the diagonal tile columns above every row of the warp) is skipped by the whole warp
+        if (J + c0 >= m || row0 >= m || (I == J && c0 > 32 * (warp & 3) + 31)) continue;
         float wv[32], wc[32];
         tmem_ld32(tW + lane_base + (uint32_t)c0, wv);
         tmem_ld32(tWc + lane_base + (uint32_t)c0, wc);
