@@ -65,10 +65,10 @@ RKS_WORKLOADS = {
 }
 # DRAM bytes (read + write) per launch of the quadrature kernel from one ncu capture of the workload's
 # timed build (profiles/); absent until a capture exists for the workload and precision.  The 61-water
-# build is too large for a full capture: its figure is the 12-water capture (1.267 GB, 1.325 GB of AO
-# cache) scaled by the AO-cache bytes (10.074 GB), the data that traffic grows with.
-NCU_TRAFFIC_BYTES = {("octane_b3lyp", "mixed"): 1.951e9, ("water12_b3lyp", "mixed"): 1.267e9,
-                     ("water61_b3lyp", "mixed"): 9.63e9}
+# build is too large for a full capture: its figure is the 12-water capture (1.229 GB, 1.325 GB of AO
+# cache) scaled by the AO-cache bytes (10.069 GB), the data that traffic grows with.
+NCU_TRAFFIC_BYTES = {("octane_b3lyp", "mixed"): 1.925e9, ("water12_b3lyp", "mixed"): 1.229e9,
+                     ("water61_b3lyp", "mixed"): 9.34e9}
 
 
 def parse():
