@@ -465,19 +465,25 @@ void ao_cache_decide(Entry& e) {
     cudaGetLastError();
     return;
   }
-  std::vector<long long> off(e.n_batches);
-  size_t total = 0;
-  for (int b = 0; b < e.n_batches; ++b) {
-    off[b] = (long long)total;
-    total += ao_cache_block_bytes(hb[b].m);
-  }
   size_t free_b = 0, tot_b = 0;
   if (cudaMemGetInfo(&free_b, &tot_b) != cudaSuccess) {
     cudaGetLastError();
     return;
   }
+  // the cache's limit: the cap, the grid's budget and the free device memory less 1 GiB; batches (in
+  // batch order) whose blocks fit within it get one (offset -1: evaluated every time)
+  const size_t reserve = (size_t)1 << 30;
   const size_t budget = e.mem_limit > e.bytes ? e.mem_limit - e.bytes : 0;  // within the grid's budget
-  if (total == 0 || total > ao_cache_cap() || total > budget || total + ((size_t)1 << 30) > free_b) return;
+  const size_t limit = std::min({ao_cache_cap(), budget, free_b > reserve ? free_b - reserve : (size_t)0});
+  std::vector<long long> off(e.n_batches, -1);
+  size_t total = 0;
+  for (int b = 0; b < e.n_batches; ++b) {
+    const size_t bb = ao_cache_block_bytes(hb[b].m);
+    if (total + bb > limit) continue;
+    off[b] = (long long)total;
+    total += bb;
+  }
+  if (total == 0) return;
   const bool ok = cudaMalloc(&e.d_ao_cache, total) == cudaSuccess &&
                   cudaMalloc(&e.d_ao_cache_off, off.size() * sizeof(long long)) == cudaSuccess &&
                   cudaMalloc(&e.d_ao_cache_ok, (size_t)e.n_batches * sizeof(int)) == cudaSuccess &&

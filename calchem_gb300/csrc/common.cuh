@@ -97,8 +97,9 @@ struct EvalArgs {
   int triplet;
   const double* fxc_coef;
   // Tensor-core form: the AO cache (nullptr: none).  Batch b's AO planes, packed GEMM1 operand and
-  // row exponents live at ao_cache + ao_cache_off[b] (ao_cache_block_bytes); ao_cache_ok[b] != 0
-  // once a launch has written them, and later launches read them instead of evaluating the AOs.
+  // row exponents live at ao_cache + ao_cache_off[b] (ao_cache_block_bytes; -1: the batch has no
+  // block and is evaluated in the CTA's slab every time); ao_cache_ok[b] != 0 once a launch has
+  // written them, and later launches read them instead of evaluating the AOs.
   unsigned char* ao_cache;
   const long long* ao_cache_off;
   int* ao_cache_ok;

@@ -418,9 +418,13 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
     const int nkb = (m + 63) / 64;
     for (int i = tid; i < m; i += kMT) s_ao[i] = G.batch_ao[bd.ao_start + i];
     // the batch's AO planes, packed operand and row exponents: in the AO cache when the grid has
-    // one (written by the first launch that reaches the batch, read by later ones), else in the
-    // CTA's scratch slab
+    // one with a block for this batch (written by the first launch that reaches the batch, read by
+    // later ones), else in the CTA's scratch slab -- with a cache, a batch without a block is laid
+    // out as a block at the slab's start (P <= P_slab, so it ends before the slab's image tiles)
     // (both layouts: the FP32 planes, then the BF16 planes, then the packed operand)
+    long long cache_off = -1;
+    if constexpr (kCache) cache_off = A.ao_cache_off[b];
+    const bool in_cache = cache_off >= 0;
     const size_t P = kCache ? (size_t)nkb * 64 * 128 : P_slab;  // floats per plane
     auto batch_planes = [&]() -> float* {
       if constexpr (kCache) return *reinterpret_cast<float* volatile*>(s_planes);
@@ -428,9 +432,9 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
     };
     bool cached = false;
     if constexpr (kCache) {
-      if (tid == 0) *s_planes = reinterpret_cast<float*>(A.ao_cache + A.ao_cache_off[b]);
+      if (tid == 0) *s_planes = in_cache ? reinterpret_cast<float*>(A.ao_cache + cache_off) : planes_slab;
       // the flag has the same value in every thread: only this CTA writes it, after the reads below
-      cached = *reinterpret_cast<volatile int*>(A.ao_cache_ok + b) != 0;
+      cached = in_cache && *reinterpret_cast<volatile int*>(A.ao_cache_ok + b) != 0;
       __syncthreads();
     }
     if (cached) {
@@ -442,7 +446,7 @@ __global__ void __launch_bounds__(kMT, MixCfg<kN>::kCtas) vxc_mixed_kernel(DevGr
       float* const planes = batch_planes();
       __nv_bfloat16* const lo_planes = reinterpret_cast<__nv_bfloat16*>(planes + 4 * P);
       unsigned char* const apack = reinterpret_cast<unsigned char*>(lo_planes + 4 * P);
-      int* const eg_cached = kCache ? reinterpret_cast<int*>(apack + (size_t)nkb * 65536) : nullptr;
+      int* const eg_cached = in_cache ? reinterpret_cast<int*>(apack + (size_t)nkb * 65536) : nullptr;
       const float vmax = ao_eval_df(G, bd, planes, lo_planes, P, nkb * 64, s_tab);
       {  // e_g: power-of-two exponent with max_mu |Phi[g][mu]| 2^-e_g < 1
         dens[0][0][g + 128 * h] = (double)vmax;  // scratch: the stage is idle

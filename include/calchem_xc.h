@@ -223,11 +223,12 @@ int calchem_xc_set_weights(uint64_t grid_id, const double* h_weights, int n_pts)
  * (crates/calchem-dft/src/vxc.rs:386-394, 600-716), the first tensor-core evaluation of a grid
  * allocates a cache of each batch's AO planes (FP32 + BF16 parts), packed GEMM1 operand and row
  * exponents (32 B per AO and point), the first launch to reach a batch fills its block, and later
- * evaluations read it instead of evaluating the AOs.  It is used when its size is within
+ * evaluations read it instead of evaluating the AOs.  Its size is limited by
  * CALCHEM_MAX_AO_GRID_BYTES (the reference's variable for its AO cache; default here 32 GiB, since
- * the cache lives in HBM where the reference's 2560 MiB default sizes host memory), within the
- * grid's memory budget (memory_limit_bytes of its upload or group) and within the free device
- * memory less 1 GiB; otherwise the AOs are evaluated every time.  enable = 0 waits for the device,
+ * the cache lives in HBM where the reference's 2560 MiB default sizes host memory), by the grid's
+ * memory budget (memory_limit_bytes of its upload or group) and by the free device memory less
+ * 1 GiB: the batches whose blocks fit within that limit, taken in batch order, are cached and the
+ * others evaluate their AOs every time (the reference caches all or nothing).  enable = 0 waits for the device,
  * frees the cache, disables it and drops a captured graph; enable = 1 allows it again (a no-op when
  * allowed, the default); -1 only reports its size in *bytes_out (0 when none).  Results are the
  * same with and without the cache. */

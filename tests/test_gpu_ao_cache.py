@@ -132,3 +132,38 @@ def test_per_point_shares_with_cache(octane):
     assert e1 == e2 == e3
     assert np.array_equal(p1, p2) and np.array_equal(p2, p3)
     assert abs(p1[0::2].sum() - e1) < 1e-9
+
+
+def test_partial_cache_equals_full_and_none(octane):
+    """With the cap below the cache's size, the batches whose blocks fit (in batch order) are cached
+    and the others evaluate their AOs in the CTA's slab: Exc and Nelec equal the full cache's and the
+    uncached form's bit for bit, the second (reading) evaluation included; Vxc to its atomics'
+    rounding."""
+    mol, basis, grid, D = octane
+    full = RksVxcEngine(basis, grid, precision="mixed")
+    e_full, V_full = full.evaluate(basis, grid, "b3lyp", D)
+    n_full = full.last_nelec
+    nbytes = full.ao_cache_bytes()
+    full.close()
+    assert nbytes > 0
+    old = os.environ.get("CALCHEM_MAX_AO_GRID_BYTES")
+    os.environ["CALCHEM_MAX_AO_GRID_BYTES"] = str(nbytes // 3)
+    try:
+        part = RksVxcEngine(basis, grid, precision="mixed")
+        e1, V1 = part.evaluate(basis, grid, "b3lyp", D)  # fills the cached batches' blocks
+        pbytes = part.ao_cache_bytes()
+        e2, V2 = part.evaluate(basis, grid, "b3lyp", D)  # reads them, evaluates the rest
+        n2 = part.last_nelec
+        part.close()
+    finally:
+        if old is None:
+            del os.environ["CALCHEM_MAX_AO_GRID_BYTES"]
+        else:
+            os.environ["CALCHEM_MAX_AO_GRID_BYTES"] = old
+    assert 0 < pbytes <= nbytes // 3
+    none = RksVxcEngine(basis, grid, precision="mixed")
+    none.set_ao_cache(False)
+    e3, V3 = none.evaluate(basis, grid, "b3lyp", D)
+    none.close()
+    assert e1 == e2 == e_full == e3 and n2 == n_full
+    assert max(np.max(np.abs(V1 - V_full)), np.max(np.abs(V2 - V_full)), np.max(np.abs(V3 - V_full))) < 1e-13
