@@ -63,6 +63,7 @@ RKS_WORKLOADS = {
                      "C8H18 all-trans, B3LYP (VWN_RPA), 6-31G(d,p) Cartesian 210 AOs, CalChem Fine grid "
                      "(99 radial shells, pruned Lebedev, Becke) as judge, seeded S-orthonormal D (33 occ, seed 7)"),
 }
+CLUSTERS_AO_CACHE_CAP = 60 << 30  # the 64-cluster group's AO-cache cap (bytes)
 # DRAM bytes (read + write) per launch of the quadrature kernel from one ncu capture of the workload's
 # timed build (profiles/); absent until a capture exists for the workload and precision.  The 61-water
 # build is too large for a full capture: its figure is the 12-water capture (1.229 GB, 1.325 GB of AO
@@ -407,6 +408,11 @@ class _Work:
                                 f"Cartesian {basis.n_ao} AOs, Fine grid, seeded D (n_alpha {na}, n_beta {nb}, "
                                 f"seeds {SEED}/{SEED + 1})")
         elif name == "water_clusters_pbe":
+            # the group's AO cache would take ~150 GB at 32 B per AO and point: on a dedicated GB300
+            # the cap is raised to 60 GiB (within the grid's 64 GiB budget), and the batches whose
+            # blocks fit are cached (CALCHEM_MAX_AO_GRID_BYTES, read at the first tensor-core build)
+            os.environ.setdefault("CALCHEM_MAX_AO_GRID_BYTES", str(CLUSTERS_AO_CACHE_CAP))
+            self.grid_info["ao_cache_cap_bytes"] = int(os.environ["CALCHEM_MAX_AO_GRID_BYTES"])
             sizes = workloads.cluster_batch_sizes()
             members, dens, self.cluster_mols = [], [], []
             for i, k in enumerate(sizes):
