@@ -605,6 +605,11 @@ def run_ours(args):
     W.host_step()  # allocates the workspace (and fills the AO cache) outside the capture
     torch.cuda.synchronize()
     first_ms = (time.perf_counter() - t_first) * 1e3
+    if W.judge is not None:
+        # the judge's first check fills its own AO cache and the build's per-point share buffers,
+        # once per geometry as the build's first evaluation does: set-up, not a timed iteration
+        W.host_judge_step()
+        torch.cuda.synchronize()
     tile = W.tune()  # the tile is chosen before the capture, which keeps it
     if tile:
         W.grid_info["tile"] = tile
