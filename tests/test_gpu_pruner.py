@@ -83,7 +83,7 @@ def test_build_with_shares_matches_the_build_and_the_share_engine(lib, precision
     """evaluate_with_shares: the same Exc, Nelec and Vxc as evaluate (the tensor-core form: the same up
     to the rounding of grad rho, which plain builds sum by FP32 FMAs and builds with shares with
     compensation), and the same per-atom shares as a shares-only evaluation of the same points; the
-    judge gives the same verdict with them."""
+    judge reverts the same atoms with them."""
     mol = workloads.water_cluster(4, 6)
     basis = BasisSet.from_name("6-31g(d)", mol)
     D = workloads.seeded_density_rks(basis.overlap(), mol.nelectron() // 2, 9)

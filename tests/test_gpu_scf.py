@@ -49,7 +49,7 @@ def test_closed_shell_uks_matches_rks(lib, func):
 
 
 def test_mixed_learned_scf_energy_matches_fp64_fine(lib):
-    """The spec accuracy criterion: converged SCF energy of the mixed-precision build on the
+    """The accuracy criterion for the fast path: converged SCF energy of the mixed-precision build on the
     learned-pruned grid (judge every 5 iterations) within 1e-6 Eh of the FP64 Fine-grid SCF."""
     mol = workloads.water_cluster(2, 17)
     basis = BasisSet.from_name("6-31g(d)", mol)
@@ -64,7 +64,7 @@ def test_mixed_learned_scf_energy_matches_fp64_fine(lib):
 
 
 def test_octane_mixed_learned_scf_energy_matches_fp64_fine(lib, oracle):
-    """The spec accuracy criterion on the C8H18 benchmark molecule (B3LYP / 6-31G(d,p), 210 AOs,
+    """The fast path's accuracy criterion on the C8H18 benchmark molecule (B3LYP / 6-31G(d,p), 210 AOs,
     33 doubly occupied orbitals): the converged SCF energy with the tensor-core build on the learned
     grid (judge every 5 iterations) within 1e-6 Eh of the FP64 Fine-grid SCF; and the FP64 Fine
     SCF's first-iteration Exc (core-Hamiltonian guess density) against the oracle's CalChem
