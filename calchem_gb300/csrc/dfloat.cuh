@@ -96,6 +96,12 @@ __device__ __forceinline__ df32 df_sqrt(df32 a) {
 // Exact scaling by a power of two (as long as no underflow/overflow occurs).
 __device__ __forceinline__ df32 df_ldexp(df32 a, int e) { return df32{ldexpf(a.hi, e), ldexpf(a.lo, e)}; }
 
+// 2^k as a float: exact for -149 <= k <= 127 (a normal number for k >= -126).  x * pow2f(k) is then
+// x 2^k rounded once, as ldexpf(x, k) gives it.
+__device__ __forceinline__ float pow2f(int k) {
+  return (k >= -126 && k <= 127) ? __int_as_float((k + 127) << 23) : ldexpf(1.f, k);
+}
+
 // exp(-x) for x >= 0 given as a double-float, relative error ~1e-13 (before underflow).
 // Method: x = (64 k + j) ln2/64 + r with |r| <= ln2/128 (Cody-Waite reduction with ln2/64 split
 // into a 10-bit head, so n * head is exact, and two tails), exp(-r) from its Taylor series to

@@ -99,11 +99,6 @@ constexpr int kOffDensInStage = 65536;
 static_assert(24 + 8 * kRing + 8 <= 64, "misc area holds the barriers, the TMEM slot, the batch index and the planes' base");
 static_assert(64 + 8 * kRing <= 96, "the ring's release barriers follow at +64");
 
-// 2^k as a float: exact for -149 <= k <= 127 (a normal number for k >= -126)
-__device__ __forceinline__ float pow2f(int k) {
-  return (k >= -126 && k <= 127) ? __int_as_float((k + 127) << 23) : ldexpf(1.f, k);
-}
-
 // (double)x for a normal float x, by moving its sign, exponent and mantissa fields: the same value
 // as the conversion, with integer instructions only
 __device__ __forceinline__ double normal_f32_to_f64(float x) {
